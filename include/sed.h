@@ -1,0 +1,264 @@
+/*
+ * sed.h — C ABI of libsed, the GB300 (sm_103a) exact-diagonalisation engine.
+ *
+ * The `ls_*` entry points have the names, argument meanings and status
+ * convention of the lattice-symmetries C ABI that SpinED binds with
+ * `foreign import ccall` in src/SpinED/Internal.hs; each declaration cites the
+ * import it replaces. The `sed_*` entry points are additions: the device
+ * eigensolver that replaces Numeric.PRIMME.eigh (src/SpinED.hs:404) and
+ * device-resident variants of the matvec.
+ *
+ * Conventions
+ *  - Every function returning int returns 0 on success and a non-zero status
+ *    otherwise; ls_error_to_string() turns a status into a message that the
+ *    caller frees with ls_destroy_string() (Internal.hs:47-65).
+ *  - Handles are opaque and are written through an out-pointer
+ *    (Internal.hs:96-97). Destroy functions accept NULL, may run on any host
+ *    thread (they are GHC finalisers, Internal.hs:72-73) and never require a
+ *    current CUDA context or stream.
+ *  - x/y block arguments may be host memory (pageable or pinned) or device
+ *    memory of the current device; the library detects which. Blocks are
+ *    column-major with the given column strides (Internal.hs:411-429).
+ *  - dtype codes: 0 = float32, 1 = float64, 2 = complex64, 3 = complex128
+ *    (Internal.hs:404-409).
+ *  - A permutation p acts on a spin configuration x as y_i = x_{p[i]}; a
+ *    generator with periodicity n and sector k has eigenvalue exp(-2 pi i k/n);
+ *    representatives are orbit minima.
+ */
+#ifndef SED_H
+#define SED_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SED_API __attribute__((visibility("default")))
+#else
+#define SED_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ls_symmetry ls_symmetry;
+typedef struct ls_group ls_group;
+typedef struct ls_spin_basis ls_spin_basis;
+typedef struct ls_states ls_states;
+typedef struct ls_interaction ls_interaction;
+typedef struct ls_operator ls_operator;
+
+/* Status codes (values are part of the ABI). */
+enum {
+  LS_SUCCESS = 0,
+  LS_OUT_OF_MEMORY = 1,
+  LS_INVALID_ARGUMENT = 2,
+  LS_INVALID_HAMMING_WEIGHT = 3,
+  LS_INVALID_SPIN_INVERSION = 4,
+  LS_INVALID_NUMBER_SPINS = 5,
+  LS_INVALID_PERMUTATION = 6,
+  LS_INVALID_SECTOR = 7,
+  LS_INVALID_STATE = 8,
+  LS_INVALID_DATATYPE = 9,
+  LS_PERMUTATION_TOO_LONG = 10,
+  LS_INCOMPATIBLE_SYMMETRIES = 11,
+  LS_NOT_A_REPRESENTATIVE = 12,
+  LS_WRONG_BASIS_TYPE = 13,
+  LS_CACHE_NOT_BUILT = 14,
+  LS_COULD_NOT_OPEN_FILE = 15,
+  LS_FILE_IO_FAILED = 16,
+  LS_CACHE_IS_CORRUPT = 17,
+  LS_OPERATOR_IS_COMPLEX = 18,
+  LS_DIMENSION_MISMATCH = 19,
+  LS_GROUP_TOO_BIG = 20,
+  LS_CUDA_ERROR = 21,
+  LS_NOT_CONVERGED = 22,
+  LS_DEVICE_TIMEOUT = 23,
+  LS_SYSTEM_ERROR = 24,
+};
+
+/* --- errors and logging -------------------------------------------------- */
+
+/* Internal.hs:39. Returns a heap string; free it with ls_destroy_string. */
+SED_API char const* ls_error_to_string(int status);
+/* Internal.hs:41 */
+SED_API void ls_destroy_string(char const* message);
+/* Internal.hs:43 */
+SED_API void ls_enable_logging(void);
+/* Internal.hs:45 */
+SED_API void ls_disable_logging(void);
+
+/* --- symmetries (Internal.hs:67-116) ------------------------------------ */
+
+/* Internal.hs:69-70. Validates that `permutation` is a permutation of
+ * 0..length-1 (length <= 64) and that sector < periodicity. */
+SED_API int ls_create_symmetry(ls_symmetry** ptr, unsigned length, unsigned const permutation[],
+                       unsigned sector);
+/* Internal.hs:72-73 */
+SED_API void ls_destroy_symmetry(ls_symmetry* symmetry);
+/* Internal.hs:75 */
+SED_API unsigned ls_get_sector(ls_symmetry const* symmetry);
+/* Internal.hs:77. Returns sector / periodicity. */
+SED_API double ls_get_phase(ls_symmetry const* symmetry);
+/* Internal.hs:79 */
+SED_API unsigned ls_get_periodicity(ls_symmetry const* symmetry);
+
+/* --- groups (Internal.hs:118-155) ---------------------------------------- */
+
+/* Internal.hs:120-121. Closure of the generators; fails with
+ * LS_INCOMPATIBLE_SYMMETRIES when two products give the same permutation
+ * with different characters. Zero generators give the trivial group. */
+SED_API int ls_create_group(ls_group** ptr, unsigned size, ls_symmetry const* generators[]);
+/* Internal.hs:123-124 */
+SED_API void ls_destroy_group(ls_group* group);
+/* Internal.hs:126-127. Number of permutations (spin inversion not counted). */
+SED_API unsigned ls_get_group_size(ls_group const* group);
+
+/* --- spin basis (Internal.hs:157-254) ------------------------------------ */
+
+/* Internal.hs:172-173. hamming_weight = -1 for no restriction; spin_inversion
+ * in {-1, 0, +1}, 0 meaning none. */
+SED_API int ls_create_spin_basis(ls_spin_basis** ptr, ls_group const* group, unsigned number_spins,
+                         int hamming_weight, int spin_inversion);
+/* Internal.hs:175-176 */
+SED_API void ls_destroy_spin_basis(ls_spin_basis* basis);
+/* Internal.hs:178-179. Enumerates the representatives on the GPU. */
+SED_API int ls_build(ls_spin_basis* basis);
+/* Internal.hs:181-182. Installs a caller-supplied sorted representative list
+ * (host or device memory); norms are recomputed on the GPU. */
+SED_API int ls_build_unsafe(ls_spin_basis* basis, uint64_t size, uint64_t const representatives[]);
+/* Internal.hs:184-185 */
+SED_API int ls_get_number_states(ls_spin_basis const* basis, uint64_t* out);
+/* Internal.hs:187-188. Copies the representatives into host memory owned by
+ * the returned states object. */
+SED_API int ls_get_states(ls_states** ptr, ls_spin_basis const* basis);
+/* Internal.hs:190-191. Host pointer, valid until ls_destroy_states. */
+SED_API uint64_t const* ls_states_get_data(ls_states const* states);
+/* Internal.hs:193-194 */
+SED_API uint64_t ls_states_get_size(ls_states const* states);
+/* Internal.hs:196-197 */
+SED_API void ls_destroy_states(ls_states* states);
+
+/* --- interactions (Internal.hs:256-367) ---------------------------------- */
+
+/* Internal.hs:260-270. matrix: 2^k x 2^k complex128, row-major, interleaved
+ * (re, im); sites: number_nodes tuples of k uint16 site indices. For a tuple
+ * (i_0, ..., i_{k-1}) the local index is sum_m bit(i_m) << (k-1-m). */
+SED_API int ls_create_interaction1(ls_interaction** ptr, void const* matrix, unsigned number_nodes,
+                           uint16_t const* nodes);
+SED_API int ls_create_interaction2(ls_interaction** ptr, void const* matrix, unsigned number_nodes,
+                           uint16_t const* nodes);
+SED_API int ls_create_interaction3(ls_interaction** ptr, void const* matrix, unsigned number_nodes,
+                           uint16_t const* nodes);
+SED_API int ls_create_interaction4(ls_interaction** ptr, void const* matrix, unsigned number_nodes,
+                           uint16_t const* nodes);
+/* Internal.hs:272-273 */
+SED_API bool ls_interaction_is_real(ls_interaction const* interaction);
+/* Internal.hs:275-276 */
+SED_API void ls_destroy_interaction(ls_interaction* interaction);
+
+/* --- operators (Internal.hs:369-458) ------------------------------------- */
+
+/* Internal.hs:371-372. Binds the terms to a basis (built now or later, as
+ * SpinED builds representatives after creating operators, Main.hs:19-22);
+ * sites must be below number_spins and distinct within a tuple. */
+SED_API int ls_create_operator(ls_operator** ptr, ls_spin_basis const* basis, unsigned number_terms,
+                       ls_interaction const* const terms[]);
+/* Internal.hs:374-375 */
+SED_API void ls_destroy_operator(ls_operator* op);
+/* Internal.hs:377-378. Y = H X for `block_size` columns of length `size`. */
+SED_API int ls_operator_matmat(ls_operator const* op, int dtype, uint64_t size, uint64_t block_size,
+                       void const* x, uint64_t x_stride, void* y, uint64_t y_stride);
+/* Internal.hs:380-381. out[c] = <x_c|H|x_c> as complex128 (interleaved). */
+SED_API int ls_operator_expectation(ls_operator const* op, int dtype, uint64_t size, uint64_t block_size,
+                            void const* x, uint64_t x_stride, void* out);
+/* Internal.hs:383-384. True iff every term is real and every character of the
+ * sector is real. */
+SED_API bool ls_operator_is_real(ls_operator const* op);
+
+/* --- additions: device eigensolver and device-resident forms ------------- */
+
+/* Matvec forms. SED_FORM_STREAM records (column, value code) once and then
+ * streams it (an HBM-bound SpMV); SED_FORM_ON_THE_FLY regenerates every
+ * element each call. SED_FORM_AUTO streams when the recorded form fits. */
+enum { SED_FORM_AUTO = 0, SED_FORM_STREAM = 1, SED_FORM_ON_THE_FLY = 2 };
+/* Krylov storage/arithmetic: plain FP64, or FP32-stored vectors for the bulk
+ * of the iterations followed by an FP64 refinement. */
+enum { SED_PRECISION_FP64 = 0, SED_PRECISION_MIXED = 1 };
+/* Start vector: Philox4x32-10 uniform [-1, 1) from `seed`, or the caller's
+ * vector(s) in `start`. */
+enum { SED_START_RANDOM = 0, SED_START_GIVEN = 1 };
+
+typedef void (*sed_progress_fn)(void* user, uint64_t iteration, double const* ritz_values,
+                                double const* residual_estimates, unsigned count);
+
+typedef struct sed_eigh_options {
+  uint32_t struct_size;      /* sizeof(sed_eigh_options) */
+  uint32_t nev;              /* number of lowest eigenpairs (number_vectors) */
+  double tol;                /* ||H psi - E psi|| bound; <= 0 means 1e-8 */
+  uint32_t max_iter;         /* Lanczos steps in total; 0 means 100000 */
+  uint32_t max_basis;        /* stored Krylov vectors per cycle; 0 = auto */
+  uint32_t block_size;       /* 1 = single-vector Lanczos */
+  uint32_t precision;        /* SED_PRECISION_* */
+  uint32_t start;            /* SED_START_* */
+  uint32_t form;             /* SED_FORM_* */
+  uint64_t seed;             /* Philox key for SED_START_RANDOM */
+  void const* start_vectors; /* column-major, size x block_size, host or device */
+  uint64_t start_stride;
+  sed_progress_fn progress;  /* may be NULL; called between iterations */
+  void* progress_user;
+} sed_eigh_options;
+
+typedef struct sed_eigh_info {
+  uint64_t iterations;       /* Lanczos steps (all phases) */
+  uint64_t matvecs;
+  uint64_t restarts;
+  uint64_t fp32_iterations;  /* steps taken with FP32-stored vectors */
+  double seconds_total;
+  double seconds_setup;      /* recording the stream form */
+  double seconds_solve;
+} sed_eigh_info;
+
+/* Fills `opts` with defaults (nev 1, tol 1e-8, FP64, random seed 1234). */
+SED_API void sed_eigh_options_init(sed_eigh_options* opts);
+
+/* Replaces Numeric.PRIMME.eigh at src/SpinED.hs:404: lowest `opts->nev`
+ * eigenpairs of `op`. eigenvalues[nev] and residuals[nev] are host arrays;
+ * eigenvectors is size x nev, column-major with stride ldv, host or device,
+ * of `dtype`; residuals are ||H psi - E psi|| of the returned unit vectors
+ * recomputed in FP64 at the end. `info` may be NULL. */
+SED_API int sed_eigh(ls_operator const* op, int dtype, sed_eigh_options const* opts, double* eigenvalues,
+             void* eigenvectors, uint64_t ldv, double* residuals, sed_eigh_info* info);
+
+/* Selects the matvec form of the operator for later calls (ls_operator_matmat,
+ * sed_eigh with SED_FORM_AUTO); SED_FORM_STREAM and SED_FORM_AUTO record the
+ * stream form now (AUTO silently keeps on-the-fly if it does not fit). */
+SED_API int sed_operator_prepare(ls_operator* op, int form);
+/* Bytes the stream form occupies on the device (0 if not recorded). */
+SED_API uint64_t sed_operator_stream_bytes(ls_operator const* op);
+/* Stored elements of the stream form (off-diagonal, per matvec). */
+SED_API uint64_t sed_operator_stream_elements(ls_operator const* op);
+
+/* Y = H X on device pointers, enqueued on `stream` (a cudaStream_t, or NULL
+ * for the operator's own stream); returns without synchronising. */
+SED_API int sed_operator_matmat_device(ls_operator const* op, int dtype, uint64_t size,
+                               uint64_t block_size, void const* x, uint64_t x_stride, void* y,
+                               uint64_t y_stride, void* stream);
+
+/* Norms ||P r|| = sqrt(S / |G|) of the representatives (host array). */
+SED_API int sed_basis_get_norms(ls_spin_basis const* basis, double* out);
+/* Device pointer to the representatives (valid while the basis lives). */
+SED_API uint64_t const* sed_basis_device_states(ls_spin_basis const* basis);
+/* Index of a representative, or LS_NOT_A_REPRESENTATIVE. */
+SED_API int sed_basis_index(ls_spin_basis const* basis, uint64_t representative, uint64_t* index);
+/* Orbit minimum and character phase (numerator of exp(-2 pi i phase / L)). */
+SED_API int sed_basis_state_info(ls_spin_basis const* basis, uint64_t bits, uint64_t* representative,
+                         unsigned* phase, unsigned* phase_modulus);
+
+/* Version string of the library (static storage). */
+SED_API char const* sed_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,517 @@
+// basis.cu — symmetry-adapted spin basis: construction, representative
+// enumeration on the GPU, export (src/SpinED/Internal.hs:157-254).
+//
+// ls_build enumerates every word of the fixed-Hamming-weight space (or all
+// 2^n words) in increasing order and keeps the orbit minima whose stabiliser
+// carries the trivial character. Three passes keep the output sorted without
+// any sort:
+//   1. mark:  one thread per 32 consecutive words (unranked once, then the
+//             next word of equal weight) writes a 32-bit mask of the words that
+//             are representatives;
+//   2. scan:  per-tile popcounts, an exclusive scan over tiles;
+//   3. write: each tile re-walks its marked words and writes them, with their
+//             stabiliser orders, at the scanned offsets.
+// A prefix table over the top bits of the representatives then serves the
+// index lookups of the matvec.
+#include <algorithm>
+#include <cstring>
+
+#include "sed_internal.hpp"
+
+namespace sed {
+namespace {
+
+constexpr unsigned kThreads = 256;
+constexpr unsigned kTileWords = kThreads * 8;  // bitmap words per tile
+
+template <class W>
+__global__ void k_mark(PlanView P, uint64_t const* __restrict__ binom, unsigned n, int hw,
+                       uint64_t space, uint64_t n_words, uint32_t* __restrict__ bitmap) {
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_words;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t const r0 = t * 32;
+    unsigned const count = (unsigned)min((uint64_t)32, space - r0);
+    uint64_t x = unrank_word(r0, n, hw, binom);
+    uint32_t mask = 0;
+    for (unsigned k = 0; k < count; ++k) {
+      if (representative_weight<W>((W)x, P)) mask |= 1u << k;
+      if (k + 1 < count) x = hw >= 0 ? next_same_weight(x) : x + 1;
+    }
+    bitmap[t] = mask;
+  }
+}
+
+__global__ void k_tile_counts(uint32_t const* __restrict__ bitmap, uint64_t n_words,
+                              uint64_t* __restrict__ tile_count) {
+  __shared__ uint64_t part[kThreads / 32];
+  uint64_t const base = (uint64_t)blockIdx.x * kTileWords;
+  uint64_t c = 0;
+  for (unsigned j = 0; j < 8; ++j) {
+    uint64_t const w = base + (uint64_t)j * kThreads + threadIdx.x;
+    if (w < n_words) c += __popc(bitmap[w]);
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t s = 0;
+    for (unsigned i = 0; i < kThreads / 32; ++i) s += part[i];
+    tile_count[blockIdx.x] = s;
+  }
+}
+
+// Exclusive scan of n values in place by one block; out[n] = total.
+__global__ void k_scan_serial(uint64_t* __restrict__ v, uint64_t n) {
+  __shared__ uint64_t sums[1024];
+  unsigned const T = blockDim.x;
+  uint64_t const per = (n + T - 1) / T;
+  uint64_t const b = min(n, (uint64_t)threadIdx.x * per), e = min(n, b + per);
+  uint64_t s = 0;
+  for (uint64_t i = b; i < e; ++i) s += v[i];
+  sums[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t acc = 0;
+    for (unsigned i = 0; i < T; ++i) {
+      uint64_t const t = sums[i];
+      sums[i] = acc;
+      acc += t;
+    }
+    v[n] = acc;
+  }
+  __syncthreads();
+  uint64_t acc = sums[threadIdx.x];
+  for (uint64_t i = b; i < e; ++i) {
+    uint64_t const t = v[i];
+    v[i] = acc;
+    acc += t;
+  }
+}
+
+template <class W>
+__global__ void k_write(PlanView P, uint64_t const* __restrict__ binom, unsigned n, int hw,
+                        uint64_t space, uint32_t const* __restrict__ bitmap, uint64_t n_words,
+                        uint64_t const* __restrict__ tile_offset, uint64_t* __restrict__ reps,
+                        uint32_t* __restrict__ weights) {
+  __shared__ uint32_t scan[kThreads];
+  uint64_t const w0 = (uint64_t)blockIdx.x * kTileWords + (uint64_t)threadIdx.x * 8;
+  uint32_t m[8];
+  uint32_t c = 0;
+  for (unsigned j = 0; j < 8; ++j) {
+    m[j] = (w0 + j < n_words) ? bitmap[w0 + j] : 0u;
+    c += __popc(m[j]);
+  }
+  scan[threadIdx.x] = c;
+  __syncthreads();
+  for (unsigned o = 1; o < kThreads; o <<= 1) {
+    uint32_t const v = threadIdx.x >= o ? scan[threadIdx.x - o] : 0u;
+    __syncthreads();
+    scan[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint64_t pos = tile_offset[blockIdx.x] + scan[threadIdx.x] - c;
+  for (unsigned j = 0; j < 8; ++j) {
+    if (!m[j]) continue;
+    uint64_t const r0 = (w0 + j) * 32;
+    unsigned const count = (unsigned)min((uint64_t)32, space - r0);
+    uint64_t x = unrank_word(r0, n, hw, binom);
+    for (unsigned k = 0; k < count; ++k) {
+      if (m[j] >> k & 1u) {
+        reps[pos] = x;
+        weights[pos] = representative_weight<W>((W)x, P);
+        ++pos;
+      }
+      if (k + 1 < count) x = hw >= 0 ? next_same_weight(x) : x + 1;
+    }
+  }
+}
+
+template <class W>
+__global__ void k_check_reps(PlanView P, uint64_t const* __restrict__ reps, uint64_t D,
+                             uint32_t* __restrict__ weights, unsigned n, int hw,
+                             uint32_t* __restrict__ bad) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t const x = reps[i];
+    uint32_t w = 0;
+    bool ok = (n == 64 || (x >> n) == 0) && (hw < 0 || __popcll(x) == hw);
+    if (ok) w = representative_weight<W>((W)x, P);
+    if (i + 1 < D && reps[i + 1] <= x) ok = false;
+    weights[i] = w;
+    if (!ok || w == 0) bad[0] = 1u;  // any writer stores the same value
+  }
+}
+
+__global__ void k_prefix(uint64_t const* __restrict__ reps, uint64_t D, unsigned shift,
+                         uint64_t n_keys, uint64_t* __restrict__ prefix) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k <= n_keys;
+       k += (uint64_t)gridDim.x * blockDim.x) {
+    if (k == n_keys) {
+      prefix[k] = D;
+      continue;
+    }
+    uint64_t const key = k << shift;
+    uint64_t lo = 0, hi = D;
+    while (lo < hi) {
+      uint64_t const mid = (lo + hi) >> 1;
+      if (reps[mid] < key)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    prefix[k] = lo;
+  }
+}
+
+unsigned grid_for(uint64_t work, int device) {
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  uint64_t const want = (work + kThreads - 1) / kThreads;
+  uint64_t const cap = (uint64_t)sms * 16;
+  return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+}  // namespace
+
+int basis_upload_plan(BasisData& b, cudaStream_t stream) {
+  if (b.plan_buf.ptr) return LS_SUCCESS;
+  SymPlanHost const& p = b.plan;
+  size_t const sz_bm = p.benes_mask.size() * 8, sz_bs = p.benes_shift.size() * 4;
+  size_t const sz_hm = p.h_mask.size() * 8, sz_hr = p.h_rot.size() * 4;
+  size_t const sz_cp = p.coset_phase.size() * 4, sz_hp = p.h_phase.size() * 4;
+  auto align = [](size_t v) { return (v + 15) & ~(size_t)15; };
+  size_t const total = align(sz_bm) + align(sz_bs) + align(sz_hm) + align(sz_hr) + align(sz_cp) +
+                       align(sz_hp) + 16;
+  std::vector<uint8_t> host(total, 0);
+  size_t off = 0;
+  PlanView v = p.view();
+  auto put = [&](void const* src, size_t n) {
+    std::memcpy(host.data() + off, src, n);
+    size_t const at = off;
+    off += align(n);
+    return at;
+  };
+  size_t const o_bm = put(p.benes_mask.data(), sz_bm), o_bs = put(p.benes_shift.data(), sz_bs);
+  size_t const o_hm = put(p.h_mask.data(), sz_hm), o_hr = put(p.h_rot.data(), sz_hr);
+  size_t const o_cp = put(p.coset_phase.data(), sz_cp), o_hp = put(p.h_phase.data(), sz_hp);
+  if (int st = b.plan_buf.allocate(total)) return st;
+  SED_TRY_CUDA(cudaMemcpyAsync(b.plan_buf.ptr, host.data(), total, cudaMemcpyHostToDevice, stream));
+  uint8_t* base = b.plan_buf.as<uint8_t>();
+  v.benes_mask = (uint64_t const*)(base + o_bm);
+  v.benes_shift = (uint32_t const*)(base + o_bs);
+  v.h_mask = (uint64_t const*)(base + o_hm);
+  v.h_rot = (uint32_t const*)(base + o_hr);
+  v.coset_phase = (uint32_t const*)(base + o_cp);
+  v.h_phase = (uint32_t const*)(base + o_hp);
+  b.plan_dev = v;
+  std::vector<uint64_t> binom(65 * 65, 0);
+  for (unsigned i = 0; i <= 64; ++i) {
+    binom[i * 65] = 1;
+    for (unsigned j = 1; j <= 64; ++j)
+      binom[i * 65 + j] = i == 0 ? 0 : binom[(i - 1) * 65 + j - 1] + binom[(i - 1) * 65 + j];
+  }
+  if (int st = b.binom.allocate(binom.size() * 8)) return st;
+  SED_TRY_CUDA(cudaMemcpyAsync(b.binom.ptr, binom.data(), binom.size() * 8, cudaMemcpyHostToDevice, stream));
+  SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  return LS_SUCCESS;
+}
+
+IndexView BasisData::index_view() const {
+  IndexView I{};
+  I.reps = reps.as<uint64_t const>();
+  I.prefix = prefix.as<uint64_t const>();
+  I.D = D;
+  I.bits = prefix_bits;
+  I.shift = prefix_shift;
+  return I;
+}
+
+int basis_build_index(BasisData& b, cudaStream_t stream) {
+  uint64_t max_rep = 0;
+  if (b.D) SED_TRY_CUDA(cudaMemcpy(&max_rep, b.reps.as<uint64_t>() + b.D - 1, 8, cudaMemcpyDeviceToHost));
+  unsigned bitlen = 0;
+  while (bitlen < 64 && (max_rep >> bitlen)) ++bitlen;
+  unsigned want = 1;
+  while (want < 26 && ((uint64_t)1 << want) < b.D) ++want;  // about one key per entry
+  b.prefix_bits = std::max(1u, std::min(bitlen ? bitlen : 1u, want));
+  b.prefix_shift = bitlen > b.prefix_bits ? bitlen - b.prefix_bits : 0;
+  uint64_t const n_keys = (uint64_t)1 << b.prefix_bits;
+  if (int st = b.prefix.allocate((n_keys + 1) * 8)) return st;
+  k_prefix<<<grid_for(n_keys + 1, b.device), kThreads, 0, stream>>>(
+      b.reps.as<uint64_t>(), b.D, b.prefix_shift, n_keys, b.prefix.as<uint64_t>());
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
+namespace {
+
+int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
+  if (b.device < 0 || !b.plan_buf.ptr)
+    if (int st = current_device(&b.device)) return st;
+  ScopedDevice dev(b.device);
+  cudaStream_t stream;
+  SED_TRY_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } guard{stream};
+  if (int st = basis_upload_plan(b, stream)) return st;
+  bool const wide = b.plan.n_bits > 32;
+  PlanView const P = b.plan_dev;
+  b.built = false;
+  b.reps.reset();
+  b.weights.reset();
+  b.prefix.reset();
+  if (given) {
+    b.D = given_size;
+    if (int st = b.reps.allocate(std::max<uint64_t>(1, given_size) * 8)) return st;
+    if (int st = b.weights.allocate(std::max<uint64_t>(1, given_size) * 4)) return st;
+    if (given_size)
+      SED_TRY_CUDA(cudaMemcpyAsync(b.reps.ptr, given, given_size * 8, cudaMemcpyDefault, stream));
+    DeviceBuffer bad;
+    if (int st = bad.allocate(4)) return st;
+    SED_TRY_CUDA(cudaMemsetAsync(bad.ptr, 0, 4, stream));
+    if (given_size) {
+      unsigned const grid = grid_for(given_size, b.device);
+      if (wide)
+        k_check_reps<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), given_size,
+                                                             b.weights.as<uint32_t>(), b.n, b.hw,
+                                                             bad.as<uint32_t>());
+      else
+        k_check_reps<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), given_size,
+                                                             b.weights.as<uint32_t>(), b.n, b.hw,
+                                                             bad.as<uint32_t>());
+      SED_TRY_CUDA(cudaGetLastError());
+    }
+    uint32_t bad_h = 0;
+    SED_TRY_CUDA(cudaMemcpyAsync(&bad_h, bad.ptr, 4, cudaMemcpyDeviceToHost, stream));
+    SED_TRY_CUDA(cudaStreamSynchronize(stream));
+    if (bad_h)
+      return fail(LS_NOT_A_REPRESENTATIVE,
+                  "ls_build_unsafe: the list is not a strictly increasing list of representatives "
+                  "of this sector");
+  } else {
+    // Space size.
+    uint64_t space;
+    if (b.hw >= 0) {
+      uint64_t row[65] = {1};
+      for (unsigned i = 1; i <= b.n; ++i)
+        for (unsigned j = i; j >= 1; --j) row[j] += row[j - 1];  // Pascal row n
+      space = row[b.hw];
+    } else {
+      if (b.n >= 48) return fail(LS_OUT_OF_MEMORY, "ls_build: 2^n words do not fit the device");
+      space = (uint64_t)1 << b.n;
+    }
+    uint64_t const n_words = (space + 31) / 32;
+    uint64_t const n_tiles = (n_words + kTileWords - 1) / kTileWords;
+    DeviceBuffer bitmap, tiles;
+    if (int st = bitmap.allocate(std::max<uint64_t>(1, n_words) * 4)) return st;
+    if (int st = tiles.allocate((n_tiles + 1) * 8)) return st;
+    unsigned const grid = grid_for(n_words, b.device) * 4;
+    if (wide)
+      k_mark<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
+                                                       n_words, bitmap.as<uint32_t>());
+    else
+      k_mark<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
+                                                       n_words, bitmap.as<uint32_t>());
+    SED_TRY_CUDA(cudaGetLastError());
+    if (n_tiles) {
+      k_tile_counts<<<(unsigned)n_tiles, kThreads, 0, stream>>>(bitmap.as<uint32_t>(), n_words,
+                                                                tiles.as<uint64_t>());
+      SED_TRY_CUDA(cudaGetLastError());
+    }
+    k_scan_serial<<<1, 1024, 0, stream>>>(tiles.as<uint64_t>(), n_tiles);
+    SED_TRY_CUDA(cudaGetLastError());
+    uint64_t D = 0;
+    SED_TRY_CUDA(cudaMemcpyAsync(&D, tiles.as<uint64_t>() + n_tiles, 8, cudaMemcpyDeviceToHost, stream));
+    SED_TRY_CUDA(cudaStreamSynchronize(stream));
+    b.D = D;
+    if (int st = b.reps.allocate(std::max<uint64_t>(1, D) * 8)) return st;
+    if (int st = b.weights.allocate(std::max<uint64_t>(1, D) * 4)) return st;
+    if (n_tiles) {
+      if (wide)
+        k_write<uint64_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
+            P, b.binom.as<uint64_t>(), b.n, b.hw, space, bitmap.as<uint32_t>(), n_words,
+            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>());
+      else
+        k_write<uint32_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
+            P, b.binom.as<uint64_t>(), b.n, b.hw, space, bitmap.as<uint32_t>(), n_words,
+            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>());
+      SED_TRY_CUDA(cudaGetLastError());
+    }
+    SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  }
+  if (int st = basis_build_index(b, stream)) return st;
+  SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  b.built = true;
+  if (logging_enabled()) log_line("basis built: %llu representatives", (unsigned long long)b.D);
+  return LS_SUCCESS;
+}
+
+}  // namespace
+
+bool characters_real(BasisData const& b) {
+  for (uint32_t ph : b.plan.coset_phase)
+    if ((2 * ph) % b.plan.L) return false;
+  for (uint32_t ph : b.plan.h_phase)
+    if ((2 * ph) % b.plan.L) return false;
+  return true;
+}
+
+}  // namespace sed
+
+using namespace sed;
+
+extern "C" {
+
+int ls_create_spin_basis(ls_spin_basis** ptr, ls_group const* group, unsigned number_spins,
+                         int hamming_weight, int spin_inversion) {
+  if (!ptr || !group) return fail(LS_INVALID_ARGUMENT, "ls_create_spin_basis: NULL argument");
+  if (number_spins == 0 || number_spins > 64)
+    return fail(LS_INVALID_NUMBER_SPINS, "number of spins must be in 1..64, got " + std::to_string(number_spins));
+  if (group->d.n && group->d.n != number_spins)
+    return fail(LS_INVALID_NUMBER_SPINS, "symmetries act on " + std::to_string(group->d.n) +
+                                             " sites but the basis has " + std::to_string(number_spins));
+  if (hamming_weight < -1 || hamming_weight > (int)number_spins)
+    return fail(LS_INVALID_HAMMING_WEIGHT, "Hamming weight must be -1 or in 0..number_spins");
+  if (spin_inversion < -1 || spin_inversion > 1)
+    return fail(LS_INVALID_SPIN_INVERSION, "spin inversion must be -1, 0 or +1");
+  if (spin_inversion != 0 && hamming_weight != -1 && 2 * hamming_weight != (int)number_spins)
+    return fail(LS_INVALID_SPIN_INVERSION,
+                "spin inversion needs Hamming weight number_spins / 2 (or no Hamming weight)");
+  try {
+    auto d = std::make_shared<BasisData>();
+    d->n = number_spins;
+    d->hw = hamming_weight;
+    d->inv = spin_inversion;
+    d->group = group->d;
+    if (int st = build_plan(d->group, number_spins, spin_inversion, d->plan)) return st;
+    d->device = -1;  // bound to the current device by ls_build
+    auto* b = new ls_spin_basis;
+    b->d = std::move(d);
+    *ptr = b;
+    return LS_SUCCESS;
+  } catch (std::bad_alloc const&) {
+    return fail(LS_OUT_OF_MEMORY, "ls_create_spin_basis");
+  } catch (std::exception const& e) {
+    return fail(LS_SYSTEM_ERROR, e.what());
+  }
+}
+
+void ls_destroy_spin_basis(ls_spin_basis* basis) { delete basis; }
+
+int ls_build(ls_spin_basis* basis) {
+  if (!basis) return fail(LS_INVALID_ARGUMENT, "ls_build: NULL basis");
+  std::lock_guard<std::mutex> lock(basis->d->mu);
+  try {
+    return build_impl(*basis->d, nullptr, 0);
+  } catch (std::exception const& e) {
+    return fail(LS_SYSTEM_ERROR, e.what());
+  }
+}
+
+int ls_build_unsafe(ls_spin_basis* basis, uint64_t size, uint64_t const representatives[]) {
+  if (!basis || (size && !representatives)) return fail(LS_INVALID_ARGUMENT, "ls_build_unsafe: NULL argument");
+  std::lock_guard<std::mutex> lock(basis->d->mu);
+  try {
+    return build_impl(*basis->d, representatives, size);
+  } catch (std::exception const& e) {
+    return fail(LS_SYSTEM_ERROR, e.what());
+  }
+}
+
+int ls_get_number_states(ls_spin_basis const* basis, uint64_t* out) {
+  if (!basis || !out) return fail(LS_INVALID_ARGUMENT, "ls_get_number_states: NULL argument");
+  if (!basis->d->built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  *out = basis->d->D;
+  return LS_SUCCESS;
+}
+
+int ls_get_states(ls_states** ptr, ls_spin_basis const* basis) {
+  if (!ptr || !basis) return fail(LS_INVALID_ARGUMENT, "ls_get_states: NULL argument");
+  BasisData& b = *basis->d;
+  if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  try {
+    auto* s = new ls_states;
+    s->data.resize(b.D);
+    ScopedDevice dev(b.device);
+    if (b.D) {
+      cudaError_t e = cudaMemcpy(s->data.data(), b.reps.ptr, b.D * 8, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) {
+        delete s;
+        return fail(LS_CUDA_ERROR, std::string("ls_get_states: ") + cudaGetErrorString(e));
+      }
+    }
+    *ptr = s;
+    return LS_SUCCESS;
+  } catch (std::bad_alloc const&) {
+    return fail(LS_OUT_OF_MEMORY, "ls_get_states");
+  }
+}
+
+uint64_t const* ls_states_get_data(ls_states const* states) {
+  return states ? states->data.data() : nullptr;
+}
+uint64_t ls_states_get_size(ls_states const* states) { return states ? states->data.size() : 0; }
+void ls_destroy_states(ls_states* states) { delete states; }
+
+int sed_basis_get_norms(ls_spin_basis const* basis, double* out) {
+  if (!basis || !out) return fail(LS_INVALID_ARGUMENT, "sed_basis_get_norms: NULL argument");
+  BasisData& b = *basis->d;
+  if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  std::vector<uint32_t> w(b.D);
+  ScopedDevice dev(b.device);
+  if (b.D) SED_TRY_CUDA(cudaMemcpy(w.data(), b.weights.ptr, b.D * 4, cudaMemcpyDeviceToHost));
+  double const G = (double)b.plan.group_order;
+  for (uint64_t i = 0; i < b.D; ++i) out[i] = std::sqrt((double)w[i] / G);
+  return LS_SUCCESS;
+}
+
+uint64_t const* sed_basis_device_states(ls_spin_basis const* basis) {
+  return (basis && basis->d->built) ? basis->d->reps.as<uint64_t const>() : nullptr;
+}
+
+int sed_basis_state_info(ls_spin_basis const* basis, uint64_t bits, uint64_t* representative,
+                         unsigned* phase, unsigned* modulus) {
+  if (!basis || !representative) return fail(LS_INVALID_ARGUMENT, "sed_basis_state_info: NULL argument");
+  BasisData const& b = *basis->d;
+  if (b.n < 64 && (bits >> b.n)) return fail(LS_INVALID_STATE, "state has bits above number_spins");
+  PlanView const P = b.plan.view();
+  uint64_t rep;
+  uint32_t ph;
+  if (b.plan.n_bits > 32) {
+    auto c = canonicalize<uint64_t>(bits, P);
+    rep = c.rep;
+    ph = c.phase;
+  } else {
+    auto c = canonicalize<uint32_t>((uint32_t)bits, P);
+    rep = c.rep;
+    ph = c.phase;
+  }
+  *representative = rep;
+  if (phase) *phase = ph;
+  if (modulus) *modulus = b.plan.L;
+  return LS_SUCCESS;
+}
+
+int sed_basis_index(ls_spin_basis const* basis, uint64_t representative, uint64_t* index) {
+  if (!basis || !index) return fail(LS_INVALID_ARGUMENT, "sed_basis_index: NULL argument");
+  BasisData& b = *basis->d;
+  if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  // Host-side binary search over a copy of the bracketing prefix entries.
+  ScopedDevice dev(b.device);
+  uint64_t const key = representative >> b.prefix_shift;
+  if (key >= ((uint64_t)1 << b.prefix_bits)) return LS_NOT_A_REPRESENTATIVE;
+  uint64_t range[2];
+  SED_TRY_CUDA(cudaMemcpy(range, b.prefix.as<uint64_t>() + key, 16, cudaMemcpyDeviceToHost));
+  std::vector<uint64_t> slice(range[1] - range[0]);
+  if (!slice.empty())
+    SED_TRY_CUDA(cudaMemcpy(slice.data(), b.reps.as<uint64_t>() + range[0], slice.size() * 8,
+                            cudaMemcpyDeviceToHost));
+  auto it = std::lower_bound(slice.begin(), slice.end(), representative);
+  if (it == slice.end() || *it != representative) return LS_NOT_A_REPRESENTATIVE;
+  *index = range[0] + (uint64_t)(it - slice.begin());
+  return LS_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,832 @@
+// operator.cu — interactions, operators and the symmetry-adapted matvec
+// (src/SpinED/Internal.hs:256-458).
+//
+// Pull form, atomic-free: row i (representative r_i) owns y_i and sums
+//     y_i = diag(r_i) x_i + (1/sqrt(S_i)) sum_e V[code_e] x_{j_e}
+// over the off-diagonal elements e of the local terms: s_e = r_i with the
+// bits of one site tuple replaced (a -> a'), coefficient <r_i|H|s_e> =
+// M[a][a'], rho_e = orbit minimum of s_e with character chi_e, j_e = index of
+// rho_e, and V[code] = M[a][a'] chi_e sqrt(S_{j_e}). This is
+// <r~_i|H|r~_j> = sum_s <r_i|H|s> chi(h_s) n_j / n_i with n = sqrt(S / |G|),
+// which holds for any G-invariant H (no Hermiticity needed).
+//
+// Two forms compute the same sum in the same order, so they agree bit for
+// bit:
+//   on-the-fly  canonicalises every s_e per call (integer-bound);
+//   stream      records (j_e, code_e) once in SELL-32 slices (32 rows per
+//               warp, slot e of row lane at slice_ptr + 32 e + lane) and then
+//               streams it: an HBM/FP64-bound SpMV.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+
+#include "operator_impl.cuh"
+
+namespace sed {
+namespace {
+
+// ---------------------------------------------------------------- kernels --
+
+// Per-slice maximum element count (slots = 32 * max) and element total.
+__global__ void k_count(uint64_t const* __restrict__ reps, uint64_t D, TermsView T,
+                        uint64_t n_slices, uint64_t* __restrict__ slots,
+                        uint64_t* __restrict__ elements) {
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  if (s >= n_slices) return;
+  uint32_t const c = i < D ? row_count(reps[i], T) : 0u;
+  uint32_t const m = __reduce_max_sync(0xffffffffu, c);
+  uint32_t const tot = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0) {
+    slots[s] = (uint64_t)m * 32;
+    elements[s] = tot;
+  }
+}
+
+template <class W, bool Real>
+__global__ void k_record(PlanView P, IndexView I, TermsView T, CodeView C,
+                         uint32_t const* __restrict__ weights, uint64_t n_slices,
+                         uint64_t const* __restrict__ slice_ptr, uint32_t col_bits, bool packed,
+                         uint32_t* __restrict__ entries, uint16_t* __restrict__ codes,
+                         void* __restrict__ diag, uint8_t* __restrict__ row_class) {
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  if (s >= n_slices) return;
+  uint32_t const lane = threadIdx.x & 31;
+  uint64_t const base = slice_ptr[s];
+  uint32_t const width = (uint32_t)((slice_ptr[s + 1] - base) >> 5);
+  uint32_t used = 0;
+  if (i < I.D) {
+    uint64_t const r = I.reps[i];
+    walk_row(r, T, [&](uint32_t e, uint64_t st, uint32_t vid) {
+      auto const c = canonicalize<W>((W)st, P);
+      int64_t const j = find_index((uint64_t)c.rep, I);
+      uint32_t ent = kNull, code = 0;
+      if (j >= 0) {
+        code = element_code(vid, c.phase, weights[j], C);
+        ent = packed ? ((uint32_t)j | (code << col_bits)) : (uint32_t)j;
+      }
+      entries[base + (uint64_t)e * 32 + lane] = ent;
+      if (!packed) codes[base + (uint64_t)e * 32 + lane] = (uint16_t)code;
+      used = e + 1;
+    });
+    if (Real) {
+      static_cast<double*>(diag)[i] = row_diag<double>(r, T);
+    } else {
+      cplx const d = row_diag<cplx>(r, T);
+      static_cast<double2*>(diag)[i] = make_double2(d.re, d.im);
+    }
+    row_class[i] = (uint8_t)divisor_class(weights[i], C);
+  }
+  for (uint32_t e = used; e < width; ++e) {
+    entries[base + (uint64_t)e * 32 + lane] = kNull;
+    if (!packed) codes[base + (uint64_t)e * 32 + lane] = 0;
+  }
+}
+
+// Streamed SpMV over SELL-32 slices. RealOp selects the real table/diagonal.
+// With an Indirect (Krylov) view, x = base + k ld and y = base + (k+1) ld
+// with k read from device memory, and each block writes sum_i Re(x_i* y_i).
+template <class X, bool RealOp, bool Packed>
+__global__ void __launch_bounds__(kBlock) k_spmv(StreamView S, uint64_t D, X const* __restrict__ x,
+                                                 X* __restrict__ y, Indirect ind) {
+  using V = typename Store<X>::V;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ double red[kBlock / 32];
+  if (ind.stop && *ind.stop) return;  // uniform across the grid
+  if (ind.k) {
+    uint64_t const k = *ind.k;
+    x += k * ind.ld;
+    y += (k + 1) * ind.ld;
+  }
+  void const* table = stage_table<RealOp>(S, smem_raw);
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  double part = 0.0;
+  if ((s << 5) < D) {
+    V const acc = stream_row_acc<V, X, RealOp, Packed>(S, table, s, threadIdx.x & 31, x);
+    if (i < D) {
+      double const f = S.inv_sqrt_s[S.row_class[i]];
+      V const xi = Store<X>::load(x, i);
+      V const yi = row_value<V>(mulv(stream_diag<V, RealOp>(S, i), xi), f, acc);
+      Store<X>::store(y, i, yi);
+      part = dot_re(xi, yi);
+    }
+  }
+  if (ind.partial) {
+    double const tot = block_sum(part, red);
+    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
+  }
+}
+
+// On-the-fly matvec: same sum, same order, recomputing every element.
+template <class W, class X, bool RealOp>
+__global__ void __launch_bounds__(kBlock)
+    k_otf(PlanView P, IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
+          void const* __restrict__ table, double const* __restrict__ inv_sqrt_s,
+          X const* __restrict__ x, X* __restrict__ y, Indirect ind) {
+  using V = typename Store<X>::V;
+  __shared__ double red[kBlock / 32];
+  if (ind.stop && *ind.stop) return;
+  if (ind.k) {
+    uint64_t const k = *ind.k;
+    x += k * ind.ld;
+    y += (k + 1) * ind.ld;
+  }
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double part = 0.0;
+  if (i < I.D) {
+    uint64_t const r = I.reps[i];
+    V acc = zero<V>();
+    walk_row(r, T, [&](uint32_t, uint64_t st, uint32_t vid) {
+      auto const c = canonicalize<W>((W)st, P);
+      int64_t const j = find_index((uint64_t)c.rep, I);
+      if (j >= 0) {
+        uint32_t const code = element_code(vid, c.phase, weights[j], C);
+        mac(acc, load_table<V>(table, code, RealOp), Store<X>::load(x, (uint64_t)j));
+      }
+    });
+    V dg;
+    if constexpr (std::is_same<V, double>::value) {
+      dg = row_diag<double>(r, T);
+    } else {
+      dg = RealOp ? cplx{row_diag<double>(r, T), 0.0} : row_diag<cplx>(r, T);
+    }
+    uint32_t const cls = divisor_class(weights[i], C);
+    V const xi = Store<X>::load(x, i);
+    V const yi = row_value<V>(mulv(dg, xi), inv_sqrt_s[cls], acc);
+    Store<X>::store(y, i, yi);
+    part = dot_re(xi, yi);
+  }
+  if (ind.partial) {
+    double const tot = block_sum(part, red);
+    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
+  }
+}
+
+template <class X>
+__global__ void k_dot_conj(X const* __restrict__ x, X const* __restrict__ y, uint64_t n,
+                           double2* __restrict__ partial) {
+  using V = typename Store<X>::V;
+  __shared__ double2 red[kBlock / 32];
+  double re = 0.0, im = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    V const a = Store<X>::load(x, i), b = Store<X>::load(y, i);
+    if constexpr (std::is_same<V, double>::value) {
+      re = fma(a, b, re);
+    } else {
+      re = fma(a.re, b.re, fma(a.im, b.im, re));
+      im = fma(a.re, b.im, fma(-a.im, b.re, im));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(re, im);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double2 s = make_double2(0.0, 0.0);
+    for (unsigned w = 0; w < kBlock / 32; ++w) {
+      s.x += red[w].x;
+      s.y += red[w].y;
+    }
+    partial[blockIdx.x] = s;
+  }
+}
+
+// ----------------------------------------------------------- host helpers --
+
+std::vector<uint32_t> divisors_of(uint32_t n) {
+  std::vector<uint32_t> d;
+  for (uint32_t k = 1; k <= n; ++k)
+    if (n % k == 0) d.push_back(k);
+  return d;
+}
+
+void root_of_unity(uint32_t q, uint32_t L, double& re, double& im) {
+  if (q == 0) {
+    re = 1.0; im = 0.0;
+  } else if (4 * q == L) {
+    re = 0.0; im = -1.0;
+  } else if (2 * q == L) {
+    re = -1.0; im = 0.0;
+  } else if (4 * q == 3 * L) {
+    re = 0.0; im = 1.0;
+  } else {
+    double const ang = -2.0 * 3.14159265358979323846 * (double)q / (double)L;
+    re = std::cos(ang);
+    im = std::sin(ang);
+  }
+}
+
+}  // namespace
+
+
+namespace {
+
+OperatorTables* tables_of(OperatorData const& op) { return op.tables.get(); }
+
+int build_tables(OperatorData& op) {
+  if (tables_of(op)) return LS_SUCCESS;
+  BasisData const& b = *op.basis;
+  auto t = std::make_unique<OperatorTables>();
+  auto div = divisors_of(b.plan.group_order);
+  uint32_t const n_div = (uint32_t)div.size();
+  bool const real_phase = characters_real(b);
+  uint32_t const n_ph = real_phase ? 2u : b.plan.L;
+  uint32_t const n_val = (uint32_t)(op.off_values.size() / 2);
+  uint64_t const n_codes = (uint64_t)std::max(1u, n_val) * n_ph * n_div;
+  if (n_codes > kMaxCodes)
+    return fail(LS_SYSTEM_ERROR, "too many distinct matrix-element codes (" + std::to_string(n_codes) + ")");
+  std::vector<double> tr, tc;
+  tc.resize(2 * n_codes, 0.0);
+  for (uint32_t v = 0; v < std::max(1u, n_val); ++v)
+    for (uint32_t p = 0; p < n_ph; ++p)
+      for (uint32_t d = 0; d < n_div; ++d) {
+        double cre = n_val ? op.off_values[2 * v] : 0.0, cim = n_val ? op.off_values[2 * v + 1] : 0.0;
+        double xr, xi;
+        root_of_unity(real_phase ? (p ? b.plan.L / 2 : 0) : p, b.plan.L, xr, xi);
+        double const sq = std::sqrt((double)div[d]);
+        uint64_t const code = ((uint64_t)v * n_ph + p) * n_div + d;
+        tc[2 * code] = (cre * xr - cim * xi) * sq;
+        tc[2 * code + 1] = (cre * xi + cim * xr) * sq;
+      }
+  std::vector<double> inv(n_div);
+  for (uint32_t d = 0; d < n_div; ++d) inv[d] = 1.0 / std::sqrt((double)div[d]);
+  if (int st = t->divisors.allocate(n_div * 4)) return st;
+  if (int st = t->inv_sqrt_s.allocate(n_div * 8)) return st;
+  SED_TRY_CUDA(cudaMemcpy(t->divisors.ptr, div.data(), n_div * 4, cudaMemcpyHostToDevice));
+  SED_TRY_CUDA(cudaMemcpy(t->inv_sqrt_s.ptr, inv.data(), n_div * 8, cudaMemcpyHostToDevice));
+  if (int st = t->table_c.allocate(n_codes * 16)) return st;
+  SED_TRY_CUDA(cudaMemcpy(t->table_c.ptr, tc.data(), n_codes * 16, cudaMemcpyHostToDevice));
+  if (op.is_real) {
+    tr.resize(n_codes);
+    for (uint64_t c = 0; c < n_codes; ++c) tr[c] = tc[2 * c];
+    if (int st = t->table.allocate(n_codes * 8)) return st;
+    SED_TRY_CUDA(cudaMemcpy(t->table.ptr, tr.data(), n_codes * 8, cudaMemcpyHostToDevice));
+  }
+  t->code.divisors = t->divisors.as<uint32_t>();
+  t->code.n_div = n_div;
+  t->code.n_ph = n_ph;
+  t->code.real_phase = real_phase ? 1u : 0u;
+  t->n_codes = (uint32_t)n_codes;
+  op.tables = std::move(t);
+  return LS_SUCCESS;
+}
+
+int elem_size(int dtype) {
+  switch (dtype) {
+    case 0: return 4;
+    case 1: return 8;
+    case 2: return 8;
+    case 3: return 16;
+    default: return 0;
+  }
+}
+
+bool is_device_pointer(void const* p) {
+  cudaPointerAttributes a{};
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+OperatorData::~OperatorData() {
+  tables.reset();
+  if (cuda_stream) {
+    ScopedDevice dev(basis ? basis->device : -1);
+    cudaStreamDestroy(cuda_stream);
+  }
+}
+
+int operator_upload_terms(OperatorData& op) {
+  if (op.term_buf.ptr) return LS_SUCCESS;
+  unsigned const n_terms = (unsigned)op.terms.size();
+  // Distinct off-diagonal values (exact bitwise dedup).
+  op.off_values.clear();
+  std::vector<uint32_t> tuple_term, tuple_sites;
+  std::vector<double> diag((size_t)std::max(1u, n_terms) * 16 * 2, 0.0);
+  std::vector<uint8_t> n_off((size_t)std::max(1u, n_terms) * 16, 0), off_col((size_t)std::max(1u, n_terms) * 256, 0);
+  std::vector<uint16_t> off_vid((size_t)std::max(1u, n_terms) * 256, 0);
+  for (unsigned t = 0; t < n_terms; ++t) {
+    InteractionData const& term = op.terms[t];
+    unsigned const dim = 1u << term.k;
+    for (unsigned a = 0; a < dim; ++a)
+      for (unsigned a2 = 0; a2 < dim; ++a2) {
+        double const re = term.matrix[2 * (a * dim + a2)], im = term.matrix[2 * (a * dim + a2) + 1];
+        if (a2 == a) {
+          diag[2 * (t * 16 + a)] = re;
+          diag[2 * (t * 16 + a) + 1] = im;
+          continue;
+        }
+        if (re == 0.0 && im == 0.0) continue;
+        size_t vid = op.off_values.size() / 2;
+        for (size_t q = 0; q < op.off_values.size() / 2; ++q)
+          if (std::memcmp(&op.off_values[2 * q], &re, 8) == 0 &&
+              std::memcmp(&op.off_values[2 * q + 1], &im, 8) == 0) {
+            vid = q;
+            break;
+          }
+        if (vid == op.off_values.size() / 2) {
+          op.off_values.push_back(re);
+          op.off_values.push_back(im);
+        }
+        unsigned const q = n_off[t * 16 + a]++;
+        off_col[(t * 16 + a) * 16 + q] = (uint8_t)a2;
+        off_vid[(t * 16 + a) * 16 + q] = (uint16_t)vid;
+      }
+    size_t const n_tuples = term.sites.size() / term.k;
+    for (size_t u = 0; u < n_tuples; ++u) {
+      uint32_t packed = 0;
+      for (unsigned m = 0; m < term.k; ++m) packed |= (uint32_t)term.sites[u * term.k + m] << (8 * m);
+      tuple_term.push_back(t | (term.k << 16));
+      tuple_sites.push_back(packed);
+    }
+  }
+  if (op.off_values.size() / 2 > 4096)
+    return fail(LS_SYSTEM_ERROR, "too many distinct off-diagonal matrix values");
+  size_t const nt = std::max<size_t>(1, tuple_term.size());
+  auto align = [](size_t v) { return (v + 15) & ~(size_t)15; };
+  size_t const sz_tt = align(nt * 4), sz_ts = align(nt * 4), sz_dg = align(diag.size() * 8),
+               sz_no = align(n_off.size()), sz_oc = align(off_col.size()),
+               sz_ov = align(off_vid.size() * 2),
+               sz_val = align(std::max<size_t>(2, op.off_values.size()) * 8);
+  size_t const total = sz_tt + sz_ts + sz_dg + sz_no + sz_oc + sz_ov + sz_val;
+  std::vector<uint8_t> host(total, 0);
+  size_t off = 0;
+  auto put = [&](void const* src, size_t n, size_t sz) {
+    if (n) std::memcpy(host.data() + off, src, n);
+    size_t const at = off;
+    off += sz;
+    return at;
+  };
+  size_t const o_tt = put(tuple_term.data(), tuple_term.size() * 4, sz_tt);
+  size_t const o_ts = put(tuple_sites.data(), tuple_sites.size() * 4, sz_ts);
+  size_t const o_dg = put(diag.data(), diag.size() * 8, sz_dg);
+  size_t const o_no = put(n_off.data(), n_off.size(), sz_no);
+  size_t const o_oc = put(off_col.data(), off_col.size(), sz_oc);
+  size_t const o_ov = put(off_vid.data(), off_vid.size() * 2, sz_ov);
+  size_t const o_val = put(op.off_values.data(), op.off_values.size() * 8, sz_val);
+  ScopedDevice dev(op.basis->device);
+  if (int st = op.term_buf.allocate(total)) return st;
+  SED_TRY_CUDA(cudaMemcpy(op.term_buf.ptr, host.data(), total, cudaMemcpyHostToDevice));
+  uint8_t* base = op.term_buf.as<uint8_t>();
+  op.terms_dev.n_tuples = (uint32_t)tuple_term.size();
+  op.terms_dev.tuple_term = (uint32_t const*)(base + o_tt);
+  op.terms_dev.tuple_sites = (uint32_t const*)(base + o_ts);
+  op.terms_dev.diag = (double const*)(base + o_dg);
+  op.terms_dev.n_off = base + o_no;
+  op.terms_dev.off_col = base + o_oc;
+  op.terms_dev.off_vid = (uint16_t const*)(base + o_ov);
+  op.terms_dev.off_val = (double const*)(base + o_val);
+  return LS_SUCCESS;
+}
+
+int operator_ensure_ready(OperatorData& op) {
+  BasisData& b = *op.basis;
+  if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  ScopedDevice dev(b.device);
+  if (!op.cuda_stream) SED_TRY_CUDA(cudaStreamCreateWithFlags(&op.cuda_stream, cudaStreamNonBlocking));
+  if (int st = basis_upload_plan(b, op.cuda_stream)) return st;
+  if (int st = operator_upload_terms(op)) return st;
+  if (int st = build_tables(op)) return st;
+  return LS_SUCCESS;
+}
+
+StreamView stream_view(OperatorData const& op) {
+  StreamForm const& sf = op.stream;
+  OperatorTables const& tb = *op.tables;
+  StreamView S{};
+  S.slice_ptr = sf.slice_ptr.as<uint64_t>();
+  S.entries = sf.entries.as<uint32_t>();
+  S.codes = sf.values.as<uint16_t>();
+  S.diag = sf.diag.ptr;
+  S.row_class = sf.row_class.as<uint8_t>();
+  S.table = op.is_real ? tb.table.ptr : tb.table_c.ptr;
+  S.inv_sqrt_s = tb.inv_sqrt_s.as<double>();
+  S.col_bits = sf.col_bits;
+  S.n_codes = tb.n_codes;
+  return S;
+}
+
+int operator_record_stream(OperatorData& op, cudaStream_t stream) {
+  if (op.stream.ready) return LS_SUCCESS;
+  if (int st = operator_ensure_ready(op)) return st;
+  BasisData& b = *op.basis;
+  OperatorTables const& tb = *tables_of(op);
+  ScopedDevice dev(b.device);
+  auto t0 = std::chrono::steady_clock::now();
+  uint64_t const D = b.D;
+  uint64_t const n_slices = (D + 31) / 32;
+  unsigned col_bits = 1;
+  while (col_bits < 32 && ((uint64_t)1 << col_bits) < std::max<uint64_t>(D, 2)) ++col_bits;
+  if (D >= ((uint64_t)1 << 32) - 1)
+    return fail(LS_OUT_OF_MEMORY, "stream form supports fewer than 2^32 - 1 representatives");
+  unsigned code_bits = 0;
+  while (((uint64_t)1 << code_bits) < tb.n_codes) ++code_bits;
+  bool const packed = col_bits + code_bits <= 31;  // kNull stays unrepresentable
+  StreamForm& sf = op.stream;
+  sf = StreamForm{};
+  DeviceBuffer elements;
+  if (int st = sf.slice_ptr.allocate((n_slices + 1) * 8)) return st;
+  if (int st = elements.allocate((n_slices + 1) * 8)) return st;
+  unsigned const grid = (unsigned)((n_slices * 32 + kBlock - 1) / kBlock);
+  if (n_slices) {
+    k_count<<<grid, kBlock, 0, stream>>>(b.reps.as<uint64_t>(), D, op.terms_dev, n_slices,
+                                         sf.slice_ptr.as<uint64_t>(), elements.as<uint64_t>());
+    SED_TRY_CUDA(cudaGetLastError());
+  }
+  k_scan_u64<<<1, 1024, 0, stream>>>(sf.slice_ptr.as<uint64_t>(), n_slices);
+  k_scan_u64<<<1, 1024, 0, stream>>>(elements.as<uint64_t>(), n_slices);
+  SED_TRY_CUDA(cudaGetLastError());
+  uint64_t n_entries = 0, n_elements = 0;
+  SED_TRY_CUDA(cudaMemcpyAsync(&n_entries, sf.slice_ptr.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
+  SED_TRY_CUDA(cudaMemcpyAsync(&n_elements, elements.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
+  SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  size_t free_b = 0, total_b = 0;
+  SED_TRY_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  uint64_t const need = n_entries * (packed ? 4 : 6) + D * (op.is_real ? 9 : 17);
+  if (need > free_b)
+    return fail(LS_OUT_OF_MEMORY, "stream form needs " + std::to_string(need) + " bytes, " +
+                                      std::to_string(free_b) + " free");
+  if (int st = sf.entries.allocate(std::max<uint64_t>(1, n_entries) * 4)) return st;
+  if (!packed)
+    if (int st = sf.values.allocate(std::max<uint64_t>(1, n_entries) * 2)) return st;
+  if (int st = sf.diag.allocate(std::max<uint64_t>(1, D) * (op.is_real ? 8 : 16))) return st;
+  if (int st = sf.row_class.allocate(std::max<uint64_t>(1, D))) return st;
+  if (n_slices) {
+    bool const wide = b.plan.n_bits > 32;
+    IndexView const I = b.index_view();
+    auto launch = [&](auto w_tag, auto real_tag) {
+      using W = decltype(w_tag);
+      constexpr bool R = decltype(real_tag)::value;
+      k_record<W, R><<<grid, kBlock, 0, stream>>>(
+          b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices,
+          sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(),
+          sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>());
+    };
+    if (wide) {
+      if (op.is_real) launch(uint64_t{}, std::true_type{});
+      else launch(uint64_t{}, std::false_type{});
+    } else {
+      if (op.is_real) launch(uint32_t{}, std::true_type{});
+      else launch(uint32_t{}, std::false_type{});
+    }
+    SED_TRY_CUDA(cudaGetLastError());
+  }
+  SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  sf.packed = packed;
+  sf.col_bits = col_bits;
+  sf.n_slices = n_slices;
+  sf.n_entries = n_entries;
+  sf.n_elements = n_elements;
+  sf.n_codes = tb.n_codes;
+  sf.ready = true;
+  sf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (logging_enabled())
+    log_line("stream form: %llu elements, %llu slots (%s), %.1f MB, %.3f s",
+             (unsigned long long)n_elements, (unsigned long long)n_entries,
+             packed ? "packed" : "split", sf.bytes() / 1e6, sf.seconds);
+  return LS_SUCCESS;
+}
+
+namespace {
+
+template <class X>
+int launch_apply(OperatorData& op, X const* x, X* y, cudaStream_t stream, bool use_stream,
+                 Indirect ind) {
+  BasisData& b = *op.basis;
+  OperatorTables const& tb = *tables_of(op);
+  using V = typename Store<X>::V;
+  constexpr bool complex_storage = std::is_same<V, cplx>::value;
+  uint64_t const D = b.D;
+  if (D == 0) return LS_SUCCESS;
+  bool const real_tab = op.is_real;  // real table exists
+  if (use_stream) {
+    StreamForm const& sf = op.stream;
+    StreamView const S = stream_view(op);
+    unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
+    size_t const smem = std::min<size_t>(32768, (size_t)tb.n_codes * (real_tab ? 8 : 16));
+    if (real_tab) {
+      if (sf.packed) k_spmv<X, true, true><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
+      else k_spmv<X, true, false><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
+    } else {
+      if constexpr (complex_storage) {
+        if (sf.packed) k_spmv<X, false, true><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
+        else k_spmv<X, false, false><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
+      } else {
+        return fail(LS_OPERATOR_IS_COMPLEX, "complex operator applied to real vectors");
+      }
+    }
+  } else {
+    IndexView const I = b.index_view();
+    unsigned const grid = (unsigned)((D + kBlock - 1) / kBlock);
+    void const* table = real_tab ? tb.table.ptr : tb.table_c.ptr;
+    bool const wide = b.plan.n_bits > 32;
+    if (real_tab) {
+      if (wide)
+        k_otf<uint64_t, X, true><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+                                                              b.weights.as<uint32_t>(), table,
+                                                              tb.inv_sqrt_s.as<double>(), x, y, ind);
+      else
+        k_otf<uint32_t, X, true><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+                                                              b.weights.as<uint32_t>(), table,
+                                                              tb.inv_sqrt_s.as<double>(), x, y, ind);
+    } else {
+      if constexpr (complex_storage) {
+        if (wide)
+          k_otf<uint64_t, X, false><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+                                                                 b.weights.as<uint32_t>(), table,
+                                                                 tb.inv_sqrt_s.as<double>(), x, y, ind);
+        else
+          k_otf<uint32_t, X, false><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+                                                                 b.weights.as<uint32_t>(), table,
+                                                                 tb.inv_sqrt_s.as<double>(), x, y, ind);
+      } else {
+        return fail(LS_OPERATOR_IS_COMPLEX, "complex operator applied to real vectors");
+      }
+    }
+  }
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
+}  // namespace
+
+int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void const* x,
+                          uint64_t ldx, void* y, uint64_t ldy, cudaStream_t stream, int form) {
+  if (int st = operator_ensure_ready(op)) return st;
+  if (dtype < 0 || dtype > 3) return fail(LS_INVALID_DATATYPE, "dtype must be 0..3");
+  if (!op.is_real && dtype < 2) return fail(LS_OPERATOR_IS_COMPLEX, "operator is complex; use dtype 2 or 3");
+  if (form == SED_FORM_AUTO) form = op.form;
+  bool use_stream = op.stream.ready && form != SED_FORM_ON_THE_FLY;
+  if (!use_stream && form != SED_FORM_ON_THE_FLY) {
+    int st = operator_record_stream(op, stream);
+    if (st == LS_SUCCESS) use_stream = true;
+    else if (form == SED_FORM_STREAM) return st;  // AUTO falls back to on-the-fly
+  }
+  size_t const es = (size_t)elem_size(dtype);
+  for (uint64_t c = 0; c < block; ++c) {
+    void const* xc = static_cast<char const*>(x) + c * ldx * es;
+    void* yc = static_cast<char*>(y) + c * ldy * es;
+    int st;
+    switch (dtype) {
+      case 0: st = launch_apply<float>(op, (float const*)xc, (float*)yc, stream, use_stream, Indirect{}); break;
+      case 1: st = launch_apply<double>(op, (double const*)xc, (double*)yc, stream, use_stream, Indirect{}); break;
+      case 2: st = launch_apply<float2>(op, (float2 const*)xc, (float2*)yc, stream, use_stream, Indirect{}); break;
+      default: st = launch_apply<double2>(op, (double2 const*)xc, (double2*)yc, stream, use_stream, Indirect{}); break;
+    }
+    if (st) return st;
+  }
+  return LS_SUCCESS;
+}
+
+int operator_apply_krylov(OperatorData& op, int dtype, void* base, Indirect ind, cudaStream_t stream,
+                          unsigned* blocks) {
+  bool const use_stream = op.stream.ready && op.form != SED_FORM_ON_THE_FLY;
+  uint64_t const D = op.basis->D;
+  *blocks = use_stream ? (unsigned)((op.stream.n_slices * 32 + kBlock - 1) / kBlock)
+                       : (unsigned)((D + kBlock - 1) / kBlock);
+  switch (dtype) {
+    case 1: return launch_apply<double>(op, (double const*)base, (double*)base, stream, use_stream, ind);
+    case 3: return launch_apply<double2>(op, (double2 const*)base, (double2*)base, stream, use_stream, ind);
+    case 0: return launch_apply<float>(op, (float const*)base, (float*)base, stream, use_stream, ind);
+    default: return launch_apply<float2>(op, (float2 const*)base, (float2*)base, stream, use_stream, ind);
+  }
+}
+
+}  // namespace sed
+
+using namespace sed;
+
+namespace {
+
+int create_interaction(ls_interaction** ptr, unsigned k, void const* matrix, unsigned number_nodes,
+                       uint16_t const* nodes) {
+  if (!ptr || !matrix || (number_nodes && !nodes))
+    return fail(LS_INVALID_ARGUMENT, "ls_create_interaction: NULL argument");
+  unsigned const dim = 1u << k;
+  auto* it = new (std::nothrow) ls_interaction;
+  if (!it) return fail(LS_OUT_OF_MEMORY, "ls_create_interaction");
+  it->d.k = k;
+  double const* m = static_cast<double const*>(matrix);
+  it->d.matrix.assign(m, m + 2 * dim * dim);
+  it->d.sites.assign(nodes, nodes + (size_t)number_nodes * k);
+  for (unsigned u = 0; u < number_nodes; ++u)
+    for (unsigned a = 0; a < k; ++a)
+      for (unsigned c = 0; c < a; ++c)
+        if (nodes[u * k + a] == nodes[u * k + c]) {
+          delete it;
+          return fail(LS_INVALID_ARGUMENT, "a site tuple repeats a site");
+        }
+  it->d.is_real = true;
+  for (unsigned q = 0; q < dim * dim; ++q)
+    if (m[2 * q + 1] != 0.0) it->d.is_real = false;
+  *ptr = it;
+  return LS_SUCCESS;
+}
+
+int host_blocks(OperatorData& op, int dtype, uint64_t size, uint64_t block, void const* x,
+                uint64_t ldx, void* y, uint64_t ldy) {
+  BasisData& b = *op.basis;
+  size_t const es = (size_t)elem_size(dtype);
+  bool const x_dev = is_device_pointer(x), y_dev = is_device_pointer(y);
+  cudaStream_t s = op.cuda_stream;
+  DeviceBuffer xb, yb;
+  void const* xd = x;
+  void* yd = y;
+  uint64_t lx = ldx, ly = ldy;
+  if (!x_dev) {
+    if (int st = xb.allocate(size * block * es)) return st;
+    SED_TRY_CUDA(cudaMemcpy2DAsync(xb.ptr, size * es, x, ldx * es, size * es, block, cudaMemcpyHostToDevice, s));
+    xd = xb.ptr;
+    lx = size;
+  }
+  if (!y_dev) {
+    if (int st = yb.allocate(size * block * es)) return st;
+    yd = yb.ptr;
+    ly = size;
+  }
+  if (int st = operator_apply_device(op, dtype, block, xd, lx, yd, ly, s, SED_FORM_AUTO)) return st;
+  if (!y_dev)
+    SED_TRY_CUDA(cudaMemcpy2DAsync(y, ldy * es, yd, size * es, size * es, block, cudaMemcpyDeviceToHost, s));
+  SED_TRY_CUDA(cudaStreamSynchronize(s));
+  (void)b;
+  return LS_SUCCESS;
+}
+
+int check_block(OperatorData const& op, int dtype, uint64_t size, uint64_t block, uint64_t ldx) {
+  if (!op.basis->built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  if (dtype < 0 || dtype > 3) return fail(LS_INVALID_DATATYPE, "dtype must be 0..3");
+  if (size != op.basis->D)
+    return fail(LS_DIMENSION_MISMATCH, "vector length " + std::to_string(size) +
+                                           " != basis dimension " + std::to_string(op.basis->D));
+  if (block > 0 && ldx < size) return fail(LS_INVALID_ARGUMENT, "column stride is smaller than the size");
+  return LS_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ls_create_interaction1(ls_interaction** p, void const* m, unsigned n, uint16_t const* s) {
+  return create_interaction(p, 1, m, n, s);
+}
+int ls_create_interaction2(ls_interaction** p, void const* m, unsigned n, uint16_t const* s) {
+  return create_interaction(p, 2, m, n, s);
+}
+int ls_create_interaction3(ls_interaction** p, void const* m, unsigned n, uint16_t const* s) {
+  return create_interaction(p, 3, m, n, s);
+}
+int ls_create_interaction4(ls_interaction** p, void const* m, unsigned n, uint16_t const* s) {
+  return create_interaction(p, 4, m, n, s);
+}
+bool ls_interaction_is_real(ls_interaction const* i) { return i && i->d.is_real; }
+void ls_destroy_interaction(ls_interaction* i) { delete i; }
+
+int ls_create_operator(ls_operator** ptr, ls_spin_basis const* basis, unsigned number_terms,
+                       ls_interaction const* const terms[]) {
+  if (!ptr || !basis || (number_terms && !terms))
+    return fail(LS_INVALID_ARGUMENT, "ls_create_operator: NULL argument");
+  try {
+    auto d = std::make_shared<OperatorData>();
+    d->basis = basis->d;
+    d->is_real = true;
+    for (unsigned t = 0; t < number_terms; ++t) {
+      if (!terms[t]) return fail(LS_INVALID_ARGUMENT, "ls_create_operator: NULL term");
+      for (uint16_t s : terms[t]->d.sites)
+        if (s >= basis->d->n)
+          return fail(LS_INVALID_ARGUMENT, "site index " + std::to_string(s) +
+                                               " is not below number_spins " + std::to_string(basis->d->n));
+      d->terms.push_back(terms[t]->d);
+      d->is_real = d->is_real && terms[t]->d.is_real;
+    }
+    d->is_real = d->is_real && characters_real(*basis->d);
+    auto* op = new ls_operator;
+    op->d = std::move(d);
+    *ptr = op;
+    return LS_SUCCESS;
+  } catch (std::bad_alloc const&) {
+    return fail(LS_OUT_OF_MEMORY, "ls_create_operator");
+  }
+}
+
+void ls_destroy_operator(ls_operator* op) { delete op; }
+bool ls_operator_is_real(ls_operator const* op) { return op && op->d->is_real; }
+
+int ls_operator_matmat(ls_operator const* op, int dtype, uint64_t size, uint64_t block_size,
+                       void const* x, uint64_t x_stride, void* y, uint64_t y_stride) {
+  if (!op || (block_size && (!x || !y))) return fail(LS_INVALID_ARGUMENT, "ls_operator_matmat: NULL argument");
+  OperatorData& d = *op->d;
+  std::lock_guard<std::mutex> lock(d.mu);
+  if (int st = check_block(d, dtype, size, block_size, x_stride)) return st;
+  if (block_size && y_stride < size) return fail(LS_INVALID_ARGUMENT, "column stride is smaller than the size");
+  if (!d.is_real && dtype < 2) return fail(LS_OPERATOR_IS_COMPLEX, "operator is complex; use dtype 2 or 3");
+  if (block_size == 0 || size == 0) return LS_SUCCESS;
+  try {
+    ScopedDevice dev(d.basis->device);
+    if (int st = operator_ensure_ready(d)) return st;
+    return host_blocks(d, dtype, size, block_size, x, x_stride, y, y_stride);
+  } catch (std::exception const& e) {
+    return fail(LS_SYSTEM_ERROR, e.what());
+  }
+}
+
+int sed_operator_matmat_device(ls_operator const* op, int dtype, uint64_t size, uint64_t block_size,
+                               void const* x, uint64_t x_stride, void* y, uint64_t y_stride,
+                               void* stream) {
+  if (!op || (block_size && (!x || !y))) return fail(LS_INVALID_ARGUMENT, "sed_operator_matmat_device: NULL argument");
+  OperatorData& d = *op->d;
+  std::lock_guard<std::mutex> lock(d.mu);
+  if (int st = check_block(d, dtype, size, block_size, x_stride)) return st;
+  if (block_size == 0 || size == 0) return LS_SUCCESS;
+  ScopedDevice dev(d.basis->device);
+  if (int st = operator_ensure_ready(d)) return st;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : d.cuda_stream;
+  return operator_apply_device(d, dtype, block_size, x, x_stride, y, y_stride, s, SED_FORM_AUTO);
+}
+
+int ls_operator_expectation(ls_operator const* op, int dtype, uint64_t size, uint64_t block_size,
+                            void const* x, uint64_t x_stride, void* out) {
+  if (!op || !out || (block_size && !x)) return fail(LS_INVALID_ARGUMENT, "ls_operator_expectation: NULL argument");
+  OperatorData& d = *op->d;
+  std::lock_guard<std::mutex> lock(d.mu);
+  if (int st = check_block(d, dtype, size, block_size, x_stride)) return st;
+  if (!d.is_real && dtype < 2) return fail(LS_OPERATOR_IS_COMPLEX, "operator is complex; use dtype 2 or 3");
+  double* res = static_cast<double*>(out);
+  if (block_size == 0) return LS_SUCCESS;
+  if (size == 0) {
+    for (uint64_t c = 0; c < block_size; ++c) res[2 * c] = res[2 * c + 1] = 0.0;
+    return LS_SUCCESS;
+  }
+  try {
+    ScopedDevice dev(d.basis->device);
+    if (int st = operator_ensure_ready(d)) return st;
+    size_t const es = (size_t)elem_size(dtype);
+    cudaStream_t s = d.cuda_stream;
+    DeviceBuffer xb, yb, part;
+    if (int st = xb.allocate(size * block_size * es)) return st;
+    if (int st = yb.allocate(size * block_size * es)) return st;
+    SED_TRY_CUDA(cudaMemcpy2DAsync(xb.ptr, size * es, x, x_stride * es, size * es, block_size, cudaMemcpyDefault, s));
+    if (int st = operator_apply_device(d, dtype, block_size, xb.ptr, size, yb.ptr, size, s, SED_FORM_AUTO)) return st;
+    unsigned const grid = grid_size(size, d.basis->device, 4);
+    if (int st = part.allocate((size_t)grid * 16 * block_size)) return st;
+    for (uint64_t c = 0; c < block_size; ++c) {
+      char const* xc = xb.as<char>() + c * size * es;
+      char const* yc = yb.as<char>() + c * size * es;
+      double2* pc = part.as<double2>() + c * grid;
+      switch (dtype) {
+        case 0: k_dot_conj<float><<<grid, kBlock, 0, s>>>((float const*)xc, (float const*)yc, size, pc); break;
+        case 1: k_dot_conj<double><<<grid, kBlock, 0, s>>>((double const*)xc, (double const*)yc, size, pc); break;
+        case 2: k_dot_conj<float2><<<grid, kBlock, 0, s>>>((float2 const*)xc, (float2 const*)yc, size, pc); break;
+        default: k_dot_conj<double2><<<grid, kBlock, 0, s>>>((double2 const*)xc, (double2 const*)yc, size, pc); break;
+      }
+    }
+    SED_TRY_CUDA(cudaGetLastError());
+    std::vector<double2> h((size_t)grid * block_size);
+    SED_TRY_CUDA(cudaMemcpyAsync(h.data(), part.ptr, h.size() * 16, cudaMemcpyDeviceToHost, s));
+    SED_TRY_CUDA(cudaStreamSynchronize(s));
+    for (uint64_t c = 0; c < block_size; ++c) {
+      double re = 0.0, im = 0.0;
+      for (unsigned g = 0; g < grid; ++g) {
+        re += h[c * grid + g].x;
+        im += h[c * grid + g].y;
+      }
+      res[2 * c] = re;
+      res[2 * c + 1] = im;
+    }
+    return LS_SUCCESS;
+  } catch (std::exception const& e) {
+    return fail(LS_SYSTEM_ERROR, e.what());
+  }
+}
+
+int sed_operator_prepare(ls_operator* op, int form) {
+  if (!op) return fail(LS_INVALID_ARGUMENT, "sed_operator_prepare: NULL operator");
+  OperatorData& d = *op->d;
+  std::lock_guard<std::mutex> lock(d.mu);
+  ScopedDevice dev(d.basis ? d.basis->device : -1);
+  if (int st = operator_ensure_ready(d)) return st;
+  if (form < SED_FORM_AUTO || form > SED_FORM_ON_THE_FLY) return fail(LS_INVALID_ARGUMENT, "unknown form");
+  d.form = form;
+  if (form == SED_FORM_ON_THE_FLY) return LS_SUCCESS;
+  int st = operator_record_stream(d, d.cuda_stream);
+  return (form == SED_FORM_AUTO && st == LS_OUT_OF_MEMORY) ? LS_SUCCESS : st;
+}
+
+uint64_t sed_operator_stream_bytes(ls_operator const* op) {
+  return (op && op->d->stream.ready) ? op->d->stream.bytes() : 0;
+}
+uint64_t sed_operator_stream_elements(ls_operator const* op) {
+  return (op && op->d->stream.ready) ? op->d->stream.n_elements : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,213 @@
+// sed_internal.hpp — object model shared by the libsed translation units.
+//
+// The opaque handles of sed.h wrap reference-counted payloads: SpinED hands
+// every handle to a GHC finaliser (src/SpinED/Internal.hs:116,150,228,362,402)
+// and only keeps the basis alive while ls_create_operator runs
+// (Internal.hs:391-402), so an operator owns a reference to its basis data.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sed.h"
+#include "canon.cuh"
+
+namespace sed {
+
+// ---------------------------------------------------------------- errors ---
+int fail(int status, std::string const& message);  // records message, returns status
+std::string last_message();
+bool logging_enabled();
+void log_line(char const* fmt, ...);
+
+#define SED_TRY_CUDA(expr)                                                              \
+  do {                                                                                  \
+    cudaError_t sed_err_ = (expr);                                                      \
+    if (sed_err_ != cudaSuccess)                                                        \
+      return ::sed::fail(LS_CUDA_ERROR, std::string(#expr) + ": " +                     \
+                                            cudaGetErrorString(sed_err_));              \
+  } while (0)
+
+// ------------------------------------------------------- device buffers ---
+// Owns a device allocation; frees it on the device that made it, from any
+// host thread.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int device = -1;
+  DeviceBuffer() = default;
+  DeviceBuffer(DeviceBuffer const&) = delete;
+  DeviceBuffer& operator=(DeviceBuffer const&) = delete;
+  DeviceBuffer(DeviceBuffer&& o) noexcept { swap(o); }
+  DeviceBuffer& operator=(DeviceBuffer&& o) noexcept {
+    reset();
+    swap(o);
+    return *this;
+  }
+  ~DeviceBuffer() { reset(); }
+  void swap(DeviceBuffer& o) noexcept {
+    std::swap(ptr, o.ptr);
+    std::swap(bytes, o.bytes);
+    std::swap(device, o.device);
+  }
+  int allocate(size_t n);  // LS_* status
+  void reset();
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(ptr);
+  }
+};
+
+struct ScopedDevice {
+  int previous = -1;
+  explicit ScopedDevice(int device);
+  ~ScopedDevice();
+};
+
+// ------------------------------------------------------------- symmetry ---
+struct SymmetryData {
+  std::vector<uint8_t> perm;  // y_i = x_{perm[i]}
+  unsigned sector = 0;
+  unsigned periodicity = 1;
+};
+
+struct GroupData {
+  unsigned n = 0;                  // 0: trivial group of unspecified size
+  std::vector<uint8_t> perms;      // [size][n], element 0 is the identity
+  std::vector<uint32_t> phase;     // numerators mod L
+  unsigned L = 1;
+  std::vector<SymmetryData> generators;
+  unsigned size() const { return n ? (unsigned)phase.size() : 1u; }
+};
+
+// Host-side symmetry plan; `view()` exposes it to canon.cuh.
+struct SymPlanHost {
+  unsigned n_bits = 0;
+  uint64_t mask = 0;
+  int inv = 0;
+  unsigned L = 1;
+  unsigned inv_phase = 0;
+  unsigned group_order = 1;         // including inversion
+  unsigned n_cosets = 1, n_h = 1, n_stages = 0, n_terms = 1;
+  std::vector<uint64_t> benes_mask;  // [n_cosets][n_stages]
+  std::vector<uint32_t> benes_shift; // [n_stages]
+  std::vector<uint64_t> h_mask;      // [n_h][n_terms]
+  std::vector<uint32_t> h_rot;       // [n_h][n_terms] left-rotate amounts
+  std::vector<uint32_t> coset_phase; // [n_cosets]
+  std::vector<uint32_t> h_phase;     // [n_h]
+  PlanView view() const;
+};
+
+int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymPlanHost& out);
+
+// ---------------------------------------------------------------- basis ---
+struct BasisData {
+  int device = -1;
+  unsigned n = 0;
+  int hw = -1;
+  int inv = 0;
+  GroupData group;
+  SymPlanHost plan;
+  // device copy of the plan arrays (one allocation) and the view onto it
+  DeviceBuffer plan_buf;
+  PlanView plan_dev{};
+  DeviceBuffer binom;  // [65][65] uint64
+  // built state
+  bool built = false;
+  uint64_t D = 0;
+  DeviceBuffer reps;     // uint64[D]
+  DeviceBuffer weights;  // uint32[D] stabiliser orders
+  DeviceBuffer prefix;   // uint64[(1 << prefix_bits) + 1]
+  unsigned prefix_bits = 0, prefix_shift = 0;
+  std::vector<uint32_t> s_values;  // distinct stabiliser orders (ascending)
+  std::mutex mu;
+  IndexView index_view() const;
+};
+
+int basis_upload_plan(BasisData& b, cudaStream_t stream);
+int basis_build_index(BasisData& b, cudaStream_t stream);
+
+// ----------------------------------------------------------- interaction ---
+struct InteractionData {
+  unsigned k = 2;
+  std::vector<double> matrix;  // interleaved complex, (2^k)^2 entries
+  std::vector<uint16_t> sites; // [n_tuples][k]
+  bool is_real = true;
+};
+
+// -------------------------------------------------------------- operator ---
+struct StreamForm {
+  bool ready = false;
+  bool packed = true;           // u32 entries: col | code << col_bits
+  unsigned col_bits = 0;
+  uint64_t n_slices = 0;
+  uint64_t n_entries = 0;       // padded slots
+  uint64_t n_elements = 0;      // generated off-diagonal elements
+  DeviceBuffer slice_ptr;       // uint64[n_slices + 1] (slot offsets)
+  DeviceBuffer entries;         // uint32[n_entries] (packed) or col array
+  DeviceBuffer values;          // double[n_entries] (unpacked form)
+  DeviceBuffer diag;            // double or double2 [D]
+  DeviceBuffer row_class;       // uint8[D] stabiliser class of the row
+  DeviceBuffer table;           // value table for codes (double or double2)
+  DeviceBuffer inv_sqrt_s;      // double[n classes]
+  unsigned n_codes = 0;
+  double seconds = 0;
+  uint64_t bytes() const {
+    return slice_ptr.bytes + entries.bytes + values.bytes + diag.bytes + row_class.bytes +
+           table.bytes + inv_sqrt_s.bytes;
+  }
+};
+
+struct OperatorTables;  // value tables, defined in operator.cu
+
+struct OperatorData {
+  std::shared_ptr<BasisData> basis;
+  std::vector<InteractionData> terms;
+  bool is_real = true;
+  // device term tables
+  DeviceBuffer term_buf;
+  TermsView terms_dev{};
+  std::vector<double> off_values;  // distinct off-diagonal matrix values (re, im)
+  StreamForm stream;
+  std::unique_ptr<OperatorTables> tables;
+  int form = SED_FORM_AUTO;  // selected by sed_operator_prepare
+  cudaStream_t cuda_stream = nullptr;
+  std::mutex mu;
+  ~OperatorData();
+};
+
+int operator_upload_terms(OperatorData& op);
+int operator_record_stream(OperatorData& op, cudaStream_t stream);
+int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void const* x,
+                          uint64_t ldx, void* y, uint64_t ldy, cudaStream_t stream, int form);
+
+bool characters_real(BasisData const& b);
+int current_device(int* device);
+
+}  // namespace sed
+
+struct ls_symmetry {
+  sed::SymmetryData d;
+};
+struct ls_group {
+  sed::GroupData d;
+};
+struct ls_spin_basis {
+  std::shared_ptr<sed::BasisData> d;
+};
+struct ls_states {
+  std::vector<uint64_t> data;
+};
+struct ls_interaction {
+  sed::InteractionData d;
+};
+struct ls_operator {
+  std::shared_ptr<sed::OperatorData> d;
+};

@@ -1,0 +1,156 @@
+"""ls_operator_matmat on the GPU against the oracle's pull-form matvec
+(src/SpinED/Internal.hs:411-429), in all four dtypes, for host and device
+buffers, strided blocks, both matvec forms, and ls_operator_expectation."""
+import numpy as np
+import pytest
+
+from _models import both, random_complex_term
+from spined import lattices
+from spined import _lib as L
+
+pytestmark = pytest.mark.gpu
+
+# FP64 results differ from the oracle only by summation order.
+RTOL64 = 1e-12
+RTOL32 = 2e-5
+
+
+def models():
+    rng = np.random.default_rng(11)
+    cx2 = random_complex_term(rng, 2)
+    cx3 = random_complex_term(rng, 3)
+    real3 = np.real(random_complex_term(rng, 3))
+    return {
+        "chain24": lattices.heisenberg_chain(24),
+        "chain20_j2": lattices.heisenberg_chain(20, j2=0.35),
+        "square4": lattices.heisenberg_square(4),
+        "square4_j2": lattices.heisenberg_square(4, j2=0.5),
+        "chain16_k5_complex": lattices.Model("c16k5", 16, 8, None, [(lattices.chain_translation(16), 5)],
+                                             [(cx2.tolist(), lattices.chain_bonds(16))]),
+        "chain12_3site": lattices.Model("c12t", 12, 6, 1, [(lattices.chain_translation(12), 0)],
+                                        [(real3.tolist(), [[i, (i + 1) % 12, (i + 2) % 12] for i in range(12)])]),
+        "chain10_3site_k2": lattices.Model("c10t", 10, None, None, [(lattices.chain_translation(10), 2)],
+                                           [(cx3.tolist(), [[i, (i + 1) % 10, (i + 3) % 10] for i in range(10)])]),
+        "field_1site_4site": lattices.Model("c8f", 8, None, None, [(lattices.chain_translation(8), 0)],
+                                            [([[0.3, 1.0], [1.0, -0.3]], [[i] for i in range(8)]),
+                                             (np.diag(np.arange(16) * 0.1).tolist(), [[i, (i + 1) % 8, (i + 2) % 8, (i + 3) % 8] for i in range(8)])]),
+    }
+
+
+MODELS = models()
+
+
+@pytest.mark.parametrize("name", list(MODELS))
+def test_matvec_matches_oracle(sed, oracle, name):
+    built, ob, oop = both(sed, oracle, MODELS[name])
+    D = len(ob.reps)
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=D) + (0 if oop.is_real else 1j * rng.normal(size=D))
+    want = oop.matvec(x)
+    scale = np.abs(want).max()
+    assert sed.is_operator_real(built.hamiltonian) == oop.is_real
+    dts = [np.complex128, np.complex64] + ([np.float64, np.float32] if oop.is_real else [])
+    for dt in dts:
+        xv = x.astype(dt) if np.iscomplexobj(np.zeros(1, dt)) else x.real.astype(dt)
+        y = sed.apply(built.hamiltonian, xv)
+        ref = oop.matvec(xv.astype(np.complex128))
+        tol = RTOL64 if dt in (np.float64, np.complex128) else RTOL32
+        if not np.iscomplexobj(y):
+            ref = ref.real
+        np.testing.assert_allclose(y, ref, rtol=0, atol=tol * scale * 4)
+
+
+def test_real_dtype_rejected_for_complex_operator(sed, oracle):
+    built, ob, oop = both(sed, oracle, MODELS["chain16_k5_complex"])
+    x = np.ones(len(ob.reps))
+    with pytest.raises(sed.LatticeSymmetriesException) as e:
+        sed.apply(built.hamiltonian, x)
+    assert e.value.code == L.LS_OPERATOR_IS_COMPLEX
+
+
+def test_dimension_mismatch(sed, oracle):
+    built, ob, oop = both(sed, oracle, MODELS["chain24"])
+    with pytest.raises(sed.LatticeSymmetriesException) as e:
+        sed.apply(built.hamiltonian, np.ones(len(ob.reps) - 1))
+    assert e.value.code == L.LS_DIMENSION_MISMATCH
+
+
+def test_block_with_strides(sed, oracle):
+    built, ob, oop = both(sed, oracle, MODELS["chain20_j2"])
+    D = len(ob.reps)
+    rng = np.random.default_rng(5)
+    big = np.asfortranarray(rng.normal(size=(D + 7, 3)))
+    x = big[:D, :]  # column stride D + 7
+    yb = np.asfortranarray(np.zeros((D + 3, 3)))
+    y = yb[:D, :]
+    sed.inplace_apply(built.hamiltonian, x, y)
+    for c in range(3):
+        np.testing.assert_allclose(y[:, c], oop.matvec(x[:, c]).real, atol=1e-11)
+    assert np.all(yb[D:, :] == 0)
+
+
+def test_forms_agree_bit_for_bit(sed, oracle):
+    """The on-the-fly and streamed forms sum the same elements in the same
+    order, so they agree exactly."""
+    import torch
+    built, ob, oop = both(sed, oracle, MODELS["square4_j2"])
+    D = len(ob.reps)
+    x = torch.randn(D, dtype=torch.float64, device="cuda")
+    y1 = torch.zeros_like(x)
+    y2 = torch.zeros_like(x)
+    lib = L.load()
+    import ctypes as C
+    torch.cuda.synchronize()
+    from spined.internal import check_status
+    op = built.hamiltonian
+    check_status(lib.sed_operator_prepare(op.ptr, L.SED_FORM_ON_THE_FLY))
+    assert op.stream_bytes == 0
+    sed.inplace_apply(op, x, y1)  # on-the-fly form
+    torch.cuda.synchronize()
+    assert op.stream_bytes == 0
+    op.prepare(L.SED_FORM_STREAM)
+    assert op.stream_bytes > 0 and op.stream_elements > 0
+    sed.inplace_apply(op, x, y2)  # streamed form
+    torch.cuda.synchronize()
+    assert torch.equal(y1, y2)
+    np.testing.assert_allclose(y2.cpu().numpy(), oop.matvec(x.cpu().numpy()).real, atol=1e-11)
+
+
+def test_device_pointers(sed, oracle):
+    import torch
+    built, ob, oop = both(sed, oracle, MODELS["chain24"])
+    D = len(ob.reps)
+    x = torch.randn(D, dtype=torch.float64, device="cuda")
+    y = sed.apply(built.hamiltonian, x)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(y.cpu().numpy(), oop.matvec(x.cpu().numpy()).real, atol=1e-10)
+
+
+def test_expectation(sed, oracle):
+    built, ob, oop = both(sed, oracle, MODELS["chain16_k5_complex"])
+    D = len(ob.reps)
+    rng = np.random.default_rng(9)
+    x = np.asfortranarray(rng.normal(size=(D, 2)) + 1j * rng.normal(size=(D, 2)))
+    got = sed.expectation(built.hamiltonian, x)
+    for c in range(2):
+        want = np.vdot(x[:, c], oop.matvec(x[:, c]))
+        assert got[c] == pytest.approx(want, rel=1e-11)
+
+
+def test_hermitian_property_large(sed, oracle):
+    """Size-independent check at 6x6 scale (D ~ 1.6e7): <x, H y> = <H x, y>
+    and linearity, through the device-pointer entry point."""
+    import torch
+    from spined.model import build_model
+    built = build_model(lattices.heisenberg_square(6))
+    D = sed.get_number_states(built.basis)
+    assert 15_700_000 < D < 15_800_000
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
+    y = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
+    hx, hy, hxy = sed.apply(built.hamiltonian, x), sed.apply(built.hamiltonian, y), sed.apply(built.hamiltonian, x + 2 * y)
+    torch.cuda.synchronize()
+    a = torch.dot(x, hy).item()
+    b = torch.dot(hx, y).item()
+    assert a == pytest.approx(b, rel=1e-10)
+    assert torch.allclose(hxy, hx + 2 * hy, rtol=0, atol=1e-9)
