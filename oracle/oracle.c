@@ -585,6 +585,28 @@ int or_matrix_coo(const or_operator* op, uint64_t D, const uint64_t* reps, const
   return OR_OK;
 }
 
+uint64_t or_row_work(const or_operator* op, const uint64_t* rows, uint64_t n_rows, uint64_t* n_elements) {
+  uint64_t sum = 0, count = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(^ : sum) reduction(+ : count)
+  for (uint64_t i = 0; i < n_rows; ++i) {
+    uint64_t r = rows[i];
+    for (unsigned t = 0; t < op->n_terms; ++t) {
+      const or_term* T = &op->terms[t];
+      for (unsigned u = 0; u < T->n_tuples; ++u) {
+        const uint16_t* st = T->sites + (size_t)u * T->k;
+        unsigned a = local_index(r, st, T->k);
+        for (unsigned q = 0; q < T->n_off[a]; ++q) {
+          unsigned ph;
+          sum ^= or_state_info(op->b, replace_local(r, st, T->k, T->off_col[a][q]), &ph, NULL) + ph;
+          ++count;
+        }
+      }
+    }
+  }
+  if (n_elements) *n_elements = count;
+  return sum;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the start vector.   */
 /* ------------------------------------------------------------------------ */

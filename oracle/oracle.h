@@ -103,6 +103,12 @@ int or_matvec(const or_operator* op, uint64_t D, const uint64_t* reps, const uns
 int or_matrix_coo(const or_operator* op, uint64_t D, const uint64_t* reps, const unsigned* weights,
                   uint64_t* rows, uint64_t* cols, double* vals, uint64_t capacity, uint64_t* nnz);
 
+/* Work of the on-the-fly matvec for the given rows without the index
+ * lookup (which needs the full representative list): generates every
+ * element and canonicalises it. Returns a checksum of the representatives
+ * found; used to time bounded samples of large bases on the CPU. */
+uint64_t or_row_work(const or_operator* op, const uint64_t* rows, uint64_t n_rows, uint64_t* n_elements);
+
 /* Philox4x32-10 (Salmon et al., SC'11). */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 /* Start vector: element i is uniform in [-1, 1) from Philox block i/2. */

@@ -79,6 +79,8 @@ def lib() -> C.CDLL:
         L.or_operator_destroy.argtypes = [p]
         L.or_matvec.argtypes = [p, u64, p, p, p, p, u64, u64]
         L.or_matrix_coo.argtypes = [p, u64, p, p, p, p, p, u64, C.POINTER(u64)]
+        L.or_row_work.argtypes = [p, p, u64, C.POINTER(u64)]
+        L.or_row_work.restype = u64
         L.or_philox4x32_10.argtypes = [p, p, p]
         L.or_start_vector.argtypes = [u64, u64, p]
         L.or_num_threads.restype = i
@@ -208,8 +210,8 @@ class Term:
 class Operator:
     """Operator in the symmetry-adapted basis (src/SpinED/Internal.hs:391-429)."""
 
-    def __init__(self, basis: Basis, terms: Sequence[Term]):
-        if basis.reps is None:
+    def __init__(self, basis: Basis, terms: Sequence[Term], build: bool = True):
+        if basis.reps is None and build:
             basis.build()
         self.basis = basis
         ks = np.array([t.k for t in terms], dtype=np.uint32)
@@ -233,7 +235,14 @@ class Operator:
 
     @property
     def dim(self) -> int:
-        return len(self.basis.reps)
+        return 0 if self.basis.reps is None else len(self.basis.reps)
+
+    def row_work(self, rows: np.ndarray) -> int:
+        """Element generation + canonicalisation for `rows` (no lookup); returns the element count."""
+        r = np.ascontiguousarray(rows, dtype=np.uint64)
+        n = C.c_uint64(0)
+        lib().or_row_work(self._h, _ptr(r), len(r), C.byref(n))
+        return n.value
 
     def matvec(self, x: np.ndarray, row_begin: int = 0, row_end: int | None = None) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.complex128)

@@ -105,7 +105,7 @@ __device__ __forceinline__ double row_diag<double>(uint64_t r, TermsView const& 
   for (uint32_t u = 0; u < T.n_tuples; ++u) {
     uint32_t const tk = T.tuple_term[u];
     uint32_t const t = tk & 0xFFFFu, k = tk >> 16;
-    d += T.diag[2 * (t * 16 + local_index(r, T.tuple_sites[u], k))];
+    d = __dadd_rn(d, T.diag[2 * (t * 16 + local_index(r, T.tuple_sites[u], k))]);
   }
   return d;
 }
@@ -116,8 +116,8 @@ __device__ __forceinline__ cplx row_diag<cplx>(uint64_t r, TermsView const& T) {
     uint32_t const tk = T.tuple_term[u];
     uint32_t const t = tk & 0xFFFFu, k = tk >> 16;
     uint32_t const a = local_index(r, T.tuple_sites[u], k);
-    d.re += T.diag[2 * (t * 16 + a)];
-    d.im += T.diag[2 * (t * 16 + a) + 1];
+    d.re = __dadd_rn(d.re, T.diag[2 * (t * 16 + a)]);
+    d.im = __dadd_rn(d.im, T.diag[2 * (t * 16 + a) + 1]);
   }
   return d;
 }

@@ -35,11 +35,16 @@ __device__ __forceinline__ void mac(cplx& acc, cplx a, cplx b) {
   acc.re = fma(a.re, b.re, fma(-a.im, b.im, acc.re));
   acc.im = fma(a.re, b.im, fma(a.im, b.re, acc.im));
 }
-__device__ __forceinline__ double mulv(double a, double b) { return a * b; }
-__device__ __forceinline__ cplx mulv(cplx a, cplx b) { return a * b; }
-__device__ __forceinline__ cplx mulv(double a, cplx b) { return a * b; }
-__device__ __forceinline__ double addv(double a, double b) { return a + b; }
-__device__ __forceinline__ cplx addv(cplx a, cplx b) { return a + b; }
+// Rounded products and sums (no contraction into FMA), so that every kernel
+// that evaluates the same expression gets the same bits.
+__device__ __forceinline__ double mulv(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ cplx mulv(cplx a, cplx b) {
+  return {__dsub_rn(__dmul_rn(a.re, b.re), __dmul_rn(a.im, b.im)),
+          __dadd_rn(__dmul_rn(a.re, b.im), __dmul_rn(a.im, b.re))};
+}
+__device__ __forceinline__ cplx mulv(double a, cplx b) { return {__dmul_rn(a, b.re), __dmul_rn(a, b.im)}; }
+__device__ __forceinline__ double addv(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ cplx addv(cplx a, cplx b) { return {__dadd_rn(a.re, b.re), __dadd_rn(a.im, b.im)}; }
 
 // Storage types of the four dtypes (src/SpinED/Internal.hs:404-409).
 template <class T>

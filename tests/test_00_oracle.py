@@ -171,3 +171,21 @@ def test_lattice_tables_match_reference_examples():
     perms = re.findall(r"permutation:\s*\[([^\]]*)\]", txt)
     assert ints(perms[0]) == lattices.chain_translation(40)
     assert ints(perms[1]) == lattices.chain_parity(40)
+
+
+@pytest.mark.parametrize("n,w,inv,k", [(12, 6, 1, 0), (12, 6, -1, 6), (14, 5, None, 3), (10, None, 1, 0), (16, 8, -1, 0)])
+def test_burnside_dimension_matches_enumeration(oracle, n, w, inv, k):
+    from _burnside import sector_dimension
+    gens = [([(i + 1) % n for i in range(n)], k)]
+    if k in (0, n // 2):
+        gens.append(([n - 1 - i for i in range(n)], 0))
+    b = oracle.Basis(n, w, inv, gens)
+    assert len(b.build()) == sector_dimension(b.group, n, w, inv)
+
+
+def test_burnside_square4(oracle):
+    from _burnside import sector_dimension
+    from spined import lattices
+    gens = [(g, 0) for g in lattices.square_symmetries(4)]
+    b = oracle.Basis(16, 8, 1, gens)
+    assert sector_dimension(b.group, 16, 8, 1) == 107 == len(b.build())

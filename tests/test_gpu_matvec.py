@@ -142,9 +142,12 @@ def test_hermitian_property_large(sed, oracle):
     and linearity, through the device-pointer entry point."""
     import torch
     from spined.model import build_model
-    built = build_model(lattices.heisenberg_square(6))
+    from _burnside import sector_dimension
+    m = lattices.heisenberg_square(6)
+    built = build_model(m)
     D = sed.get_number_states(built.basis)
-    assert 15_700_000 < D < 15_800_000
+    g = oracle.group_closure(36, m.symmetries)
+    assert D == sector_dimension(g, 36, 18, 1)  # 15,804,956
     g = torch.Generator(device="cuda").manual_seed(0)
     x = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
     y = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
