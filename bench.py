@@ -1,0 +1,381 @@
+"""Benchmark: time to the ground state of the 6x6 Heisenberg model on GB300.
+
+One step = one complete ground-state solve of the 36-site periodic square
+lattice (72 bonds, sigma.sigma exchange), sector Hamming weight 18,
+translations x C4v x spin inversion, all characters +1 (D = 15,804,956):
+basis enumeration on the GPU (ls_build), recording of the stream form of the
+Hamiltonian, and plain FP64 Lanczos from the Philox seed-1234 start vector to
+||H psi - E psi|| <= 1e-8, Ritz vector included.
+
+  value  seconds per solve, inputs (the lattice description) already on the
+         device side of the API; CUDA events on the current stream
+  e2e    the same solve through the public C ABI from host arrays, with the
+         representatives and the eigenvector copied back to pinned host memory
+  roofline  the streamed SpMV (the hot kernel of the Lanczos loop): algorithmic
+         bytes per launch / its CUDA-event duration against the measured HBM
+         copy bandwidth
+  cpu_baseline  the CPU restatement (oracle/) on the host cores, on bounded
+         samples of the same workload, extrapolated to one solve
+
+`--impl reference` times the reference's CPU path (the oracle restatement;
+the reference itself cannot be built without GHC) on the same workload.
+Multi-GPU runs are replicas (one independent solve per rank).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "spin-ed_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "time-to-ground-state (resid<=1e-8) vs plain FP64 GPU Lanczos; matvec HBM GB/s"
+# Lanczos steps the plain FP64 method needs on the 6x6 workload from the
+# seed-1234 Philox start vector (the CPU restatement runs the same algorithm
+# from the same start vector and needs the same number of matvecs).
+SQUARE6_STEPS = 57  # 56 Lanczos steps + the final residual check
+
+
+def workload_model(name: str, hamming_weight: int | None = None):
+    from spined import lattices
+    if name == "square6":
+        m = lattices.heisenberg_square(6)
+        if hamming_weight is not None:  # smaller sector of the same lattice (profiling)
+            m.hamming_weight, m.spin_inversion = hamming_weight, (1 if 2 * hamming_weight == 36 else None)
+        return m
+    if name == "chain24":
+        return lattices.heisenberg_chain(24)
+    if name == "square4":
+        return lattices.heisenberg_square(4)
+    if name == "chain32":
+        return lattices.heisenberg_chain(32)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ GPU --
+
+def gpu_arm(args, rank, world, dist):
+    import numpy as np
+    import torch
+    from spined import internal as I
+    from spined import _lib as L
+    from spined.model import build_model
+
+    dev = torch.cuda.current_device()
+    lib = L.load()
+    m = workload_model(args.workload)
+    # A dedicated stream: the legacy default stream does not order work that
+    # libsed enqueues on its own non-blocking streams.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def solve_device(built):
+        """One step: build basis, record stream form, Lanczos (device output)."""
+        I.build_basis(built.basis)
+        op = I.mk_operator(built.basis, built.interactions)
+        op.prepare(L.SED_FORM_STREAM)
+        D = I.get_number_states(built.basis)
+        out = torch.empty(D, dtype=torch.float64, device="cuda")
+        res = I.eigh(op, tol=1e-8, seed=1234, out=out, precision=args.precision_code)
+        return op, res
+
+    built = build_model(m, build=False)
+    # warm-up
+    for _ in range(args.warmup):
+        op, res = solve_device(built)
+        del op
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches0 = lib.sed_kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times, phases = [], []
+    with Clocks(dev) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            op, res = solve_device(built)
+            phases.append({"solve_s": res.seconds_total, "record_s": res.seconds_setup,
+                           "lanczos_steps": res.iterations, "restarts": res.restarts,
+                           "wall_s": time.perf_counter() - t0})
+            last = (op, res)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.sed_kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    op, res = last
+    D = I.get_number_states(built.basis)
+
+    # End to end through the C ABI from host arrays (fresh objects each step).
+    pin_v = torch.empty(D, dtype=torch.float64, pin_memory=True)
+    e2e_times = []
+    h2d = 0
+    for s in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b2 = build_model(m, build=False)  # copies the permutations/matrices/sites in
+        I.build_basis(b2.basis)
+        reps = I.basis_get_states(b2.basis)  # /basis/representatives, src/SpinED.hs:334-337
+        r2 = I.eigh(b2.hamiltonian, tol=1e-8, seed=1234, out=pin_v.numpy().reshape(D, 1, order="F"),
+                    precision=args.precision_code)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        h2d = sum(len(p) * 4 + 4 for p, _ in m.symmetries) + sum(
+            16 * len(mat) ** 2 + 2 * len(sites) * len(sites[0]) for mat, sites in m.terms)
+        del b2
+    e2e_s = statistics.median(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = t.item()
+    d2h = D * 8 * 2 + 16
+
+    # Roofline of the streamed SpMV: CUDA events on the launching stream.
+    x = torch.randn(D, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    h = C.c_void_p(stream.cuda_stream)
+    for _ in range(5):
+        I.check_status(lib.sed_operator_matmat_device(op.ptr, 1, D, 1, C.c_void_p(x.data_ptr()), D,
+                                                      C.c_void_p(y.data_ptr()), D, h))
+    reps_n = 30
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps_n):
+        lib.sed_operator_matmat_device(op.ptr, 1, D, 1, C.c_void_p(x.data_ptr()), D, C.c_void_p(y.data_ptr()), D, h)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    spmv_ms = e0.elapsed_time(e1) / reps_n
+    E_tot = op.stream_elements
+    s_bytes = 8
+    alg = E_tot * 4 + D * 9 + D * s_bytes + E_tot * s_bytes + D * s_bytes  # SURVEY 8d form for the stream matvec
+    compulsory = E_tot * 4 + D * 9 + 2 * D * s_bytes
+    peak, peak_kind = peaks()
+    achieved = alg / (spmv_ms * 1e-3) / 1e9
+    return {
+        "ms": ms, "D": D, "E_tot": E_tot, "phases": phases, "launches": launches / args.steps,
+        "clocks": clk.summary(), "e2e_s": e2e_s, "h2d": h2d, "d2h": d2h,
+        "spmv_ms": spmv_ms, "alg_bytes": alg, "compulsory_bytes": compulsory, "achieved": achieved,
+        "peak": peak, "peak_kind": peak_kind, "stream_bytes": op.stream_bytes,
+        "E0": float(res.eigenvalues[0]), "residual": float(res.residuals[0]),
+        "steps_lanczos": res.iterations,
+    }
+
+
+# ------------------------------------------------------------------ CPU --
+
+def cpu_sample(workload: str, budget_s: float = 8.0):
+    """Times the CPU restatement on bounded samples of the workload and
+    extrapolates one solve: basis scan + SQUARE6_STEPS on-the-fly matvecs."""
+    import numpy as np
+    import oracle as O
+    m = workload_model(workload)
+    b = O.Basis(m.number_spins, m.hamming_weight, m.spin_inversion, m.symmetries)
+    space = b.space_size()
+    # Basis: 8 slices spread over the word space.
+    slices, per = 8, 1 << 16
+    while True:
+        t0 = time.perf_counter()
+        reps = []
+        for k in range(slices):
+            start = (space // slices) * k
+            reps.append(b.build(start, start + per))
+        tb = time.perf_counter() - t0
+        if tb > budget_s / 2 or per >= space // slices:
+            break
+        per *= 4
+    scanned = slices * per
+    t_basis = tb * space / scanned
+    D_est = sum(len(r) for r in reps) * space / scanned
+    rows = np.concatenate(reps)
+    op = O.Operator(b, [O.Term(np.array(a, dtype=complex), np.array(s)) for a, s in m.terms], build=False)
+    n = min(len(rows), 2000)
+    while True:
+        t0 = time.perf_counter()
+        ne = op.row_work(rows[:n])
+        tm = time.perf_counter() - t0
+        if tm > budget_s / 2 or n >= len(rows):
+            break
+        n = min(len(rows), n * 4)
+    D = 15_804_956 if workload == "square6" else D_est
+    t_matvec = tm * D / n
+    steps = SQUARE6_STEPS
+    total = t_basis + steps * t_matvec
+    return {
+        "value": total, "cores": O.num_threads(), "t_basis_s": t_basis, "t_matvec_s": t_matvec,
+        "sample": (f"basis: {slices} slices x {per} words of {space} (fraction {scanned / space:.2e}); "
+                   f"matvec: element generation + canonicalisation of {n} sampled rows "
+                   f"({ne} elements; index lookups excluded); solve = basis + {steps} matvecs"),
+    }
+
+
+def reference_arm(args, rank):
+    if rank != 0:
+        return
+    t_all = time.perf_counter()
+    samples = []
+    for _ in range(args.warmup):
+        cpu_sample(args.workload, budget_s=args.cpu_budget)
+    for _ in range(args.steps):
+        samples.append(cpu_sample(args.workload, budget_s=args.cpu_budget))
+    v = statistics.median(s["value"] for s in samples)
+    s0 = samples[0]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (lattice generated in code)",
+        "config": {"workload": args.workload},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": s0["cores"], "kind": "port", "sample": s0["sample"]},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement (oracle/), not the reference binary: GHC and the unpinned "
+                "lattice-symmetries/PRIMME sources are unavailable",
+        "bench_wall_s": time.perf_counter() - t_all,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- main --
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="square6")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-budget", type=float, default=6.0, help="seconds of CPU work per baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
+    ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
+    args = ap.parse_args()
+    args.precision_code = 0 if args.precision == "fp64" else 1
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return reference_arm(args, rank)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group("nccl")
+        dist = tdist
+    import __graft_entry__ as g
+    g.build()
+    if args.once:
+        from spined import internal as I
+        from spined.model import build_model
+        b = build_model(workload_model(args.workload, args.hamming_weight))
+        r = I.eigh(b.hamiltonian, tol=1e-8, seed=1234, precision=args.precision_code)
+        torch.cuda.synchronize()
+        print(json.dumps({"D": I.get_number_states(b.basis), "E0": float(r.eigenvalues[0]),
+                          "residual": float(r.residuals[0]), "steps": r.iterations}))
+        return
+    r = gpu_arm(args, rank, world, dist)
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            c = cpu_sample(args.workload, budget_s=args.cpu_budget)
+            cpu = {"value": c["value"], "unit": "s", "cores": c["cores"], "kind": "port", "sample": c["sample"]}
+        ph = r["phases"][-1]
+        line = {
+            "metric": METRIC, "value": r["ms"] / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-stored/f64",
+            "data": "synthetic (lattice generated in code; no dataset)",
+            "config": {"workload": f"{args.workload}: Heisenberg, D={r['D']}, plain FP64 Lanczos to resid<=1e-8, seed 1234"
+                       if args.precision == "fp64" else f"{args.workload}: mixed precision",
+                       "D": r["D"], "elements_per_matvec": r["E_tot"], "parallelism": f"replicas x{world}",
+                       "l2": "working set (stream form %.2f GB) exceeds L2" % (r["stream_bytes"] / 1e9)},
+            "gpu_launches": r["launches"],
+            "e2e": {"value": r["e2e_s"], "unit": "s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+            "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
+                         "frac": r["achieved"] / r["peak"], "traffic": None,
+                         "kernel": "k_spmv (streamed SELL-32 SpMV, FP64)", "spmv_ms": r["spmv_ms"],
+                         "alg_bytes": r["alg_bytes"], "compulsory_bytes": r["compulsory_bytes"],
+                         "peak_kind": r["peak_kind"]},
+            "clocks": r["clocks"],
+            "result": {"E0": r["E0"], "residual": r["residual"], "lanczos_steps": r["steps_lanczos"],
+                       "phases_last_step": ph},
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -255,6 +255,10 @@ SED_API int sed_basis_index(ls_spin_basis const* basis, uint64_t representative,
 SED_API int sed_basis_state_info(ls_spin_basis const* basis, uint64_t bits, uint64_t* representative,
                          unsigned* phase, unsigned* phase_modulus);
 
+/* Number of libsed kernels launched by this process so far (graph replays
+ * count their kernel nodes). */
+SED_API uint64_t sed_kernel_launches(void);
+
 /* Version string of the library (static storage). */
 SED_API char const* sed_version(void);
 

@@ -237,8 +237,8 @@ int basis_build_index(BasisData& b, cudaStream_t stream) {
   b.prefix_shift = bitlen > b.prefix_bits ? bitlen - b.prefix_bits : 0;
   uint64_t const n_keys = (uint64_t)1 << b.prefix_bits;
   if (int st = b.prefix.allocate((n_keys + 1) * 8)) return st;
-  k_prefix<<<grid_for(n_keys + 1, b.device), kThreads, 0, stream>>>(
-      b.reps.as<uint64_t>(), b.D, b.prefix_shift, n_keys, b.prefix.as<uint64_t>());
+  { k_prefix<<<grid_for(n_keys + 1, b.device), kThreads, 0, stream>>>(
+      b.reps.as<uint64_t>(), b.D, b.prefix_shift, n_keys, b.prefix.as<uint64_t>()); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   return LS_SUCCESS;
 }
@@ -274,13 +274,13 @@ int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
     if (given_size) {
       unsigned const grid = grid_for(given_size, b.device);
       if (wide)
-        k_check_reps<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), given_size,
+        { k_check_reps<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), given_size,
                                                              b.weights.as<uint32_t>(), b.n, b.hw,
-                                                             bad.as<uint32_t>());
+                                                             bad.as<uint32_t>()); note_launches(1); }
       else
-        k_check_reps<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), given_size,
+        { k_check_reps<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), given_size,
                                                              b.weights.as<uint32_t>(), b.n, b.hw,
-                                                             bad.as<uint32_t>());
+                                                             bad.as<uint32_t>()); note_launches(1); }
       SED_TRY_CUDA(cudaGetLastError());
     }
     uint32_t bad_h = 0;
@@ -309,18 +309,18 @@ int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
     if (int st = tiles.allocate((n_tiles + 1) * 8)) return st;
     unsigned const grid = grid_for(n_words, b.device) * 4;
     if (wide)
-      k_mark<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
-                                                       n_words, bitmap.as<uint32_t>());
+      { k_mark<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
+                                                       n_words, bitmap.as<uint32_t>()); note_launches(1); }
     else
-      k_mark<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
-                                                       n_words, bitmap.as<uint32_t>());
+      { k_mark<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
+                                                       n_words, bitmap.as<uint32_t>()); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
     if (n_tiles) {
-      k_tile_counts<<<(unsigned)n_tiles, kThreads, 0, stream>>>(bitmap.as<uint32_t>(), n_words,
-                                                                tiles.as<uint64_t>());
+      { k_tile_counts<<<(unsigned)n_tiles, kThreads, 0, stream>>>(bitmap.as<uint32_t>(), n_words,
+                                                                tiles.as<uint64_t>()); note_launches(1); }
       SED_TRY_CUDA(cudaGetLastError());
     }
-    k_scan_serial<<<1, 1024, 0, stream>>>(tiles.as<uint64_t>(), n_tiles);
+    { k_scan_serial<<<1, 1024, 0, stream>>>(tiles.as<uint64_t>(), n_tiles); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
     uint64_t D = 0;
     SED_TRY_CUDA(cudaMemcpyAsync(&D, tiles.as<uint64_t>() + n_tiles, 8, cudaMemcpyDeviceToHost, stream));
@@ -330,13 +330,13 @@ int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
     if (int st = b.weights.allocate(std::max<uint64_t>(1, D) * 4)) return st;
     if (n_tiles) {
       if (wide)
-        k_write<uint64_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
+        { k_write<uint64_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
             P, b.binom.as<uint64_t>(), b.n, b.hw, space, bitmap.as<uint32_t>(), n_words,
-            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>());
+            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>()); note_launches(1); }
       else
-        k_write<uint32_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
+        { k_write<uint32_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
             P, b.binom.as<uint64_t>(), b.n, b.hw, space, bitmap.as<uint32_t>(), n_words,
-            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>());
+            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>()); note_launches(1); }
       SED_TRY_CUDA(cudaGetLastError());
     }
     SED_TRY_CUDA(cudaStreamSynchronize(stream));

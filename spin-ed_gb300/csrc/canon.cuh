@@ -32,6 +32,14 @@ constexpr unsigned SED_MAX_TERMS = 4;    // displacements per element of H
 constexpr unsigned SED_MAX_STAGES = 11;  // Benes stages for 64 bits
 
 struct PlanView {
+  // When cyc > 0, H = <g1> x <g2> (cyc = number of generators) is walked by
+  // nested loops that apply the generators' two-term shift decompositions
+  // held right here (kernel-parameter space): no memory traffic per image.
+  uint32_t cyc;
+  uint32_t cyc_ord[2];
+  uint32_t cyc_phase[2];
+  uint32_t cyc_rot[2][2];
+  uint64_t cyc_mask[2][2];
   uint64_t mask;
   uint32_t n_bits;
   int32_t inv;  // 0 none, +1 / -1
@@ -105,12 +113,50 @@ struct Canon {
   uint32_t phase;  // character of the element mapping x to rep: exp(-2 pi i phase / L)
 };
 
+template <class W>
+SED_HD W apply2(W y, uint64_t m0, uint64_t m1, unsigned r0, unsigned r1) {
+  return rotl<W>(y & (W)m0, r0) | rotl<W>(y & (W)m1, r1);
+}
+
 // Orbit minimum of x and the phase of an element mapping x onto it.
 template <class W>
 SED_HD Canon<W> canonicalize(W x, PlanView const& P) {
   W best = x;
-  uint32_t bc = 0, bh = 0, binv = 0;
   W const mask = (W)P.mask;
+  if (P.cyc) {
+    // candidate index: ((c * o1) + a) * o2 + b, bit 31 = inversion
+    uint32_t const o1 = P.cyc_ord[0], o2 = P.cyc_ord[1];
+    uint32_t bc = 0, cand = 0;
+    for (uint32_t c = 0; c < P.n_cosets; ++c) {
+      W y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
+                           c == 0 ? 0u : P.n_stages);
+      for (uint32_t a = 0; a < o1; ++a) {
+        W z = y;
+        for (uint32_t b = 0; b < o2; ++b, ++cand) {
+          if (z < best) {
+            best = z;
+            bc = cand;
+          }
+          if (P.inv) {
+            W const zi = ~z & mask;
+            if (zi < best) {
+              best = zi;
+              bc = cand | 0x80000000u;
+            }
+          }
+          z = apply2<W>(z, P.cyc_mask[1][0], P.cyc_mask[1][1], P.cyc_rot[1][0], P.cyc_rot[1][1]);
+        }
+        y = apply2<W>(y, P.cyc_mask[0][0], P.cyc_mask[0][1], P.cyc_rot[0][0], P.cyc_rot[0][1]);
+      }
+    }
+    uint32_t const k = bc & 0x7FFFFFFFu;
+    uint32_t const c = k / (o1 * o2), rem = k % (o1 * o2);
+    uint32_t const a = rem / o2, b = rem % o2;
+    uint64_t ph = (uint64_t)P.coset_phase[c] + (uint64_t)a * P.cyc_phase[0] + (uint64_t)b * P.cyc_phase[1];
+    if (bc >> 31) ph += P.inv_phase;
+    return {best, (uint32_t)(ph % P.L)};
+  }
+  uint32_t bc = 0, bh = 0, binv = 0;
   for (uint32_t c = 0; c < P.n_cosets; ++c) {
     W const y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
                                c == 0 ? 0u : P.n_stages);
@@ -144,6 +190,38 @@ template <class W>
 SED_HD uint32_t representative_weight(W x, PlanView const& P) {
   uint32_t S = 0;
   W const mask = (W)P.mask;
+  if (P.cyc) {
+    uint32_t const o1 = P.cyc_ord[0], o2 = P.cyc_ord[1];
+    for (uint32_t c = 0; c < P.n_cosets; ++c) {
+      W y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
+                           c == 0 ? 0u : P.n_stages);
+      uint32_t pa = P.coset_phase[c];
+      for (uint32_t a = 0; a < o1; ++a) {
+        W z = y;
+        uint32_t pb = pa;
+        for (uint32_t b = 0; b < o2; ++b) {
+          if (z < x) return 0;
+          if (z == x) {
+            if (pb != 0) return 0;
+            ++S;
+          }
+          if (P.inv) {
+            W const zi = ~z & mask;
+            if (zi < x) return 0;
+            if (zi == x) {
+              if (add_phase(pb, P.inv_phase, P.L) != 0) return 0;
+              ++S;
+            }
+          }
+          z = apply2<W>(z, P.cyc_mask[1][0], P.cyc_mask[1][1], P.cyc_rot[1][0], P.cyc_rot[1][1]);
+          pb = add_phase(pb, P.cyc_phase[1], P.L);
+        }
+        y = apply2<W>(y, P.cyc_mask[0][0], P.cyc_mask[0][1], P.cyc_rot[0][0], P.cyc_rot[0][1]);
+        pa = add_phase(pa, P.cyc_phase[0], P.L);
+      }
+    }
+    return S;
+  }
   for (uint32_t c = 0; c < P.n_cosets; ++c) {
     W const y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
                                c == 0 ? 0u : P.n_stages);

@@ -16,6 +16,8 @@ namespace {
 thread_local int t_last_status = 0;
 thread_local std::string t_last_message;
 std::atomic<bool> g_logging{false};
+std::atomic<uint64_t> g_launches{0};
+thread_local bool t_capturing = false;
 
 char const* describe(int status) {
   switch (status) {
@@ -59,6 +61,10 @@ int fail(int status, std::string const& message) {
 }
 
 std::string last_message() { return t_last_message; }
+void note_launches(uint64_t n) {
+  if (!t_capturing) g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+void set_capturing(bool on) { t_capturing = on; }
 bool logging_enabled() { return g_logging.load(std::memory_order_relaxed); }
 
 void log_line(char const* fmt, ...) {
@@ -140,5 +146,6 @@ void ls_destroy_string(char const* message) { std::free(const_cast<char*>(messag
 void ls_enable_logging(void) { g_logging.store(true); }
 void ls_disable_logging(void) { g_logging.store(false); }
 char const* sed_version(void) { return "libsed 0.1.0 (sm_103a)"; }
+uint64_t sed_kernel_launches(void) { return g_launches.load(); }
 
 }  // extern "C"

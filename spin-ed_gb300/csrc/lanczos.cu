@@ -593,6 +593,7 @@ struct Solver {
   unsigned spmv_blocks = 0;
   unsigned vblocks = 0;
   cudaGraphExec_t graph = nullptr;
+  size_t graph_kernels = 0;
   LzHeader* hh = nullptr;  // pinned host mirror
 
   Solver(OperatorData& o, int dt, cudaStream_t s) : op(o), dtype(dt), D(o.basis->D), stream(s) {}
@@ -638,30 +639,30 @@ struct Solver {
   // One Lanczos step (all kernels read k from the header).
   int enqueue_step() {
     LzHeader* h = hdr();
-    k_zero_alpha<X><<<1, 1, 0, stream>>>(h, ws.alpha.as<double>());
+    { k_zero_alpha<X><<<1, 1, 0, stream>>>(h, ws.alpha.as<double>()); note_launches(1); }
     Indirect ind;
     ind.k = &h->k;
     ind.stop = &h->stop;
     ind.ld = D;
     ind.partial = ws.partial.as<double>();
     if (int st = operator_apply_krylov(op, dtype, V(), ind, stream, &spmv_blocks)) return st;
-    k_reduce<<<1, kRedThreads, 0, stream>>>(ws.partial.as<double>(), spmv_blocks, h, ws.alpha.as<double>(), 0);
-    k_update<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.alpha.as<double>(), ws.beta.as<double>(),
-                                                ws.partial.as<double>());
+    { k_reduce<<<1, kRedThreads, 0, stream>>>(ws.partial.as<double>(), spmv_blocks, h, ws.alpha.as<double>(), 0); note_launches(1); }
+    { k_update<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.alpha.as<double>(), ws.beta.as<double>(),
+                                                ws.partial.as<double>()); note_launches(1); }
     if (hh->reorth) {
       for (int pass = 0; pass < 2; ++pass) {
         dim3 grid(vblocks, (m_max + 15) / 16);
-        k_cgs_dots<X><<<grid, kBlock, 0, stream>>>(V(), D, D, h, ws.cgs_partial.as<double>());
-        k_cgs_reduce<<<1, kRedThreads, 0, stream>>>(ws.cgs_partial.as<double>(), vblocks, h,
-                                                    ws.coef.as<double>(), ws.alpha.as<double>());
-        k_cgs_update<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.coef.as<double>(),
-                                                        ws.partial.as<double>());
+        { k_cgs_dots<X><<<grid, kBlock, 0, stream>>>(V(), D, D, h, ws.cgs_partial.as<double>()); note_launches(1); }
+        { k_cgs_reduce<<<1, kRedThreads, 0, stream>>>(ws.cgs_partial.as<double>(), vblocks, h,
+                                                    ws.coef.as<double>(), ws.alpha.as<double>()); note_launches(1); }
+        { k_cgs_update<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.coef.as<double>(),
+                                                        ws.partial.as<double>()); note_launches(1); }
       }
     }
-    k_reduce<<<1, kRedThreads, 0, stream>>>(ws.partial.as<double>(), vblocks, h, ws.beta.as<double>(), 1);
-    k_scale_next<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.beta.as<double>());
-    k_tridiag<<<1, 32, 0, stream>>>(h, ws.alpha.as<double>(), ws.beta.as<double>(), ws.s.as<double>(),
-                                    ws.work.as<double>());
+    { k_reduce<<<1, kRedThreads, 0, stream>>>(ws.partial.as<double>(), vblocks, h, ws.beta.as<double>(), 1); note_launches(1); }
+    { k_scale_next<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.beta.as<double>()); note_launches(1); }
+    { k_tridiag<<<1, 32, 0, stream>>>(h, ws.alpha.as<double>(), ws.beta.as<double>(), ws.s.as<double>(),
+                                    ws.work.as<double>()); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
     return LS_SUCCESS;
   }
@@ -669,14 +670,19 @@ struct Solver {
   int capture(uint32_t steps) {
     cudaGraph_t g;
     SED_TRY_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
     int st = LS_SUCCESS;
     for (uint32_t i = 0; i < steps && st == LS_SUCCESS; ++i) st = enqueue_step();
+    set_capturing(false);
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (st) {
       if (e == cudaSuccess) cudaGraphDestroy(g);
       return st;
     }
     SED_TRY_CUDA(e);
+    size_t n_nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &n_nodes);
+    graph_kernels = n_nodes;
     e = cudaGraphInstantiate(&graph, g, 0);
     cudaGraphDestroy(g);
     SED_TRY_CUDA(e);
@@ -706,10 +712,10 @@ struct Solver {
     if (!ws.scratch.ptr || ws.scratch.bytes < D * es)
       if (int st = ws.scratch.allocate(D * es)) return st;
     switch (out_dtype) {
-      case 0: k_convert<X, float><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<float>()); break;
-      case 1: k_convert<X, double><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<double>()); break;
-      case 2: k_convert<X, float2><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<float2>()); break;
-      default: k_convert<X, double2><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<double2>()); break;
+      case 0: { k_convert<X, float><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<float>()); note_launches(1); } break;
+      case 1: { k_convert<X, double><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<double>()); note_launches(1); } break;
+      case 2: { k_convert<X, float2><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<float2>()); note_launches(1); } break;
+      default: { k_convert<X, double2><<<vblocks, kBlock, 0, stream>>>(x, D, ws.scratch.as<double2>()); note_launches(1); } break;
     }
     SED_TRY_CUDA(cudaGetLastError());
     SED_TRY_CUDA(cudaMemcpyAsync(dst, ws.scratch.ptr, D * es, cudaMemcpyDefault, stream));
@@ -719,14 +725,14 @@ struct Solver {
 
   // ||x||, normalises x in place.
   int normalise_vec(X* x, double* out_norm) {
-    k_dots<X><<<vblocks, kBlock, 0, stream>>>(x, x, D, 0.0, 0, ws.partial.as<double>());
+    { k_dots<X><<<vblocks, kBlock, 0, stream>>>(x, x, D, 0.0, 0, ws.partial.as<double>()); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
     int st = LS_SUCCESS;
     double const n2 = host_sum<X>(ws.partial, vblocks, 2, 0, stream, &st);
     if (st) return st;
     double const nrm = std::sqrt(n2);
     if (!(nrm > 0.0)) return fail(LS_INVALID_ARGUMENT, "start vector is zero");
-    k_scale<X><<<vblocks, kBlock, 0, stream>>>(x, D, 1.0 / nrm);
+    { k_scale<X><<<vblocks, kBlock, 0, stream>>>(x, D, 1.0 / nrm); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
     if (out_norm) *out_norm = nrm;
     return LS_SUCCESS;
@@ -735,7 +741,7 @@ struct Solver {
   // y = H x with residual: returns E = <x,Hx>/<x,x> and ||Hx - E x||/||x||.
   int residual(X* x, double* E, double* r) {
     if (int st = operator_apply_device(op, dtype, 1, x, D, ws.y.ptr, D, stream, SED_FORM_AUTO)) return st;
-    k_dots<X><<<vblocks, kBlock, 0, stream>>>(x, ws.y.as<X>(), D, 0.0, 0, ws.partial.as<double>());
+    { k_dots<X><<<vblocks, kBlock, 0, stream>>>(x, ws.y.as<X>(), D, 0.0, 0, ws.partial.as<double>()); note_launches(1); }
     int st = LS_SUCCESS;
     std::vector<double> h(2 * (size_t)vblocks);
     SED_TRY_CUDA(cudaMemcpyAsync(h.data(), ws.partial.ptr, h.size() * 8, cudaMemcpyDeviceToHost, stream));
@@ -746,7 +752,7 @@ struct Solver {
       xy += h[2 * i + 1];
     }
     *E = xy / xx;
-    k_dots<X><<<vblocks, kBlock, 0, stream>>>(x, ws.y.as<X>(), D, *E, 1, ws.partial.as<double>());
+    { k_dots<X><<<vblocks, kBlock, 0, stream>>>(x, ws.y.as<X>(), D, *E, 1, ws.partial.as<double>()); note_launches(1); }
     double const rr = host_sum<X>(ws.partial, vblocks, 2, 0, stream, &st);
     if (st) return st;
     *r = std::sqrt(rr / xx);
@@ -802,7 +808,7 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
     size_t const es = sizeof(X);
     SED_TRY_CUDA(cudaMemcpyAsync(S.V(), o.start_vectors, D * es, cudaMemcpyDefault, stream));
   } else {
-    k_random<X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, o.seed);
+    { k_random<X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, o.seed); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
   }
   if (int st = S.normalise_vec(S.V(), nullptr)) return st;
@@ -813,6 +819,7 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
   std::vector<double> theta_h(nev), est_h(nev);
   while (!converged) {
     SED_TRY_CUDA(cudaGraphLaunch(S.graph, stream));
+    note_launches(S.graph_kernels);
     if (int st = S.read_header()) return st;
     if (o.progress) {
       for (uint32_t j = 0; j < nev; ++j) {
@@ -832,8 +839,8 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
     // Ritz vectors and their true residuals.
     bool all_ok = true;
     for (uint32_t j = 0; j < nev; ++j) {
-      k_ritz<X, X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, D, S.ws.s.template as<double>() + (uint64_t)j * m,
-                                                     n, S.ws.ritz.template as<X>());
+      { k_ritz<X, X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, D, S.ws.s.template as<double>() + (uint64_t)j * m,
+                                                     n, S.ws.ritz.template as<X>()); note_launches(1); }
       SED_TRY_CUDA(cudaGetLastError());
       if (int st = S.normalise_vec(S.ws.ritz.template as<X>(), nullptr)) return st;
       double e = 0.0, r = 0.0;
@@ -855,7 +862,7 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
     if (nev == 1) {
       SED_TRY_CUDA(cudaMemcpyAsync(S.V(), S.ws.ritz.ptr, D * sizeof(X), cudaMemcpyDeviceToDevice, stream));
     } else {
-      k_ritz<X, X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, D, S.ws.s.template as<double>(), n, S.ws.ritz.template as<X>());
+      { k_ritz<X, X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, D, S.ws.s.template as<double>(), n, S.ws.ritz.template as<X>()); note_launches(1); }
       // sum of all nev Ritz directions
       std::vector<double> ones(n, 0.0);
       std::vector<double> sh((size_t)nev * m);
@@ -863,8 +870,8 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
       for (uint32_t j = 0; j < nev; ++j)
         for (uint32_t i = 0; i < n; ++i) ones[i] += sh[(size_t)j * m + i];
       SED_TRY_CUDA(cudaMemcpy(S.ws.work.ptr, ones.data(), n * 8, cudaMemcpyHostToDevice));
-      k_ritz<X, X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, D, S.ws.work.template as<double>(), n,
-                                                     S.ws.ritz.template as<X>());
+      { k_ritz<X, X><<<S.vblocks, kBlock, 0, stream>>>(S.V(), D, D, S.ws.work.template as<double>(), n,
+                                                     S.ws.ritz.template as<X>()); note_launches(1); }
       SED_TRY_CUDA(cudaMemcpyAsync(S.V(), S.ws.ritz.ptr, D * sizeof(X), cudaMemcpyDeviceToDevice, stream));
     }
     if (int st = S.normalise_vec(S.V(), nullptr)) return st;

@@ -44,33 +44,91 @@ __global__ void k_count(uint64_t const* __restrict__ reps, uint64_t D, TermsView
   }
 }
 
+constexpr unsigned kRecWarps = 4;    // warps per block of k_record
+constexpr unsigned kRecMaxElems = 96; // flattened path: elements per row
+
+// Records the stream form. One warp per SELL-32 slice. When the slice is at
+// most kRecMaxElems wide, each lane first lists its row's elements as
+// (tuple, column) descriptors in shared memory and the warp then walks the
+// flattened (row, element) list 32 at a time, so rows of different length do
+// not leave lanes idle; wider slices fall back to one row per lane. Entries
+// land in the same slots (slice_ptr + 32 e + row) either way.
 template <class W, bool Real>
-__global__ void k_record(PlanView P, IndexView I, TermsView T, CodeView C,
-                         uint32_t const* __restrict__ weights, uint64_t n_slices,
-                         uint64_t const* __restrict__ slice_ptr, uint32_t col_bits, bool packed,
-                         uint32_t* __restrict__ entries, uint16_t* __restrict__ codes,
-                         void* __restrict__ diag, uint8_t* __restrict__ row_class) {
-  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t const s = i >> 5;
-  if (s >= n_slices) return;
-  uint32_t const lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(kRecWarps * 32)
+    k_record(PlanView P, IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
+             uint64_t n_slices, uint64_t const* __restrict__ slice_ptr, uint32_t col_bits, bool packed,
+             uint32_t* __restrict__ entries, uint16_t* __restrict__ codes, void* __restrict__ diag,
+             uint8_t* __restrict__ row_class) {
+  __shared__ uint32_t desc[kRecWarps][32][kRecMaxElems];  // q << 28 | tuple << 8 | column a'
+  uint32_t const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t const s = (uint64_t)blockIdx.x * kRecWarps + warp;
+  if (s >= n_slices) return;  // warp-uniform
+  uint64_t const i = s * 32 + lane;
   uint64_t const base = slice_ptr[s];
   uint32_t const width = (uint32_t)((slice_ptr[s + 1] - base) >> 5);
-  uint32_t used = 0;
-  if (i < I.D) {
-    uint64_t const r = I.reps[i];
-    walk_row(r, T, [&](uint32_t e, uint64_t st, uint32_t vid) {
-      auto const c = canonicalize<W>((W)st, P);
-      int64_t const j = find_index((uint64_t)c.rep, I);
-      uint32_t ent = kNull, code = 0;
-      if (j >= 0) {
-        code = element_code(vid, c.phase, weights[j], C);
-        ent = packed ? ((uint32_t)j | (code << col_bits)) : (uint32_t)j;
+  bool const valid = i < I.D;
+  uint64_t const r = valid ? I.reps[i] : 0;
+  auto emit = [&](uint32_t e, uint32_t row, uint64_t st, uint32_t vid) {
+    auto const c = canonicalize<W>((W)st, P);
+    int64_t const j = find_index((uint64_t)c.rep, I);
+    uint32_t ent = kNull, code = 0;
+    if (j >= 0) {
+      code = element_code(vid, c.phase, weights[j], C);
+      ent = packed ? ((uint32_t)j | (code << col_bits)) : (uint32_t)j;
+    }
+    entries[base + (uint64_t)e * 32 + row] = ent;
+    if (!packed) codes[base + (uint64_t)e * 32 + row] = (uint16_t)code;
+  };
+  uint32_t count = 0;
+  if (width <= kRecMaxElems && T.n_tuples < 65536) {
+    if (valid) {
+      for (uint32_t u = 0; u < T.n_tuples; ++u) {
+        uint32_t const tk = T.tuple_term[u];
+        uint32_t const t = tk & 0xFFFFu, k = tk >> 16;
+        uint32_t const a = local_index(r, T.tuple_sites[u], k);
+        uint32_t const n = T.n_off[t * 16 + a];
+        for (uint32_t q = 0; q < n; ++q)
+          desc[warp][lane][count++] = (q << 28) | (u << 8) | T.off_col[(t * 16 + a) * 16 + q];
       }
-      entries[base + (uint64_t)e * 32 + lane] = ent;
-      if (!packed) codes[base + (uint64_t)e * 32 + lane] = (uint16_t)code;
-      used = e + 1;
+    }
+    __syncwarp();
+    // exclusive prefix of counts over the lanes
+    uint32_t incl = count;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t const v = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += v;
+    }
+    uint32_t const total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t const excl = incl - count;
+    for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+      uint32_t const f = f0 + lane;
+      // owning row: the largest lane whose exclusive prefix is <= f
+      uint32_t row = 0;
+      for (uint32_t step = 16; step > 0; step >>= 1) {
+        uint32_t const probe = row + step;
+        uint32_t const ex = __shfl_sync(0xffffffffu, excl, probe & 31u);
+        if (probe < 32u && ex <= f) row = probe;
+      }
+      uint32_t const ex_row = __shfl_sync(0xffffffffu, excl, row);
+      uint64_t const r_row = __shfl_sync(0xffffffffu, r, row);
+      if (f < total) {
+        uint32_t const e = f - ex_row;
+        uint32_t const d = desc[warp][row][e];
+        uint32_t const u = (d >> 8) & 0xFFFFu, a2 = d & 0xFFu, q = d >> 28;
+        uint32_t const tk = T.tuple_term[u];
+        uint32_t const t = tk & 0xFFFFu, k = tk >> 16;
+        uint32_t const sites = T.tuple_sites[u];
+        uint32_t const a = local_index(r_row, sites, k);
+        emit(e, row, replace_local(r_row, sites, k, a2), T.off_vid[(t * 16 + a) * 16 + q]);
+      }
+    }
+  } else if (valid) {
+    walk_row(r, T, [&](uint32_t e, uint64_t st, uint32_t vid) {
+      emit(e, lane, st, vid);
+      count = e + 1;
     });
+  }
+  if (valid) {
     if (Real) {
       static_cast<double*>(diag)[i] = row_diag<double>(r, T);
     } else {
@@ -79,7 +137,7 @@ __global__ void k_record(PlanView P, IndexView I, TermsView T, CodeView C,
     }
     row_class[i] = (uint8_t)divisor_class(weights[i], C);
   }
-  for (uint32_t e = used; e < width; ++e) {
+  for (uint32_t e = count; e < width; ++e) {
     entries[base + (uint64_t)e * 32 + lane] = kNull;
     if (!packed) codes[base + (uint64_t)e * 32 + lane] = 0;
   }
@@ -440,12 +498,12 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
   if (int st = elements.allocate((n_slices + 1) * 8)) return st;
   unsigned const grid = (unsigned)((n_slices * 32 + kBlock - 1) / kBlock);
   if (n_slices) {
-    k_count<<<grid, kBlock, 0, stream>>>(b.reps.as<uint64_t>(), D, op.terms_dev, n_slices,
-                                         sf.slice_ptr.as<uint64_t>(), elements.as<uint64_t>());
+    { k_count<<<grid, kBlock, 0, stream>>>(b.reps.as<uint64_t>(), D, op.terms_dev, n_slices,
+                                         sf.slice_ptr.as<uint64_t>(), elements.as<uint64_t>()); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
   }
-  k_scan_u64<<<1, 1024, 0, stream>>>(sf.slice_ptr.as<uint64_t>(), n_slices);
-  k_scan_u64<<<1, 1024, 0, stream>>>(elements.as<uint64_t>(), n_slices);
+  { k_scan_u64<<<1, 1024, 0, stream>>>(sf.slice_ptr.as<uint64_t>(), n_slices); note_launches(1); }
+  { k_scan_u64<<<1, 1024, 0, stream>>>(elements.as<uint64_t>(), n_slices); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   uint64_t n_entries = 0, n_elements = 0;
   SED_TRY_CUDA(cudaMemcpyAsync(&n_entries, sf.slice_ptr.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
@@ -468,10 +526,10 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     auto launch = [&](auto w_tag, auto real_tag) {
       using W = decltype(w_tag);
       constexpr bool R = decltype(real_tag)::value;
-      k_record<W, R><<<grid, kBlock, 0, stream>>>(
+      { k_record<W, R><<<(unsigned)((n_slices + kRecWarps - 1) / kRecWarps), kRecWarps * 32, 0, stream>>>(
           b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices,
           sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(),
-          sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>());
+          sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>()); note_launches(1); }
     };
     if (wide) {
       if (op.is_real) launch(uint64_t{}, std::true_type{});
@@ -516,12 +574,12 @@ int launch_apply(OperatorData& op, X const* x, X* y, cudaStream_t stream, bool u
     unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
     size_t const smem = std::min<size_t>(32768, (size_t)tb.n_codes * (real_tab ? 8 : 16));
     if (real_tab) {
-      if (sf.packed) k_spmv<X, true, true><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
-      else k_spmv<X, true, false><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
+      if (sf.packed) { k_spmv<X, true, true><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind); note_launches(1); }
+      else { k_spmv<X, true, false><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind); note_launches(1); }
     } else {
       if constexpr (complex_storage) {
-        if (sf.packed) k_spmv<X, false, true><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
-        else k_spmv<X, false, false><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind);
+        if (sf.packed) { k_spmv<X, false, true><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind); note_launches(1); }
+        else { k_spmv<X, false, false><<<grid, kBlock, smem, stream>>>(S, D, x, y, ind); note_launches(1); }
       } else {
         return fail(LS_OPERATOR_IS_COMPLEX, "complex operator applied to real vectors");
       }
@@ -533,23 +591,23 @@ int launch_apply(OperatorData& op, X const* x, X* y, cudaStream_t stream, bool u
     bool const wide = b.plan.n_bits > 32;
     if (real_tab) {
       if (wide)
-        k_otf<uint64_t, X, true><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+        { k_otf<uint64_t, X, true><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
                                                               b.weights.as<uint32_t>(), table,
-                                                              tb.inv_sqrt_s.as<double>(), x, y, ind);
+                                                              tb.inv_sqrt_s.as<double>(), x, y, ind); note_launches(1); }
       else
-        k_otf<uint32_t, X, true><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+        { k_otf<uint32_t, X, true><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
                                                               b.weights.as<uint32_t>(), table,
-                                                              tb.inv_sqrt_s.as<double>(), x, y, ind);
+                                                              tb.inv_sqrt_s.as<double>(), x, y, ind); note_launches(1); }
     } else {
       if constexpr (complex_storage) {
         if (wide)
-          k_otf<uint64_t, X, false><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+          { k_otf<uint64_t, X, false><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
                                                                  b.weights.as<uint32_t>(), table,
-                                                                 tb.inv_sqrt_s.as<double>(), x, y, ind);
+                                                                 tb.inv_sqrt_s.as<double>(), x, y, ind); note_launches(1); }
         else
-          k_otf<uint32_t, X, false><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
+          { k_otf<uint32_t, X, false><<<grid, kBlock, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code,
                                                                  b.weights.as<uint32_t>(), table,
-                                                                 tb.inv_sqrt_s.as<double>(), x, y, ind);
+                                                                 tb.inv_sqrt_s.as<double>(), x, y, ind); note_launches(1); }
       } else {
         return fail(LS_OPERATOR_IS_COMPLEX, "complex operator applied to real vectors");
       }
@@ -784,10 +842,10 @@ int ls_operator_expectation(ls_operator const* op, int dtype, uint64_t size, uin
       char const* yc = yb.as<char>() + c * size * es;
       double2* pc = part.as<double2>() + c * grid;
       switch (dtype) {
-        case 0: k_dot_conj<float><<<grid, kBlock, 0, s>>>((float const*)xc, (float const*)yc, size, pc); break;
-        case 1: k_dot_conj<double><<<grid, kBlock, 0, s>>>((double const*)xc, (double const*)yc, size, pc); break;
-        case 2: k_dot_conj<float2><<<grid, kBlock, 0, s>>>((float2 const*)xc, (float2 const*)yc, size, pc); break;
-        default: k_dot_conj<double2><<<grid, kBlock, 0, s>>>((double2 const*)xc, (double2 const*)yc, size, pc); break;
+        case 0: { k_dot_conj<float><<<grid, kBlock, 0, s>>>((float const*)xc, (float const*)yc, size, pc); note_launches(1); } break;
+        case 1: { k_dot_conj<double><<<grid, kBlock, 0, s>>>((double const*)xc, (double const*)yc, size, pc); note_launches(1); } break;
+        case 2: { k_dot_conj<float2><<<grid, kBlock, 0, s>>>((float2 const*)xc, (float2 const*)yc, size, pc); note_launches(1); } break;
+        default: { k_dot_conj<double2><<<grid, kBlock, 0, s>>>((double2 const*)xc, (double2 const*)yc, size, pc); note_launches(1); } break;
       }
     }
     SED_TRY_CUDA(cudaGetLastError());

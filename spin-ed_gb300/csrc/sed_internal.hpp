@@ -102,6 +102,12 @@ struct SymPlanHost {
   std::vector<uint32_t> h_rot;       // [n_h][n_terms] left-rotate amounts
   std::vector<uint32_t> coset_phase; // [n_cosets]
   std::vector<uint32_t> h_phase;     // [n_h]
+  // H = <g1> x <g2> as nested cyclic loops (cyc = 0: explicit list above)
+  unsigned cyc = 0;
+  unsigned cyc_ord[2] = {1, 1};
+  unsigned cyc_phase[2] = {0, 0};
+  unsigned cyc_rot[2][2] = {{0, 0}, {0, 0}};
+  uint64_t cyc_mask[2][2] = {{0, 0}, {0, 0}};
   PlanView view() const;
 };
 
@@ -189,6 +195,12 @@ int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void cons
                           uint64_t ldx, void* y, uint64_t ldy, cudaStream_t stream, int form);
 
 bool characters_real(BasisData const& b);
+
+// Kernel-launch accounting (sed_kernel_launches): every launch site calls
+// note_launches(1); launches made while capturing a graph are not counted,
+// the graph's kernel nodes are counted at each replay instead.
+void note_launches(uint64_t n);
+void set_capturing(bool on);
 int current_device(int* device);
 
 }  // namespace sed

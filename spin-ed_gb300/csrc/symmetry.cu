@@ -255,6 +255,70 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
     }
   }
 
+  // H as a product of at most two cyclic groups of two-term generators.
+  if (H.size() > 1) {
+    auto order_of = [&](unsigned g) { return (unsigned)closure_of({g}).size(); };
+    auto two_terms = [&](unsigned g, std::vector<uint64_t>& m, std::vector<uint32_t>& r) {
+      return shift_terms(elems[g], width, 2, m, r);
+    };
+    std::vector<unsigned> cand;
+    for (unsigned g : cheap)
+      if (std::find(H.begin(), H.end(), g) != H.end()) cand.push_back(g);
+    unsigned g1 = 0, g2 = 0;
+    bool found = false;
+    for (unsigned a : cand)
+      if (!found && order_of(a) == H.size()) {
+        g1 = a;
+        g2 = 0;
+        found = true;
+      }
+    for (size_t i = 0; i < cand.size() && !found; ++i)
+      for (size_t j = i + 1; j < cand.size() && !found; ++j) {
+        unsigned const a = cand[i], b = cand[j];
+        if (compose(elems[a], elems[b]) != compose(elems[b], elems[a])) continue;
+        if ((size_t)order_of(a) * order_of(b) == H.size() && closure_of({a, b}).size() == H.size()) {
+          g1 = a;
+          g2 = b;
+          found = true;
+        }
+      }
+    if (found) {
+      unsigned const gens[2] = {g1, g2};
+      for (int q = 0; q < 2; ++q) {
+        std::vector<uint64_t> m;
+        std::vector<uint32_t> r;
+        two_terms(gens[q], m, r);
+        out.cyc_ord[q] = gens[q] ? order_of(gens[q]) : 1u;
+        out.cyc_phase[q] = phase[gens[q]];
+        for (size_t t = 0; t < 2; ++t) {
+          out.cyc_mask[q][t] = t < m.size() ? m[t] : 0;
+          out.cyc_rot[q][t] = t < r.size() ? r[t] : 0;
+        }
+        if (!gens[q]) {  // identity: keep every bit in place
+          out.cyc_mask[q][0] = out.mask;
+          out.cyc_mask[q][1] = 0;
+          out.cyc_rot[q][0] = out.cyc_rot[q][1] = 0;
+        }
+      }
+      // Check: g1^a g2^b runs over H exactly once with the closure's phases.
+      std::vector<bool> seen(G, false);
+      std::vector<uint8_t> pa = elems[0];
+      bool ok = true;
+      for (unsigned a = 0; a < out.cyc_ord[0] && ok; ++a) {
+        std::vector<uint8_t> pb = pa;
+        for (unsigned b = 0; b < out.cyc_ord[1] && ok; ++b) {
+          unsigned const k = index.at(key_of(pb.data(), n_bits));
+          uint64_t const want = ((uint64_t)a * out.cyc_phase[0] + (uint64_t)b * out.cyc_phase[1]) % out.L;
+          if (seen[k] || phase[k] != want || std::find(H.begin(), H.end(), k) == H.end()) ok = false;
+          seen[k] = true;
+          pb = compose(pb, elems[g2]);
+        }
+        pa = compose(pa, elems[g1]);
+      }
+      out.cyc = ok ? (g2 ? 2u : 1u) : 0u;
+    }
+  }
+
   // H as shift decompositions.
   out.n_h = (unsigned)H.size();
   out.n_terms = 1;
@@ -321,9 +385,33 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
                                               v.n_terms);
       if (want != got) return fail(LS_SYSTEM_ERROR, "shift decomposition failed");
     }
+  if (out.cyc) {
+    PlanView vx = out.view();
+    PlanView ve = vx;
+    ve.cyc = 0;
+    uint64_t rng = 0x9E3779B97F4A7C15ull;
+    for (int t = 0; t < 256; ++t) {
+      rng ^= rng << 13;
+      rng ^= rng >> 7;
+      rng ^= rng << 17;
+      uint64_t const x = rng & out.mask;
+      bool same;
+      if (width == 32) {
+        auto c1 = canonicalize<uint32_t>((uint32_t)x, vx), c2 = canonicalize<uint32_t>((uint32_t)x, ve);
+        same = c1.rep == c2.rep && representative_weight<uint32_t>((uint32_t)x, vx) ==
+                                       representative_weight<uint32_t>((uint32_t)x, ve);
+      } else {
+        auto c1 = canonicalize<uint64_t>(x, vx), c2 = canonicalize<uint64_t>(x, ve);
+        same = c1.rep == c2.rep &&
+               representative_weight<uint64_t>(x, vx) == representative_weight<uint64_t>(x, ve);
+      }
+      if (!same) return fail(LS_SYSTEM_ERROR, "cyclic subgroup walk disagrees with the explicit list");
+    }
+  }
   if (logging_enabled())
-    log_line("symmetry plan: |G| = %u (x%u inversion), |H| = %u, cosets = %u, stages = %u, terms = %u",
-             G, spin_inversion ? 2u : 1u, out.n_h, out.n_cosets, out.n_stages, out.n_terms);
+    log_line("symmetry plan: |G| = %u (x%u inversion), |H| = %u (cyclic product: %u), cosets = %u, "
+             "stages = %u, terms = %u",
+             G, spin_inversion ? 2u : 1u, out.n_h, out.cyc, out.n_cosets, out.n_stages, out.n_terms);
   return LS_SUCCESS;
 }
 
@@ -344,6 +432,15 @@ PlanView SymPlanHost::view() const {
   v.h_rot = h_rot.data();
   v.coset_phase = coset_phase.data();
   v.h_phase = h_phase.data();
+  v.cyc = cyc;
+  for (int q = 0; q < 2; ++q) {
+    v.cyc_ord[q] = cyc_ord[q];
+    v.cyc_phase[q] = cyc_phase[q];
+    for (int t = 0; t < 2; ++t) {
+      v.cyc_rot[q][t] = cyc_rot[q][t];
+      v.cyc_mask[q][t] = cyc_mask[q][t];
+    }
+  }
   return v;
 }
 

@@ -118,6 +118,7 @@ SIGNATURES = [
     ("sed_basis_device_states", _P, [_P]),
     ("sed_basis_index", _I, [_P, _U64, C.POINTER(_U64)]),
     ("sed_basis_state_info", _I, [_P, _U64, C.POINTER(_U64), C.POINTER(_U), C.POINTER(_U)]),
+    ("sed_kernel_launches", _U64, []),
     ("sed_version", C.c_char_p, []),
 ]
 
