@@ -245,6 +245,25 @@ SED_API int sed_operator_matmat_device(ls_operator const* op, int dtype, uint64_
                                uint64_t block_size, void const* x, uint64_t x_stride, void* y,
                                uint64_t y_stride, void* stream);
 
+/* No counterpart in the reference: ls_operator_expectation for callers that
+ * cannot let the library allocate device memory (a process whose device
+ * memory belongs to its own pool allocator, or a latency-critical loop that
+ * cannot afford cudaMalloc's implicit synchronisation). Computes Y = H X
+ * into the caller's device buffer y (column stride y_stride) and
+ * out[c] = <x_c|y_c> as complex128 (out: host or device memory). x and y
+ * must be device memory; at most 64 columns per call. It performs no device
+ * allocation: the operator must already be prepared (sed_operator_prepare,
+ * or an earlier ls_operator_matmat); the streamed form is used if recorded,
+ * else the on-the-fly form, and neither is recorded here. Partial sums live
+ * in a 66 KiB scratch array in the library's static device memory (held on
+ * every GPU that loads the library until exit) and shared by all calls: calls
+ * that overlap on the GPU race on it. The first call on each device looks up
+ * the scratch address (cudaGetSymbolAddress), so make that first call before
+ * any stream capture. */
+SED_API int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, uint64_t size,
+                                             uint64_t block_size, void const* x, uint64_t x_stride,
+                                             void* y, uint64_t y_stride, void* out);
+
 /* Norms ||P r|| = sqrt(S / |G|) of the representatives (host array). */
 SED_API int sed_basis_get_norms(ls_spin_basis const* basis, double* out);
 /* Device pointer to the representatives (valid while the basis lives). */

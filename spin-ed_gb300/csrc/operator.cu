@@ -888,3 +888,146 @@ uint64_t sed_operator_stream_elements(ls_operator const* op) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// sed_operator_expectation_noalloc: ls_operator_expectation without any device
+// allocation.
+//
+// Some callers cannot let a library call cudaMalloc: a process whose device
+// memory is already handed out to its own pool allocator (the allocation would
+// fail or fragment the pool), or a latency-critical loop for which cudaMalloc's
+// and cudaFree's implicit device synchronisation is unacceptable. For them this
+// entry point computes Y = H X into the caller's device buffer and
+// out[c] = <x_c|y_c> with the per-block partial sums kept in the file-scope
+// array below, so the call itself allocates nothing (the operator must already
+// be prepared, see sed.h).
+namespace sed {
+namespace {
+
+constexpr unsigned kNoAllocCols = 64;        // columns per call
+constexpr unsigned kNoAllocPartials = 4096;  // partial sums shared by all columns
+// Scratch shared by every call in this process: partial sums, then the
+// per-column results. 4096 x 16 B + 64 x 16 B = 66 KiB on every GPU that
+// loads the library, held until exit.
+static __device__ __align__(256) double2 g_noalloc_scratch[kNoAllocPartials + kNoAllocCols];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {nullptr};  // device address of the scratch, per device
+
+// Set-up, once per device and with that device current: the host-side name of
+// g_noalloc_scratch is not a device address, so look the address up.
+int noalloc_scratch(int device, double2** out) {
+  if (device < 0 || device >= 64) return fail(LS_CUDA_ERROR, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(LS_CUDA_ERROR, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+    g_noalloc_addr[device] = p;
+  }
+  *out = static_cast<double2*>(g_noalloc_addr[device]);
+  return LS_SUCCESS;
+}
+
+// Per-block partial sums of conj(x_i) y_i into partial[blockIdx.x].
+template <class X>
+__global__ void k_dot_conj_noalloc(X const* __restrict__ x, X const* __restrict__ y, uint64_t n,
+                                   double2* __restrict__ partial) {
+  using V = typename Store<X>::V;
+  __shared__ double red_re[kBlock / 32], red_im[kBlock / 32];
+  double re = 0.0, im = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    V const a = Store<X>::load(x, i), b = Store<X>::load(y, i);
+    if constexpr (std::is_same<V, double>::value) {
+      re = fma(a, b, re);
+    } else {
+      re = fma(a.re, b.re, fma(a.im, b.im, re));
+      im = fma(a.re, b.im, fma(-a.im, b.re, im));
+    }
+  }
+  double const sre = block_sum(re, red_re);
+  double const sim = block_sum(im, red_im);
+  if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(sre, sim);
+}
+
+// results[c] = sum of the `per_col` partials of column c.
+__global__ void k_sum_partials_noalloc(double2 const* __restrict__ partial, unsigned per_col,
+                                       unsigned cols, double2* __restrict__ results) {
+  __shared__ double red_re[kBlock / 32], red_im[kBlock / 32];
+  for (unsigned c = 0; c < cols; ++c) {
+    double re = 0.0, im = 0.0;
+    for (unsigned i = threadIdx.x; i < per_col; i += blockDim.x) {
+      re += partial[(uint64_t)c * per_col + i].x;
+      im += partial[(uint64_t)c * per_col + i].y;
+    }
+    double const sre = block_sum(re, red_re);
+    double const sim = block_sum(im, red_im);
+    if (threadIdx.x == 0) results[c] = make_double2(sre, sim);
+  }
+}
+
+}  // namespace
+}  // namespace sed
+
+extern "C" int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, uint64_t size,
+                                                uint64_t block_size, void const* x, uint64_t x_stride,
+                                                void* y, uint64_t y_stride, void* out) {
+  using namespace sed;
+  if (!op || !out || (block_size && (!x || !y)))
+    return fail(LS_INVALID_ARGUMENT, "sed_operator_expectation_noalloc: NULL argument");
+  OperatorData& d = *op->d;
+  std::lock_guard<std::mutex> lock(d.mu);
+  if (int st = check_block(d, dtype, size, block_size, x_stride)) return st;
+  if (block_size && y_stride < size) return fail(LS_INVALID_ARGUMENT, "column stride is smaller than the size");
+  if (block_size > kNoAllocCols)
+    return fail(LS_INVALID_ARGUMENT, "sed_operator_expectation_noalloc: at most " + std::to_string(kNoAllocCols) +
+                                         " columns per call (got " + std::to_string(block_size) + ")");
+  if (!d.is_real && dtype < 2) return fail(LS_OPERATOR_IS_COMPLEX, "operator is complex; use dtype 2 or 3");
+  if (!d.tables || !d.term_buf.ptr || !d.cuda_stream || !d.basis->plan_buf.ptr)
+    return fail(LS_CACHE_NOT_BUILT,
+                "sed_operator_expectation_noalloc: prepare the operator first (sed_operator_prepare)");
+  if (block_size == 0) return LS_SUCCESS;
+  if (!is_device_pointer(x) || !is_device_pointer(y))
+    return fail(LS_INVALID_ARGUMENT, "sed_operator_expectation_noalloc: x and y must be device memory");
+  ScopedDevice dev(d.basis->device);
+  double2* scratch = nullptr;
+  if (int st = noalloc_scratch(d.basis->device, &scratch)) return st;
+  cudaStream_t s = d.cuda_stream;
+  bool const use_stream = d.stream.ready && d.form != SED_FORM_ON_THE_FLY;
+  size_t const es = (size_t)elem_size(dtype);
+  unsigned const per_col = std::max(1u, std::min(grid_size(size, d.basis->device, 4),
+                                                 kNoAllocPartials / (unsigned)block_size));
+  for (uint64_t c = 0; c < block_size; ++c) {
+    char const* xc = static_cast<char const*>(x) + c * x_stride * es;
+    char* yc = static_cast<char*>(y) + c * y_stride * es;
+    double2* pc = scratch + c * per_col;
+    int st;
+    switch (dtype) {
+      case 0:
+        st = launch_apply<float>(d, (float const*)xc, (float*)yc, s, use_stream, Indirect{});
+        if (!st) { k_dot_conj_noalloc<float><<<per_col, kBlock, 0, s>>>((float const*)xc, (float const*)yc, size, pc); note_launches(1); }
+        break;
+      case 1:
+        st = launch_apply<double>(d, (double const*)xc, (double*)yc, s, use_stream, Indirect{});
+        if (!st) { k_dot_conj_noalloc<double><<<per_col, kBlock, 0, s>>>((double const*)xc, (double const*)yc, size, pc); note_launches(1); }
+        break;
+      case 2:
+        st = launch_apply<float2>(d, (float2 const*)xc, (float2*)yc, s, use_stream, Indirect{});
+        if (!st) { k_dot_conj_noalloc<float2><<<per_col, kBlock, 0, s>>>((float2 const*)xc, (float2 const*)yc, size, pc); note_launches(1); }
+        break;
+      default:
+        st = launch_apply<double2>(d, (double2 const*)xc, (double2*)yc, s, use_stream, Indirect{});
+        if (!st) { k_dot_conj_noalloc<double2><<<per_col, kBlock, 0, s>>>((double2 const*)xc, (double2 const*)yc, size, pc); note_launches(1); }
+        break;
+    }
+    if (st) return st;
+  }
+  double2* results = scratch + kNoAllocPartials;
+  { k_sum_partials_noalloc<<<1, kBlock, 0, s>>>(scratch, per_col, (unsigned)block_size, results); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  SED_TRY_CUDA(cudaMemcpyAsync(out, results, block_size * sizeof(double2), cudaMemcpyDefault, s));
+  SED_TRY_CUDA(cudaStreamSynchronize(s));
+  return LS_SUCCESS;
+}
