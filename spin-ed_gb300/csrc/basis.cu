@@ -25,8 +25,10 @@ constexpr unsigned kThreads = 256;
 constexpr unsigned kTileWords = kThreads * 8;  // bitmap words per tile
 
 template <class W>
-__global__ void k_mark(PlanView P, uint64_t const* __restrict__ binom, unsigned n, int hw,
+__global__ void k_mark(__grid_constant__ const PlanView P, uint64_t const* __restrict__ binom, unsigned n, int hw,
                        uint64_t space, uint64_t n_words, uint32_t* __restrict__ bitmap) {
+  __shared__ uint16_t srow[2048];
+  RowTab const RT = stage_rows(P, srow);
   for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_words;
        t += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t const r0 = t * 32;
@@ -34,7 +36,7 @@ __global__ void k_mark(PlanView P, uint64_t const* __restrict__ binom, unsigned 
     uint64_t x = unrank_word(r0, n, hw, binom);
     uint32_t mask = 0;
     for (unsigned k = 0; k < count; ++k) {
-      if (representative_weight<W>((W)x, P)) mask |= 1u << k;
+      if (representative_weight<W>((W)x, P, RT)) mask |= 1u << k;
       if (k + 1 < count) x = hw >= 0 ? next_same_weight(x) : x + 1;
     }
     bitmap[t] = mask;
@@ -88,11 +90,9 @@ __global__ void k_scan_serial(uint64_t* __restrict__ v, uint64_t n) {
   }
 }
 
-template <class W>
-__global__ void k_write(PlanView P, uint64_t const* __restrict__ binom, unsigned n, int hw,
-                        uint64_t space, uint32_t const* __restrict__ bitmap, uint64_t n_words,
-                        uint64_t const* __restrict__ tile_offset, uint64_t* __restrict__ reps,
-                        uint32_t* __restrict__ weights) {
+__global__ void k_write(uint64_t const* __restrict__ binom, unsigned n, int hw, uint64_t space,
+                        uint32_t const* __restrict__ bitmap, uint64_t n_words,
+                        uint64_t const* __restrict__ tile_offset, uint64_t* __restrict__ reps) {
   __shared__ uint32_t scan[kThreads];
   uint64_t const w0 = (uint64_t)blockIdx.x * kTileWords + (uint64_t)threadIdx.x * 8;
   uint32_t m[8];
@@ -116,26 +116,35 @@ __global__ void k_write(PlanView P, uint64_t const* __restrict__ binom, unsigned
     unsigned const count = (unsigned)min((uint64_t)32, space - r0);
     uint64_t x = unrank_word(r0, n, hw, binom);
     for (unsigned k = 0; k < count; ++k) {
-      if (m[j] >> k & 1u) {
-        reps[pos] = x;
-        weights[pos] = representative_weight<W>((W)x, P);
-        ++pos;
-      }
+      if (m[j] >> k & 1u) reps[pos++] = x;
       if (k + 1 < count) x = hw >= 0 ? next_same_weight(x) : x + 1;
     }
   }
 }
 
+// Stabiliser orders of the written representatives, one thread per entry.
 template <class W>
-__global__ void k_check_reps(PlanView P, uint64_t const* __restrict__ reps, uint64_t D,
+__global__ void k_weights(__grid_constant__ const PlanView P, uint64_t const* __restrict__ reps, uint64_t D,
+                          uint32_t* __restrict__ weights) {
+  __shared__ uint16_t srow[2048];
+  RowTab const RT = stage_rows(P, srow);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    weights[i] = representative_weight<W>((W)reps[i], P, RT);
+}
+
+template <class W>
+__global__ void k_check_reps(__grid_constant__ const PlanView P, uint64_t const* __restrict__ reps, uint64_t D,
                              uint32_t* __restrict__ weights, unsigned n, int hw,
                              uint32_t* __restrict__ bad) {
+  __shared__ uint16_t srow[2048];
+  RowTab const RT = stage_rows(P, srow);
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
        i += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t const x = reps[i];
     uint32_t w = 0;
     bool ok = (n == 64 || (x >> n) == 0) && (hw < 0 || __popcll(x) == hw);
-    if (ok) w = representative_weight<W>((W)x, P);
+    if (ok) w = representative_weight<W>((W)x, P, RT);
     if (i + 1 < D && reps[i + 1] <= x) ok = false;
     weights[i] = w;
     if (!ok || w == 0) bad[0] = 1u;  // any writer stores the same value
@@ -176,33 +185,49 @@ unsigned grid_for(uint64_t work, int device) {
 int basis_upload_plan(BasisData& b, cudaStream_t stream) {
   if (b.plan_buf.ptr) return LS_SUCCESS;
   SymPlanHost const& p = b.plan;
-  size_t const sz_bm = p.benes_mask.size() * 8, sz_bs = p.benes_shift.size() * 4;
-  size_t const sz_hm = p.h_mask.size() * 8, sz_hr = p.h_rot.size() * 4;
-  size_t const sz_cp = p.coset_phase.size() * 4, sz_hp = p.h_phase.size() * 4;
   auto align = [](size_t v) { return (v + 15) & ~(size_t)15; };
-  size_t const total = align(sz_bm) + align(sz_bs) + align(sz_hm) + align(sz_hr) + align(sz_cp) +
-                       align(sz_hp) + 16;
-  std::vector<uint8_t> host(total, 0);
-  size_t off = 0;
-  PlanView v = p.view();
-  auto put = [&](void const* src, size_t n) {
-    std::memcpy(host.data() + off, src, n);
-    size_t const at = off;
-    off += align(n);
-    return at;
+  struct Part {
+    void const* src;
+    size_t bytes;
+    size_t off;
   };
-  size_t const o_bm = put(p.benes_mask.data(), sz_bm), o_bs = put(p.benes_shift.data(), sz_bs);
-  size_t const o_hm = put(p.h_mask.data(), sz_hm), o_hr = put(p.h_rot.data(), sz_hr);
-  size_t const o_cp = put(p.coset_phase.data(), sz_cp), o_hp = put(p.h_phase.data(), sz_hp);
+  std::vector<Part> parts = {
+      {p.benes_mask.data(), p.benes_mask.size() * 8, 0}, {p.benes_shift.data(), p.benes_shift.size() * 4, 0},
+      {p.h_mask.data(), p.h_mask.size() * 8, 0},         {p.h_rot.data(), p.h_rot.size() * 4, 0},
+      {p.coset_phase.data(), p.coset_phase.size() * 4, 0}, {p.h_phase.data(), p.h_phase.size() * 4, 0},
+      {p.row_min.data(), p.row_min.size() * 2, 0},       {p.row_set.data(), p.row_set.size() * 2, 0},
+      {p.rot_mask.data(), p.rot_mask.size() * 8, 0},     {p.rot_rot.data(), p.rot_rot.size() * 4, 0},
+      {p.rot_exp.data(), p.rot_exp.size() * 4, 0},       {p.sh_mask.data(), p.sh_mask.size() * 8, 0},
+      {p.sh_rot.data(), p.sh_rot.size() * 4, 0},         {p.sh_exp.data(), p.sh_exp.size() * 4, 0},
+      {p.pos.data(), p.pos.size(), 0},
+  };
+  size_t total = 16;
+  for (auto& q : parts) {
+    q.off = total;
+    total += align(q.bytes);
+  }
+  std::vector<uint8_t> host(total, 0);
+  for (auto const& q : parts)
+    if (q.bytes) std::memcpy(host.data() + q.off, q.src, q.bytes);
   if (int st = b.plan_buf.allocate(total)) return st;
   SED_TRY_CUDA(cudaMemcpyAsync(b.plan_buf.ptr, host.data(), total, cudaMemcpyHostToDevice, stream));
   uint8_t* base = b.plan_buf.as<uint8_t>();
-  v.benes_mask = (uint64_t const*)(base + o_bm);
-  v.benes_shift = (uint32_t const*)(base + o_bs);
-  v.h_mask = (uint64_t const*)(base + o_hm);
-  v.h_rot = (uint32_t const*)(base + o_hr);
-  v.coset_phase = (uint32_t const*)(base + o_cp);
-  v.h_phase = (uint32_t const*)(base + o_hp);
+  PlanView v = p.view();
+  v.benes_mask = (uint64_t const*)(base + parts[0].off);
+  v.benes_shift = (uint32_t const*)(base + parts[1].off);
+  v.h_mask = (uint64_t const*)(base + parts[2].off);
+  v.h_rot = (uint32_t const*)(base + parts[3].off);
+  v.coset_phase = (uint32_t const*)(base + parts[4].off);
+  v.h_phase = (uint32_t const*)(base + parts[5].off);
+  v.row_min = (uint16_t const*)(base + parts[6].off);
+  v.row_set = (uint16_t const*)(base + parts[7].off);
+  v.rot_mask = (uint64_t const*)(base + parts[8].off);
+  v.rot_rot = (uint32_t const*)(base + parts[9].off);
+  v.rot_exp = (uint32_t const*)(base + parts[10].off);
+  v.sh_mask = (uint64_t const*)(base + parts[11].off);
+  v.sh_rot = (uint32_t const*)(base + parts[12].off);
+  v.sh_exp = (uint32_t const*)(base + parts[13].off);
+  v.pos = (uint8_t const*)(base + parts[14].off);
   b.plan_dev = v;
   std::vector<uint64_t> binom(65 * 65, 0);
   for (unsigned i = 0; i <= 64; ++i) {
@@ -329,14 +354,17 @@ int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
     if (int st = b.reps.allocate(std::max<uint64_t>(1, D) * 8)) return st;
     if (int st = b.weights.allocate(std::max<uint64_t>(1, D) * 4)) return st;
     if (n_tiles) {
+      { k_write<<<(unsigned)n_tiles, kThreads, 0, stream>>>(b.binom.as<uint64_t>(), b.n, b.hw, space,
+                                                          bitmap.as<uint32_t>(), n_words, tiles.as<uint64_t>(),
+                                                          b.reps.as<uint64_t>()); note_launches(1); }
+      SED_TRY_CUDA(cudaGetLastError());
+    }
+    if (D) {
+      unsigned const grid = grid_for(D, b.device);
       if (wide)
-        { k_write<uint64_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
-            P, b.binom.as<uint64_t>(), b.n, b.hw, space, bitmap.as<uint32_t>(), n_words,
-            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>()); note_launches(1); }
+        { k_weights<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), D, b.weights.as<uint32_t>()); note_launches(1); }
       else
-        { k_write<uint32_t><<<(unsigned)n_tiles, kThreads, 0, stream>>>(
-            P, b.binom.as<uint64_t>(), b.n, b.hw, space, bitmap.as<uint32_t>(), n_words,
-            tiles.as<uint64_t>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>()); note_launches(1); }
+        { k_weights<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.reps.as<uint64_t>(), D, b.weights.as<uint32_t>()); note_launches(1); }
       SED_TRY_CUDA(cudaGetLastError());
     }
     SED_TRY_CUDA(cudaStreamSynchronize(stream));

@@ -30,8 +30,19 @@ namespace sed {
 
 constexpr unsigned SED_MAX_TERMS = 4;    // displacements per element of H
 constexpr unsigned SED_MAX_STAGES = 11;  // Benes stages for 64 bits
+constexpr unsigned SED_PARAM_COSETS = 16;  // cosets whose networks travel in kernel parameters
+constexpr unsigned SED_MAX_ROWS = 8;       // rows handled in registers by the row path
 
 struct PlanView {
+  // Benes masks of every coset for the full, unpruned network of the word
+  // width (stage shifts 32,16,...,1,...,16,32 for 64 bits; 16,...,1,...,16 for
+  // 32), carried in kernel-parameter space when n_cosets <= SED_PARAM_COSETS
+  // (fixed_nets = 1) so that each stage is a handful of immediate-shift ops.
+  uint32_t fixed_nets;
+  uint64_t nets[SED_PARAM_COSETS][SED_MAX_STAGES];
+  // pos[c * 64 + i]: bit position where bit i of x lands under coset
+  // representative c (so P_c(x ^ d) = P_c(x) ^ P_c(d) is cheap for sparse d)
+  uint8_t const* pos;
   // When cyc > 0, H = <g1> x <g2> (cyc = number of generators) is walked by
   // nested loops that apply the generators' two-term shift decompositions
   // held right here (kernel-parameter space): no memory traffic per image.
@@ -52,6 +63,23 @@ struct PlanView {
   uint32_t const* h_rot;       // [n_h][n_terms]
   uint32_t const* coset_phase; // [n_cosets]
   uint32_t const* h_phase;     // [n_h]
+  // Row structure of H (rows != 0): the word is n_rows blocks ("rows") of
+  // row_bits bits, one generator rotates every row by the same amount, the
+  // other (if n_rows > 1) shifts rows cyclically. rows == 1: row_bits <= 10,
+  // smallest rotation of each row from a table; rows == 2: a single row
+  // (chains), smallest rotation from the longest circular run of zeros.
+  uint32_t rows;
+  uint32_t row_bits, n_rows;
+  uint32_t rot_phase, shift_phase;  // characters of the rotation / shift generators
+  uint64_t row_mask;
+  uint16_t const* row_min;     // [1 << row_bits] smallest rotation of a row
+  uint16_t const* row_set;     // [1 << row_bits] rotations r reaching it (bit r)
+  uint64_t const* rot_mask;    // [row_bits][2] two-term shift: rotate every row left by r
+  uint32_t const* rot_rot;     // [row_bits][2]
+  uint32_t const* rot_exp;     // [row_bits] exponent of the rotation generator
+  uint64_t const* sh_mask;     // [n_rows][2] shift: image row j <- source row (j + t) mod n_rows
+  uint32_t const* sh_rot;      // [n_rows][2]
+  uint32_t const* sh_exp;      // [n_rows] exponent of the shift generator
 };
 
 struct IndexView {
@@ -96,10 +124,46 @@ SED_HD W benes_apply(W x, uint64_t const* masks, uint32_t const* shifts, unsigne
 }
 
 template <class W>
+SED_HD W benes_fixed(W x, uint64_t const* m) {
+  constexpr unsigned B = sizeof(W) * 8;
+  constexpr unsigned L = B == 64 ? 6 : 5;
+#pragma unroll
+  for (unsigned i = 0; i < 2 * L - 1; ++i) {
+    unsigned const s = i < L ? (B >> (i + 1)) : (B >> (2 * L - 1 - i));
+    W const t = ((x >> s) ^ x) & (W)m[i];
+    x ^= t ^ (t << s);
+  }
+  return x;
+}
+
+// Image of x under coset representative c.
+template <class W>
+SED_HD W coset_apply(W x, PlanView const& P, uint32_t c) {
+  if (c == 0) return x;
+  if (P.fixed_nets) return benes_fixed<W>(x, P.nets[c]);
+  return benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift, P.n_stages);
+}
+
+template <class W>
 SED_HD W shift_apply(W y, uint64_t const* masks, uint32_t const* rots, unsigned n_terms) {
   W z = 0;
   for (unsigned t = 0; t < n_terms; ++t) z |= rotl<W>(y & (W)masks[t], rots[t]);
   return z;
+}
+
+SED_HD int __builtin_ctz_sed(uint32_t v) {
+#ifdef __CUDA_ARCH__
+  return __ffs((int)v) - 1;
+#else
+  return __builtin_ctz(v);
+#endif
+}
+SED_HD int __builtin_ctzll_sed(uint64_t v) {
+#ifdef __CUDA_ARCH__
+  return __ffsll((long long)v) - 1;
+#else
+  return __builtin_ctzll(v);
+#endif
 }
 
 SED_HD uint32_t add_phase(uint32_t a, uint32_t b, uint32_t L) {
@@ -118,18 +182,202 @@ SED_HD W apply2(W y, uint64_t m0, uint64_t m1, unsigned r0, unsigned r1) {
   return rotl<W>(y & (W)m0, r0) | rotl<W>(y & (W)m1, r1);
 }
 
-// Orbit minimum of x and the phase of an element mapping x onto it.
+// --- row-structured subgroup ------------------------------------------------
+struct RowTab {
+  uint16_t const* min;  // smallest rotation of a row
+  uint16_t const* set;  // rotations reaching it
+};
+// Both routines enumerate the H-images (of y, and of ~y with inversion) that
+// can be the smallest one: the smallest image has the smallest top row (most
+// significant row_bits bits), so only (row, rotation) pairs reaching that top
+// row can produce it. f(image, r, t, inverted) returns false to stop early.
+
 template <class W>
-SED_HD Canon<W> canonicalize(W x, PlanView const& P) {
+SED_HD W rotl_n(W v, unsigned r, unsigned n, W mask) {
+  return r ? (W)(((v << r) | (v >> (n - r))) & mask) : v;
+}
+
+template <class W>
+SED_HD W rotr_n(W v, unsigned r, unsigned n, W mask) {
+  return r ? (W)(((v >> r) | (v << (n - r))) & mask) : v;
+}
+
+// Rows of y (row k = bits [k B, (k+1) B)) and, per row and orientation, the
+// smallest rotation; returns the smallest top row over all H-images of y
+// (and ~y).
+template <class W>
+SED_HD uint32_t rows_scan(W y, PlanView const& P, RowTab const& T, uint32_t (&rv)[SED_MAX_ROWS]) {
+  uint32_t best = 0xFFFFFFFFu;
+  uint32_t const rm = (uint32_t)P.row_mask;
+  W v = y;
+#pragma unroll
+  for (uint32_t k = 0; k < SED_MAX_ROWS; ++k) {
+    if (k < P.n_rows) {
+      rv[k] = (uint32_t)v & rm;
+      v >>= P.row_bits;
+      uint32_t const a = T.min[rv[k]];
+      best = a < best ? a : best;
+      if (P.inv) {
+        uint32_t const b = T.min[rv[k] ^ rm];
+        best = b < best ? b : best;
+      }
+    }
+  }
+  return best;
+}
+
+template <class W, class F>
+SED_HD bool rows_top_each(W y, W mask, PlanView const& P, RowTab const& T, uint32_t top,
+                          uint32_t const (&rv)[SED_MAX_ROWS], F&& f) {
+  uint32_t const rm = (uint32_t)P.row_mask;
+#pragma unroll
+  for (uint32_t k = 0; k < SED_MAX_ROWS; ++k) {
+    if (k >= P.n_rows) break;
+    uint32_t const t = k + 1 == P.n_rows ? 0u : k + 1;  // the image's top row comes from row k
+    for (uint32_t inv = 0; inv <= (P.inv ? 1u : 0u); ++inv) {
+      uint32_t const v = inv ? (rv[k] ^ rm) : rv[k];
+      if (T.min[v] != top) continue;
+      W const yy = inv ? (W)(~y & mask) : y;
+      uint32_t set = T.set[v];
+      while (set) {
+        uint32_t const r = (uint32_t)__builtin_ctz_sed(set);
+        set &= set - 1;
+        W z = apply2<W>(yy, P.rot_mask[2 * r], P.rot_mask[2 * r + 1], P.rot_rot[2 * r], P.rot_rot[2 * r + 1]);
+        z = apply2<W>(z, P.sh_mask[2 * t], P.sh_mask[2 * t + 1], P.sh_rot[2 * t], P.sh_rot[2 * t + 1]);
+        if (!f(z, r, t, inv)) return false;
+      }
+    }
+  }
+  return true;
+}
+
+// Single row of n bits (chains): rotations of v that bring a longest circular
+// run of zeros to the top. Returns the run length and writes the run starts.
+template <class W>
+SED_HD uint32_t zero_runs(W v, unsigned n, W mask, W* starts) {
+  W const Z = (W)(~v & mask);
+  if (Z == 0) {  // no zeros: every rotation is the same word
+    *starts = mask;
+    return 0;
+  }
+  // pw[i]: starts of circular zero runs of length >= 2^i (fully unrolled, so
+  // every index is a compile-time constant and pw stays in registers)
+  W pw[7];
+  pw[0] = Z;
+  int top = 0;
+#pragma unroll
+  for (int i = 1; i < 7; ++i) {
+    unsigned const len = 1u << (i - 1);
+    pw[i] = 0;
+    if (2 * len <= n && top == i - 1) {
+      W const nxt = pw[i - 1] & rotr_n<W>(pw[i - 1], len, n, mask);
+      if (nxt) {
+        pw[i] = nxt;
+        top = i;
+      }
+    }
+  }
+  W cur = pw[0];
+#pragma unroll
+  for (int i = 1; i < 7; ++i)
+    if (top == i) cur = pw[i];
+  uint32_t len = 1u << top;
+#pragma unroll
+  for (int j = 5; j >= 0; --j) {
+    if (j < top) {
+      uint32_t const s = 1u << j;
+      if (len + s <= n) {
+        W const t = cur & rotr_n<W>(pw[j], len, n, mask);
+        if (t) {
+          cur = t;
+          len += s;
+        }
+      }
+    }
+  }
+  *starts = cur;
+  return len;
+}
+
+template <class W, class F>
+SED_HD bool chain_each(W y, W mask, PlanView const& P, F&& f) {
+  unsigned const n = P.row_bits;
+  W s0, s1 = 0;
+  uint32_t const k0 = zero_runs<W>(y, n, mask, &s0);
+  uint32_t k1 = 0;
+  if (P.inv) k1 = zero_runs<W>((W)(~y & mask), n, mask, &s1);
+  for (uint32_t inv = 0; inv <= (P.inv ? 1u : 0u); ++inv) {
+    uint32_t const k = inv ? k1 : k0;
+    if (k < (inv ? k0 : k1)) continue;  // a longer leading run of zeros always wins
+    W set = inv ? s1 : s0;
+    W const yy = inv ? (W)(~y & mask) : y;
+    while (set) {
+      uint32_t const p = (uint32_t)__builtin_ctzll_sed((uint64_t)set);
+      set &= set - 1;
+      uint32_t const r = (n - k - p + 2 * n) % n;
+      if (!f(rotl_n<W>(yy, r, n, mask), r, 0u, inv)) return false;
+    }
+  }
+  return true;
+}
+
+#ifdef __CUDACC__
+// Copies the row tables into shared memory (2048 uint16 slots) and returns
+// them. Every thread of the block must call it.
+__device__ __forceinline__ RowTab stage_rows(PlanView const& P, uint16_t* sm) {
+  if (P.rows == 1) {
+    unsigned const n = 1u << P.row_bits;
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+      sm[i] = P.row_min[i];
+      sm[1024 + i] = P.row_set[i];
+    }
+    __syncthreads();
+    return {sm, sm + 1024};
+  }
+  return {P.row_min, P.row_set};
+}
+#endif
+
+// Orbit minimum of x and the phase of an element mapping x onto it.
+// img(c) returns the image of x under coset representative c.
+template <class W, class Img>
+SED_HD Canon<W> canonicalize_img(W x, PlanView const& P, RowTab const& T, Img&& img) {
   W best = x;
   W const mask = (W)P.mask;
+  if (P.rows) {
+    uint32_t bc = 0, br = 0, bt = 0, binv = 0;
+    for (uint32_t c = 0; c < P.n_cosets; ++c) {
+      W const y = img(c);
+      auto take = [&](W z, uint32_t r, uint32_t t, uint32_t inv) {
+        if (z < best) {
+          best = z;
+          bc = c;
+          br = r;
+          bt = t;
+          binv = inv;
+        }
+        return true;
+      };
+      if (P.rows == 1) {
+        uint32_t rv[SED_MAX_ROWS];
+        uint32_t const top = rows_scan<W>(y, P, T, rv);
+        if (top > (uint32_t)(best >> ((P.n_rows - 1) * P.row_bits))) continue;
+        rows_top_each<W>(y, mask, P, T, top, rv, take);
+      } else {
+        chain_each<W>(y, mask, P, take);
+      }
+    }
+    uint64_t ph = (uint64_t)P.coset_phase[bc] + (uint64_t)P.rot_exp[br] * P.rot_phase +
+                  (uint64_t)P.sh_exp[bt] * P.shift_phase;
+    if (binv) ph += P.inv_phase;
+    return {best, (uint32_t)(ph % P.L)};
+  }
   if (P.cyc) {
     // candidate index: ((c * o1) + a) * o2 + b, bit 31 = inversion
     uint32_t const o1 = P.cyc_ord[0], o2 = P.cyc_ord[1];
     uint32_t bc = 0, cand = 0;
     for (uint32_t c = 0; c < P.n_cosets; ++c) {
-      W y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
-                           c == 0 ? 0u : P.n_stages);
+      W y = img(c);
       for (uint32_t a = 0; a < o1; ++a) {
         W z = y;
         for (uint32_t b = 0; b < o2; ++b, ++cand) {
@@ -158,8 +406,7 @@ SED_HD Canon<W> canonicalize(W x, PlanView const& P) {
   }
   uint32_t bc = 0, bh = 0, binv = 0;
   for (uint32_t c = 0; c < P.n_cosets; ++c) {
-    W const y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
-                               c == 0 ? 0u : P.n_stages);
+    W const y = img(c);
     for (uint32_t h = 0; h < P.n_h; ++h) {
       W const z = shift_apply<W>(y, P.h_mask + (uint64_t)h * P.n_terms,
                                  P.h_rot + (uint64_t)h * P.n_terms, P.n_terms);
@@ -187,14 +434,46 @@ SED_HD Canon<W> canonicalize(W x, PlanView const& P) {
 
 // Stabiliser order of x if x is a representative of the sector, else 0.
 template <class W>
-SED_HD uint32_t representative_weight(W x, PlanView const& P) {
+SED_HD uint32_t representative_weight(W x, PlanView const& P, RowTab const& T) {
   uint32_t S = 0;
   W const mask = (W)P.mask;
+  if (P.rows) {
+    bool reject = false;
+    for (uint32_t c = 0; c < P.n_cosets && !reject; ++c) {
+      W const y = coset_apply<W>(x, P, c);
+      auto visit = [&](W z, uint32_t r, uint32_t t, uint32_t inv) {
+        if (z < x) {
+          reject = true;
+          return false;
+        }
+        if (z == x) {
+          uint64_t ph = (uint64_t)P.coset_phase[c] + (uint64_t)P.rot_exp[r] * P.rot_phase +
+                        (uint64_t)P.sh_exp[t] * P.shift_phase + (inv ? P.inv_phase : 0u);
+          if (ph % P.L != 0) {
+            reject = true;
+            return false;
+          }
+          ++S;
+        }
+        return true;
+      };
+      if (P.rows == 1) {
+        uint32_t rv[SED_MAX_ROWS];
+        uint32_t const top = rows_scan<W>(y, P, T, rv);
+        uint32_t const xt = (uint32_t)(x >> ((P.n_rows - 1) * P.row_bits));
+        if (top < xt) return 0;
+        if (top > xt) continue;
+        rows_top_each<W>(y, mask, P, T, top, rv, visit);
+      } else {
+        chain_each<W>(y, mask, P, visit);
+      }
+    }
+    return reject ? 0 : S;
+  }
   if (P.cyc) {
     uint32_t const o1 = P.cyc_ord[0], o2 = P.cyc_ord[1];
     for (uint32_t c = 0; c < P.n_cosets; ++c) {
-      W y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
-                           c == 0 ? 0u : P.n_stages);
+      W y = coset_apply<W>(x, P, c);
       uint32_t pa = P.coset_phase[c];
       for (uint32_t a = 0; a < o1; ++a) {
         W z = y;
@@ -223,8 +502,7 @@ SED_HD uint32_t representative_weight(W x, PlanView const& P) {
     return S;
   }
   for (uint32_t c = 0; c < P.n_cosets; ++c) {
-    W const y = benes_apply<W>(x, P.benes_mask + (uint64_t)c * P.n_stages, P.benes_shift,
-                               c == 0 ? 0u : P.n_stages);
+    W const y = coset_apply<W>(x, P, c);
     for (uint32_t h = 0; h < P.n_h; ++h) {
       W const z = shift_apply<W>(y, P.h_mask + (uint64_t)h * P.n_terms,
                                  P.h_rot + (uint64_t)h * P.n_terms, P.n_terms);
@@ -245,6 +523,19 @@ SED_HD uint32_t representative_weight(W x, PlanView const& P) {
     }
   }
   return S;
+}
+
+template <class W>
+SED_HD Canon<W> canonicalize(W x, PlanView const& P, RowTab const& T) {
+  return canonicalize_img<W>(x, P, T, [&](uint32_t c) { return coset_apply<W>(x, P, c); });
+}
+template <class W>
+SED_HD Canon<W> canonicalize(W x, PlanView const& P) {
+  return canonicalize<W>(x, P, RowTab{P.row_min, P.row_set});
+}
+template <class W>
+SED_HD uint32_t representative_weight(W x, PlanView const& P) {
+  return representative_weight<W>(x, P, RowTab{P.row_min, P.row_set});
 }
 
 // ------------------------------------------------ fixed-weight word order ---

@@ -760,6 +760,70 @@ struct Solver {
   }
 };
 
+// ------------------------------------------------- mixed precision ----
+// FP32 Lanczos steps: vectors and their updates in FP32, reductions per warp
+// in FP32 and per block in FP64.
+__global__ void k_update32(float* __restrict__ V, uint64_t ld_v, uint64_t D, LzHeader const* h,
+                           double const* __restrict__ alpha, double const* __restrict__ beta,
+                           double* __restrict__ partial) {
+  __shared__ double red[kBlock / 32];
+  if (h->stop) return;
+  uint32_t const k = h->k;
+  float* w = V + (uint64_t)(k + 1) * ld_v;
+  float const* v = V + (uint64_t)k * ld_v;
+  float const* vp = k ? V + (uint64_t)(k - 1) * ld_v : v;
+  float const a = (float)alpha[k];
+  float const b = k ? (float)beta[k - 1] : 0.0f;
+  float part = 0.0f;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    float const wi = fmaf(-a, v[i], fmaf(-b, vp[i], w[i]));
+    w[i] = wi;
+    part = fmaf(wi, wi, part);
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  double const tot = block_sum((threadIdx.x & 31) == 0 ? (double)part : 0.0, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+__global__ void k_scale_next32(float* __restrict__ V, uint64_t ld_v, uint64_t D, LzHeader const* h,
+                               double const* __restrict__ beta) {
+  if (h->stop) return;
+  uint32_t const k = h->k;
+  double const b = beta[k];
+  if (!(b > 0.0)) return;
+  float const inv = (float)(1.0 / b);
+  float* w = V + (uint64_t)(k + 1) * ld_v;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    w[i] *= inv;
+}
+
+// out = s_0 psi + sum_{j=1}^{n-1} s_j V_j, accumulated in FP64.
+__global__ void k_ritz_mixed(double const* __restrict__ psi, float const* __restrict__ V, uint64_t ld_v,
+                             uint64_t D, double const* __restrict__ s, uint32_t n, double* __restrict__ out) {
+  __shared__ double c[2048];
+  for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) c[j] = s[j];
+  __syncthreads();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    double acc = c[0] * psi[i];
+    for (uint32_t j = 1; j < n; ++j) acc = fma(c[j], (double)V[(uint64_t)j * ld_v + i], acc);
+    out[i] = acc;
+  }
+}
+
+// v0 = (float) psi, v1 = (float) ((y - theta psi) / rn)
+__global__ void k_start_cycle(double const* __restrict__ psi, double const* __restrict__ y, uint64_t D,
+                              double theta, double inv_rn, float* __restrict__ v0, float* __restrict__ v1) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    double const p = psi[i];
+    v0[i] = (float)p;
+    v1[i] = (float)((y[i] - theta * p) * inv_rn);
+  }
+}
+
 uint32_t auto_basis(uint64_t D, size_t elem, uint32_t nev, uint32_t requested) {
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
@@ -907,6 +971,200 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
   return LS_SUCCESS;
 }
 
+// Mixed precision: FP64 anchor psi, FP32 Krylov cycles (see the file head).
+int solve_mixed(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* evals, void* evecs,
+                uint64_t ldv, double* rnorms, sed_eigh_info* info) {
+  auto t0 = std::chrono::steady_clock::now();
+  uint64_t const D = op.basis->D;
+  cudaStream_t stream = op.cuda_stream;
+  double const tol = o.tol > 0 ? o.tol : 1e-8;
+  uint64_t const max_iter = o.max_iter ? o.max_iter : 100000;
+  auto ts = std::chrono::steady_clock::now();
+  if (int st = operator_record_stream(op, stream)) return st;
+  if (int st = operator_prepare_fp32(op, stream)) return st;
+  double const setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
+  int const saved_form = op.form;
+  op.form = SED_FORM_STREAM;
+  struct FormGuard {
+    OperatorData& o;
+    int f;
+    ~FormGuard() { o.form = f; }
+  } form_guard{op, saved_form};
+  uint32_t const m = std::max<uint32_t>(3, auto_basis(D, 4, 1, o.max_basis ? o.max_basis : 300));
+  uint32_t const check = m < 64 ? 1u : 4u;
+  unsigned const vb = grid_size(D, op.basis->device, 8);
+  DeviceBuffer psi, y, V, hdr_b, alpha, beta, sbuf, work, partial;
+  if (int st = psi.allocate(D * 8)) return st;
+  if (int st = y.allocate(D * 8)) return st;
+  if (int st = V.allocate((size_t)m * D * 4)) return st;
+  if (int st = hdr_b.allocate(sizeof(LzHeader))) return st;
+  if (int st = alpha.allocate((size_t)m * 8)) return st;
+  if (int st = beta.allocate((size_t)m * 8)) return st;
+  if (int st = sbuf.allocate((size_t)kMaxNev * m * 8)) return st;
+  if (int st = work.allocate((size_t)5 * m * 8 + 64)) return st;
+  uint64_t const nb = std::max<uint64_t>((D + kBlock - 1) / kBlock + 64, vb);
+  if (int st = partial.allocate(nb * 16)) return st;
+  LzHeader* hh = nullptr;
+  SED_TRY_CUDA(cudaMallocHost(&hh, sizeof(LzHeader)));
+  struct HostGuard {
+    LzHeader* p;
+    ~HostGuard() { cudaFreeHost(p); }
+  } host_guard{hh};
+  LzHeader* h = hdr_b.as<LzHeader>();
+  float* Vf = V.as<float>();
+  // FP64 start vector
+  if (o.start == SED_START_GIVEN && o.start_vectors)
+    SED_TRY_CUDA(cudaMemcpyAsync(psi.ptr, o.start_vectors, D * 8, cudaMemcpyDefault, stream));
+  else
+    { k_random<double><<<vb, kBlock, 0, stream>>>(psi.as<double>(), D, o.seed); note_launches(1); }
+  auto sum2 = [&](int mode, double e, double& a, double& b) -> int {
+    { k_dots<double><<<vb, kBlock, 0, stream>>>(psi.as<double>(), y.as<double>(), D, e, mode, partial.as<double>()); note_launches(1); }
+    std::vector<double> hs(2 * (size_t)vb);
+    SED_TRY_CUDA(cudaMemcpyAsync(hs.data(), partial.ptr, hs.size() * 8, cudaMemcpyDeviceToHost, stream));
+    SED_TRY_CUDA(cudaStreamSynchronize(stream));
+    a = b = 0.0;
+    for (unsigned i = 0; i < vb; ++i) {
+      a += hs[2 * i];
+      b += hs[2 * i + 1];
+    }
+    return LS_SUCCESS;
+  };
+  // normalise psi: y <- psi so that mode 0 gives <psi,psi>
+  SED_TRY_CUDA(cudaMemcpyAsync(y.ptr, psi.ptr, D * 8, cudaMemcpyDeviceToDevice, stream));
+  double nn = 0, dummy = 0;
+  if (int st = sum2(0, 0.0, nn, dummy)) return st;
+  { k_scale<double><<<vb, kBlock, 0, stream>>>(psi.as<double>(), D, 1.0 / std::sqrt(nn)); note_launches(1); }
+  // graph of `check` FP32 steps
+  cudaGraphExec_t graph = nullptr;
+  size_t graph_kernels = 0;
+  {
+    cudaGraph_t g;
+    SED_TRY_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
+    int st = LS_SUCCESS;
+    unsigned spmv_blocks = 0;
+    for (uint32_t i = 0; i < check && st == LS_SUCCESS; ++i) {
+      k_zero_alpha<float><<<1, 1, 0, stream>>>(h, alpha.as<double>());
+      Indirect ind;
+      ind.k = &h->k;
+      ind.stop = &h->stop;
+      ind.ld = D;
+      ind.partial = partial.as<double>();
+      st = operator_apply_krylov32(op, Vf, ind, stream, &spmv_blocks);
+      if (st) break;
+      k_reduce<<<1, kRedThreads, 0, stream>>>(partial.as<double>(), spmv_blocks, h, alpha.as<double>(), 0);
+      k_update32<<<vb, kBlock, 0, stream>>>(Vf, D, D, h, alpha.as<double>(), beta.as<double>(), partial.as<double>());
+      k_reduce<<<1, kRedThreads, 0, stream>>>(partial.as<double>(), vb, h, beta.as<double>(), 1);
+      k_scale_next32<<<vb, kBlock, 0, stream>>>(Vf, D, D, h, beta.as<double>());
+      k_tridiag<<<1, 32, 0, stream>>>(h, alpha.as<double>(), beta.as<double>(), sbuf.as<double>(), work.as<double>());
+    }
+    set_capturing(false);
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (st) {
+      if (e == cudaSuccess) cudaGraphDestroy(g);
+      return st;
+    }
+    SED_TRY_CUDA(e);
+    cudaGraphGetNodes(g, nullptr, &graph_kernels);
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    SED_TRY_CUDA(e);
+  }
+  struct GraphGuard {
+    cudaGraphExec_t g;
+    ~GraphGuard() {
+      if (g) cudaGraphExecDestroy(g);
+    }
+  } graph_guard{graph};
+  uint64_t steps32 = 0, matvecs = 0, cycles = 0;
+  double E = 0.0, R = 1e300;
+  bool converged = false;
+  while (true) {
+    // FP64: theta = <psi, H psi>, r = H psi - theta psi
+    if (int st = operator_apply_device(op, 1, 1, psi.ptr, D, y.ptr, D, stream, SED_FORM_STREAM)) return st;
+    ++matvecs;
+    double pp = 0, py = 0;
+    if (int st = sum2(0, 0.0, pp, py)) return st;
+    E = py / pp;
+    double rr = 0, unused = 0;
+    if (int st = sum2(1, E, rr, unused)) return st;
+    R = std::sqrt(rr / pp);
+    if (o.progress) o.progress(o.progress_user, steps32 + matvecs, &E, &R, 1);
+    if (R <= tol) {
+      converged = true;
+      break;
+    }
+    if (steps32 >= max_iter || cycles >= 64) break;
+    // FP32 cycle from v0 = psi, v1 = r / ||r||
+    double const rn = R * std::sqrt(pp);
+    { k_start_cycle<<<vb, kBlock, 0, stream>>>(psi.as<double>(), y.as<double>(), D, E, 1.0 / rn, Vf, Vf + D); note_launches(1); }
+    std::memset(hh, 0, sizeof(LzHeader));
+    hh->k = 1;
+    hh->m_max = m;
+    hh->check = check;
+    hh->nev = 1;
+    hh->tol_est = std::max(0.5 * tol, 2e-6 * rn);
+    SED_TRY_CUDA(cudaMemcpyAsync(h, hh, sizeof(LzHeader), cudaMemcpyHostToDevice, stream));
+    double const a0 = E, b0 = rn;
+    SED_TRY_CUDA(cudaMemcpyAsync(alpha.ptr, &a0, 8, cudaMemcpyHostToDevice, stream));
+    SED_TRY_CUDA(cudaMemcpyAsync(beta.ptr, &b0, 8, cudaMemcpyHostToDevice, stream));
+    SED_TRY_CUDA(cudaStreamSynchronize(stream));
+    while (true) {
+      SED_TRY_CUDA(cudaGraphLaunch(graph, stream));
+      note_launches(graph_kernels);
+      SED_TRY_CUDA(cudaMemcpyAsync(hh, h, sizeof(LzHeader), cudaMemcpyDeviceToHost, stream));
+      SED_TRY_CUDA(cudaStreamSynchronize(stream));
+      if (hh->stop) break;
+      if (steps32 + hh->steps >= max_iter) break;
+    }
+    steps32 += hh->steps;
+    ++cycles;
+    uint32_t const n = hh->size ? hh->size : 1;
+    if (!hh->stop) break;  // out of steps
+    { k_ritz_mixed<<<vb, kBlock, 0, stream>>>(psi.as<double>(), Vf, D, D, sbuf.as<double>(), n, y.as<double>()); note_launches(1); }
+    SED_TRY_CUDA(cudaMemcpyAsync(psi.ptr, y.ptr, D * 8, cudaMemcpyDeviceToDevice, stream));
+    double pn = 0, d2 = 0;
+    if (int st = sum2(0, 0.0, pn, d2)) return st;  // y == psi here
+    { k_scale<double><<<vb, kBlock, 0, stream>>>(psi.as<double>(), D, 1.0 / std::sqrt(pn)); note_launches(1); }
+  }
+  // output
+  if (evecs) {
+    int const own = 1;
+    char* dst = static_cast<char*>(evecs);
+    if (out_dtype == own) {
+      SED_TRY_CUDA(cudaMemcpyAsync(dst, psi.ptr, D * 8, cudaMemcpyDefault, stream));
+    } else {
+      DeviceBuffer tmp;
+      if (int st = tmp.allocate(D * (size_t)elem_bytes(out_dtype))) return st;
+      switch (out_dtype) {
+        case 0: { k_convert<double, float><<<vb, kBlock, 0, stream>>>(psi.as<double>(), D, tmp.as<float>()); note_launches(1); } break;
+        case 2: { k_convert<double, float2><<<vb, kBlock, 0, stream>>>(psi.as<double>(), D, tmp.as<float2>()); note_launches(1); } break;
+        default: { k_convert<double, double2><<<vb, kBlock, 0, stream>>>(psi.as<double>(), D, tmp.as<double2>()); note_launches(1); } break;
+      }
+      SED_TRY_CUDA(cudaMemcpyAsync(dst, tmp.ptr, D * (size_t)elem_bytes(out_dtype), cudaMemcpyDefault, stream));
+    }
+  }
+  SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  if (evals) evals[0] = E;
+  if (rnorms) rnorms[0] = R;
+  double const total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (info) {
+    info->iterations = steps32 + matvecs;
+    info->matvecs = steps32 + matvecs;
+    info->restarts = cycles;
+    info->fp32_iterations = steps32;
+    info->seconds_total = total;
+    info->seconds_setup = setup;
+    info->seconds_solve = total - setup;
+  }
+  if (logging_enabled())
+    log_line("sed_eigh (mixed): E0 = %.15g, residual %.3e, %llu FP32 steps, %llu FP64 matvecs, %llu cycles, %.3f s",
+             E, R, (unsigned long long)steps32, (unsigned long long)matvecs, (unsigned long long)cycles, total);
+  if (!converged)
+    return fail(LS_NOT_CONVERGED, "mixed precision: residual " + std::to_string(R) + " above tolerance");
+  return LS_SUCCESS;
+}
+
 }  // namespace
 }  // namespace sed
 
@@ -951,6 +1209,8 @@ int sed_eigh(ls_operator const* op, int dtype, sed_eigh_options const* opts, dou
     ScopedDevice dev(d.basis->device);
     if (int st = operator_ensure_ready(d)) return st;
     if (dtype >= 2 || !d.is_real) return solve<double2>(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);
+    if (o.precision == SED_PRECISION_MIXED && o.nev == 1 && o.form != SED_FORM_ON_THE_FLY)
+      return solve_mixed(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);
     return solve<double>(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);
   } catch (std::exception const& e) {
     return fail(LS_SYSTEM_ERROR, e.what());

@@ -45,35 +45,76 @@ __global__ void k_count(uint64_t const* __restrict__ reps, uint64_t D, TermsView
 }
 
 constexpr unsigned kRecWarps = 4;    // warps per block of k_record
-constexpr unsigned kRecMaxElems = 96; // flattened path: elements per row
+constexpr unsigned kRecMaxElems = 80; // flattened path: elements per row
 
-// Records the stream form. One warp per SELL-32 slice. When the slice is at
-// most kRecMaxElems wide, each lane first lists its row's elements as
-// (tuple, column) descriptors in shared memory and the warp then walks the
-// flattened (row, element) list 32 at a time, so rows of different length do
-// not leave lanes idle; wider slices fall back to one row per lane. Entries
-// land in the same slots (slice_ptr + 32 e + row) either way.
+size_t record_smem_bytes() {
+  return (size_t)kRecWarps * 32 * kRecMaxElems * 4      // element descriptors
+         + (size_t)kRecWarps * 32 * SED_PARAM_COSETS * 8  // coset images of each row
+         + SED_PARAM_COSETS * 64                         // bit landing positions
+         + 2048 * 2;                                     // row tables
+}
+
+// Records the stream form. One warp per SELL-32 slice (lane = row).
+//  - Each lane applies the coset representatives to its row's representative
+//    r once (Benes networks) and keeps the images in shared memory; an
+//    element s = r ^ d (d: the few flipped bits) then costs
+//    P_c(s) = P_c(r) ^ P_c(d), with P_c(d) assembled from the bit landing
+//    table, instead of a full network per coset.
+//  - When the slice is at most kRecMaxElems wide, each lane lists its row's
+//    elements as (tuple, column) descriptors and the warp walks the flattened
+//    (row, element) list 32 at a time, so rows of different length do not
+//    leave lanes idle; wider slices fall back to one row per lane.
+// Entries land in the same slots (slice_ptr + 32 e + row) either way.
 template <class W, bool Real>
-__global__ void __launch_bounds__(kRecWarps * 32)
-    k_record(PlanView P, IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
-             uint64_t n_slices, uint64_t const* __restrict__ slice_ptr, uint32_t col_bits, bool packed,
-             uint32_t* __restrict__ entries, uint16_t* __restrict__ codes, void* __restrict__ diag,
-             uint8_t* __restrict__ row_class) {
-  __shared__ uint32_t desc[kRecWarps][32][kRecMaxElems];  // q << 28 | tuple << 8 | column a'
+__global__ void __launch_bounds__(kRecWarps * 32, 1)
+    k_record(__grid_constant__ const PlanView P, IndexView I, TermsView T, CodeView C,
+             uint32_t const* __restrict__ weights, uint64_t n_slices, uint64_t const* __restrict__ slice_ptr,
+             uint32_t col_bits, bool packed, uint32_t* __restrict__ entries, uint16_t* __restrict__ codes,
+             void* __restrict__ diag, uint8_t* __restrict__ row_class) {
+  extern __shared__ __align__(16) unsigned char rec_smem[];
+  uint32_t* desc_all = reinterpret_cast<uint32_t*>(rec_smem);
+  W* imgs_all = reinterpret_cast<W*>(rec_smem + (size_t)kRecWarps * 32 * kRecMaxElems * 4);
+  uint8_t* pos_s = rec_smem + (size_t)kRecWarps * 32 * kRecMaxElems * 4 +
+                   (size_t)kRecWarps * 32 * SED_PARAM_COSETS * 8;
+  uint16_t* srow = reinterpret_cast<uint16_t*>(pos_s + SED_PARAM_COSETS * 64);
+  RowTab const RT = stage_rows(P, srow);
+  bool const use_pos = P.fixed_nets != 0;
+  if (use_pos) {
+    for (uint32_t q = threadIdx.x; q < P.n_cosets * 64; q += blockDim.x) pos_s[q] = P.pos[q];
+    __syncthreads();
+  }
   uint32_t const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t const s = (uint64_t)blockIdx.x * kRecWarps + warp;
   if (s >= n_slices) return;  // warp-uniform
+  uint32_t* desc = desc_all + (size_t)warp * 32 * kRecMaxElems;
+  W* imgs = imgs_all + (size_t)warp * 32 * SED_PARAM_COSETS;
   uint64_t const i = s * 32 + lane;
   uint64_t const base = slice_ptr[s];
   uint32_t const width = (uint32_t)((slice_ptr[s + 1] - base) >> 5);
   bool const valid = i < I.D;
   uint64_t const r = valid ? I.reps[i] : 0;
-  auto emit = [&](uint32_t e, uint32_t row, uint64_t st, uint32_t vid) {
-    auto const c = canonicalize<W>((W)st, P);
-    int64_t const j = find_index((uint64_t)c.rep, I);
+  if (use_pos)
+    for (uint32_t c = 0; c < P.n_cosets; ++c) imgs[lane * SED_PARAM_COSETS + c] = coset_apply<W>((W)r, P, c);
+  __syncwarp();
+  auto emit = [&](uint32_t e, uint32_t row, uint64_t r_row, uint64_t st, uint32_t vid) {
+    W const x = (W)st;
+    W const delta = (W)(st ^ r_row);
+    auto img = [&](uint32_t c) -> W {
+      if (c == 0) return x;
+      if (!use_pos) return coset_apply<W>(x, P, c);
+      W d = delta, pd = 0;
+      while (d) {
+        uint32_t const b = (uint32_t)__ffsll((long long)(uint64_t)d) - 1u;
+        d &= d - 1;
+        pd |= (W)1 << pos_s[c * 64 + b];
+      }
+      return imgs[row * SED_PARAM_COSETS + c] ^ pd;
+    };
+    auto const cz = canonicalize_img<W>(x, P, RT, img);
+    int64_t const j = find_index((uint64_t)cz.rep, I);
     uint32_t ent = kNull, code = 0;
     if (j >= 0) {
-      code = element_code(vid, c.phase, weights[j], C);
+      code = element_code(vid, cz.phase, weights[j], C);
       ent = packed ? ((uint32_t)j | (code << col_bits)) : (uint32_t)j;
     }
     entries[base + (uint64_t)e * 32 + row] = ent;
@@ -88,7 +129,7 @@ __global__ void __launch_bounds__(kRecWarps * 32)
         uint32_t const a = local_index(r, T.tuple_sites[u], k);
         uint32_t const n = T.n_off[t * 16 + a];
         for (uint32_t q = 0; q < n; ++q)
-          desc[warp][lane][count++] = (q << 28) | (u << 8) | T.off_col[(t * 16 + a) * 16 + q];
+          desc[lane * kRecMaxElems + count++] = (q << 28) | (u << 8) | T.off_col[(t * 16 + a) * 16 + q];
       }
     }
     __syncwarp();
@@ -113,18 +154,18 @@ __global__ void __launch_bounds__(kRecWarps * 32)
       uint64_t const r_row = __shfl_sync(0xffffffffu, r, row);
       if (f < total) {
         uint32_t const e = f - ex_row;
-        uint32_t const d = desc[warp][row][e];
+        uint32_t const d = desc[row * kRecMaxElems + e];
         uint32_t const u = (d >> 8) & 0xFFFFu, a2 = d & 0xFFu, q = d >> 28;
         uint32_t const tk = T.tuple_term[u];
         uint32_t const t = tk & 0xFFFFu, k = tk >> 16;
         uint32_t const sites = T.tuple_sites[u];
         uint32_t const a = local_index(r_row, sites, k);
-        emit(e, row, replace_local(r_row, sites, k, a2), T.off_vid[(t * 16 + a) * 16 + q]);
+        emit(e, row, r_row, replace_local(r_row, sites, k, a2), T.off_vid[(t * 16 + a) * 16 + q]);
       }
     }
   } else if (valid) {
     walk_row(r, T, [&](uint32_t e, uint64_t st, uint32_t vid) {
-      emit(e, lane, st, vid);
+      emit(e, lane, r, st, vid);
       count = e + 1;
     });
   }
@@ -181,12 +222,14 @@ __global__ void __launch_bounds__(kBlock) k_spmv(StreamView S, uint64_t D, X con
 // On-the-fly matvec: same sum, same order, recomputing every element.
 template <class W, class X, bool RealOp>
 __global__ void __launch_bounds__(kBlock)
-    k_otf(PlanView P, IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
+    k_otf(__grid_constant__ const PlanView P, IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
           void const* __restrict__ table, double const* __restrict__ inv_sqrt_s,
           X const* __restrict__ x, X* __restrict__ y, Indirect ind) {
   using V = typename Store<X>::V;
   __shared__ double red[kBlock / 32];
+  __shared__ uint16_t srow[2048];
   if (ind.stop && *ind.stop) return;
+  RowTab const RT = stage_rows(P, srow);
   if (ind.k) {
     uint64_t const k = *ind.k;
     x += k * ind.ld;
@@ -198,7 +241,7 @@ __global__ void __launch_bounds__(kBlock)
     uint64_t const r = I.reps[i];
     V acc = zero<V>();
     walk_row(r, T, [&](uint32_t, uint64_t st, uint32_t vid) {
-      auto const c = canonicalize<W>((W)st, P);
+      auto const c = canonicalize<W>((W)st, P, RT);
       int64_t const j = find_index((uint64_t)c.rep, I);
       if (j >= 0) {
         uint32_t const code = element_code(vid, c.phase, weights[j], C);
@@ -526,7 +569,9 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     auto launch = [&](auto w_tag, auto real_tag) {
       using W = decltype(w_tag);
       constexpr bool R = decltype(real_tag)::value;
-      { k_record<W, R><<<(unsigned)((n_slices + kRecWarps - 1) / kRecWarps), kRecWarps * 32, 0, stream>>>(
+      size_t const smem = record_smem_bytes();
+      cudaFuncSetAttribute(k_record<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      { k_record<W, R><<<(unsigned)((n_slices + kRecWarps - 1) / kRecWarps), kRecWarps * 32, smem, stream>>>(
           b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices,
           sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(),
           sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>()); note_launches(1); }
@@ -645,6 +690,113 @@ int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void cons
     if (st) return st;
   }
   return LS_SUCCESS;
+}
+
+namespace {
+
+__global__ void k_to_float(double const* __restrict__ a, uint64_t n, float* __restrict__ b) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// FP32 streamed SpMV (real operators): FP32 entries of the value table and
+// diagonal, FP32 accumulation per row; the partial sums of x_i y_i are
+// reduced per warp in FP32 and per block in FP64.
+template <bool Packed>
+__global__ void __launch_bounds__(kBlock)
+    k_spmv32(StreamView S, float const* __restrict__ table_f, float const* __restrict__ diag_f,
+             float const* __restrict__ invs_f, uint64_t D, float const* __restrict__ x,
+             float* __restrict__ y, Indirect ind) {
+  __shared__ float tab[8192];
+  __shared__ double red[kBlock / 32];
+  if (ind.stop && *ind.stop) return;
+  if (ind.k) {
+    uint64_t const k = *ind.k;
+    x += k * ind.ld;
+    y += (k + 1) * ind.ld;
+  }
+  bool const in_smem = S.n_codes <= 8192u;
+  if (in_smem) {
+    for (uint32_t c = threadIdx.x; c < S.n_codes; c += blockDim.x) tab[c] = table_f[c];
+    __syncthreads();
+  }
+  float const* tb = in_smem ? tab : table_f;
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  float part = 0.0f;
+  if ((s << 5) < D) {
+    uint32_t const lane = threadIdx.x & 31;
+    uint64_t const base = S.slice_ptr[s];
+    uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
+    uint32_t const col_mask = Packed ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
+    float acc = 0.0f;
+    uint32_t const* ent = S.entries + base + lane;
+    for (uint32_t e = 0; e < width; ++e) {
+      uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
+      if (v != kNull) {
+        uint32_t const col = v & col_mask;
+        uint32_t const code =
+            Packed ? (v >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)e * 32);
+        acc = fmaf(tb[code], x[col], acc);
+      }
+    }
+    if (i < D) {
+      float const xi = x[i];
+      float const yi = fmaf(diag_f[i], xi, invs_f[S.row_class[i]] * acc);
+      y[i] = yi;
+      part = xi * yi;
+    }
+  }
+  if (ind.partial) {
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    double const tot = block_sum((threadIdx.x & 31) == 0 ? (double)part : 0.0, red);
+    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
+  }
+}
+
+}  // namespace
+
+int operator_prepare_fp32(OperatorData& op, cudaStream_t stream) {
+  StreamForm& sf = op.stream;
+  if (!sf.ready) return fail(LS_CACHE_NOT_BUILT, "the FP32 SpMV needs the stream form");
+  if (!op.is_real) return fail(LS_OPERATOR_IS_COMPLEX, "the FP32 Krylov phase supports real operators");
+  if (sf.diag_f.ptr) return LS_SUCCESS;
+  OperatorTables const& tb = *op.tables;
+  uint64_t const D = op.basis->D;
+  if (int st = sf.diag_f.allocate(std::max<uint64_t>(1, D) * 4)) return st;
+  if (int st = sf.table_f.allocate((size_t)tb.n_codes * 4)) return st;
+  if (int st = sf.invs_f.allocate((size_t)tb.code.n_div * 4)) return st;
+  { k_to_float<<<grid_size(D, op.basis->device, 8), kBlock, 0, stream>>>(sf.diag.as<double>(), D, sf.diag_f.as<float>()); note_launches(1); }
+  { k_to_float<<<1, kBlock, 0, stream>>>(tb.table.as<double>(), tb.n_codes, sf.table_f.as<float>()); note_launches(1); }
+  { k_to_float<<<1, kBlock, 0, stream>>>(tb.inv_sqrt_s.as<double>(), tb.code.n_div, sf.invs_f.as<float>()); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  return LS_SUCCESS;
+}
+
+namespace {
+int launch32(OperatorData& op, float const* x, float* y, Indirect ind, cudaStream_t stream, unsigned* blocks) {
+  StreamForm const& sf = op.stream;
+  if (!sf.diag_f.ptr) return fail(LS_CACHE_NOT_BUILT, "FP32 companions are not prepared");
+  StreamView const S = stream_view(op);
+  unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
+  if (blocks) *blocks = grid;
+  if (sf.packed)
+    { k_spmv32<true><<<grid, kBlock, 0, stream>>>(S, sf.table_f.as<float>(), sf.diag_f.as<float>(), sf.invs_f.as<float>(), op.basis->D, x, y, ind); note_launches(1); }
+  else
+    { k_spmv32<false><<<grid, kBlock, 0, stream>>>(S, sf.table_f.as<float>(), sf.diag_f.as<float>(), sf.invs_f.as<float>(), op.basis->D, x, y, ind); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+}  // namespace
+
+int operator_apply_krylov32(OperatorData& op, float* base, Indirect ind, cudaStream_t stream, unsigned* blocks) {
+  return launch32(op, base, base, ind, stream, blocks);
+}
+
+int operator_apply32(OperatorData& op, float const* x, float* y, cudaStream_t stream) {
+  return launch32(op, x, y, Indirect{}, stream, nullptr);
 }
 
 int operator_apply_krylov(OperatorData& op, int dtype, void* base, Indirect ind, cudaStream_t stream,

@@ -186,6 +186,12 @@ __device__ __forceinline__ void const* stage_table(StreamView const& S, unsigned
 }
 
 StreamView stream_view(OperatorData const& op);
+// FP32 streamed SpMV in Krylov-indirect mode (x = base + k ld, y = base +
+// (k+1) ld); FP32 arithmetic, per-block partial sums of x_i y_i in FP64.
+int operator_apply_krylov32(OperatorData& op, float* base, Indirect ind, cudaStream_t stream,
+                            unsigned* blocks);
+// The same SpMV on explicit FP32 vectors.
+int operator_apply32(OperatorData& op, float const* x, float* y, cudaStream_t stream);
 // Krylov-indirect apply (see Indirect); `blocks` receives the grid size, i.e.
 // the number of partial sums written.
 int operator_apply_krylov(OperatorData& op, int dtype, void* base, Indirect ind, cudaStream_t stream,

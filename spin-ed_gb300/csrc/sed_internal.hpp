@@ -97,6 +97,8 @@ struct SymPlanHost {
   unsigned group_order = 1;         // including inversion
   unsigned n_cosets = 1, n_h = 1, n_stages = 0, n_terms = 1;
   std::vector<uint64_t> benes_mask;  // [n_cosets][n_stages]
+  std::vector<uint64_t> full_nets;   // [n_cosets][SED_MAX_STAGES] unpruned networks
+  std::vector<uint8_t> pos;          // [n_cosets][64] landing position of each bit
   std::vector<uint32_t> benes_shift; // [n_stages]
   std::vector<uint64_t> h_mask;      // [n_h][n_terms]
   std::vector<uint32_t> h_rot;       // [n_h][n_terms] left-rotate amounts
@@ -108,6 +110,12 @@ struct SymPlanHost {
   unsigned cyc_phase[2] = {0, 0};
   unsigned cyc_rot[2][2] = {{0, 0}, {0, 0}};
   uint64_t cyc_mask[2][2] = {{0, 0}, {0, 0}};
+  // row structure (see PlanView::rows)
+  unsigned rows = 0, row_bits = 0, n_rows = 1, rot_phase = 0, shift_phase = 0;
+  uint64_t row_mask = 0;
+  std::vector<uint16_t> row_min, row_set;
+  std::vector<uint64_t> rot_mask, sh_mask;
+  std::vector<uint32_t> rot_rot, rot_exp, sh_rot, sh_exp;
   PlanView view() const;
 };
 
@@ -165,6 +173,10 @@ struct StreamForm {
   DeviceBuffer inv_sqrt_s;      // double[n classes]
   unsigned n_codes = 0;
   double seconds = 0;
+  // FP32 companions for the mixed-precision Krylov phase (real operators)
+  DeviceBuffer diag_f;   // float[D]
+  DeviceBuffer table_f;  // float[n_codes]
+  DeviceBuffer invs_f;   // float[n classes]
   uint64_t bytes() const {
     return slice_ptr.bytes + entries.bytes + values.bytes + diag.bytes + row_class.bytes +
            table.bytes + inv_sqrt_s.bytes;
@@ -193,6 +205,8 @@ int operator_upload_terms(OperatorData& op);
 int operator_record_stream(OperatorData& op, cudaStream_t stream);
 int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void const* x,
                           uint64_t ldx, void* y, uint64_t ldy, cudaStream_t stream, int form);
+// FP32 companions of the stream form (mixed-precision Krylov phase).
+int operator_prepare_fp32(OperatorData& op, cudaStream_t stream);
 
 bool characters_real(BasisData const& b);
 

@@ -256,6 +256,7 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
   }
 
   // H as a product of at most two cyclic groups of two-term generators.
+  unsigned cyc_g[2] = {0, 0};
   if (H.size() > 1) {
     auto order_of = [&](unsigned g) { return (unsigned)closure_of({g}).size(); };
     auto two_terms = [&](unsigned g, std::vector<uint64_t>& m, std::vector<uint32_t>& r) {
@@ -283,6 +284,8 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
         }
       }
     if (found) {
+      cyc_g[0] = g1;
+      cyc_g[1] = g2;
       unsigned const gens[2] = {g1, g2};
       for (int q = 0; q < 2; ++q) {
         std::vector<uint64_t> m;
@@ -348,6 +351,12 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
     for (size_t s = 0; s < shifts.size(); ++s)
       if (nets[c][s]) used[s] = true;
   }
+  out.pos.assign(cosets.size() * 64, 0);
+  for (size_t c = 0; c < cosets.size(); ++c)
+    for (unsigned j = 0; j < n_bits; ++j) out.pos[c * 64 + elems[cosets[c]][j]] = (uint8_t)j;  // bit p[j] -> j
+  out.full_nets.assign(cosets.size() * SED_MAX_STAGES, 0);
+  for (size_t c = 0; c < cosets.size(); ++c)
+    for (size_t st = 0; st < shifts.size(); ++st) out.full_nets[c * SED_MAX_STAGES + st] = nets[c][st];
   out.benes_shift.clear();
   for (size_t s = 0; s < shifts.size(); ++s)
     if (used[s]) out.benes_shift.push_back(shifts[s]);
@@ -385,12 +394,133 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
                                               v.n_terms);
       if (want != got) return fail(LS_SYSTEM_ERROR, "shift decomposition failed");
     }
+  // Row structure: a rotation within rows of B bits (and a cyclic shift of rows).
+  if (out.cyc) {
+    unsigned const gens[2] = {cyc_g[0], cyc_g[1]};
+    auto rotation_rows = [&](unsigned g, unsigned& B) -> bool {  // +-1 rotation inside rows
+      B = closure_of({g}).size();
+      if (B < 2 || n_bits % B) return false;
+      int d = -1;
+      for (unsigned i = 0; i < n_bits; ++i) {
+        unsigned const q = elems[g][i];
+        if (q / B != i / B) return false;
+        int const di = (int)((q % B + B - i % B) % B);
+        if (d < 0) d = di;
+        if (di != d) return false;
+      }
+      return d == 1 || d == (int)B - 1;
+    };
+    auto shift_rows = [&](unsigned g, unsigned B) -> bool {  // +-B shift of the whole word
+      unsigned const R = n_bits / B;
+      if (closure_of({g}).size() != R) return false;
+      for (int sgn : {1, -1}) {
+        bool ok = true;
+        for (unsigned i = 0; i < n_bits && ok; ++i)
+          ok = elems[g][i] == (unsigned)(((int)i + sgn * (int)B + 2 * (int)n_bits) % (int)n_bits);
+        if (ok) return true;
+      }
+      return false;
+    };
+    unsigned rot_g = 0, sh_g = 0, B = 0;
+    bool found = false;
+    if (out.cyc == 1 && rotation_rows(gens[0], B) && B == n_bits) {
+      rot_g = gens[0];
+      found = true;
+      out.rows = 2;
+    } else if (out.cyc == 2) {
+      for (int q = 0; q < 2 && !found; ++q) {
+        unsigned Bq = 0;
+        if (rotation_rows(gens[q], Bq) && Bq <= 10 && Bq < n_bits && shift_rows(gens[1 - q], Bq)) {
+          rot_g = gens[q];
+          sh_g = gens[1 - q];
+          B = Bq;
+          found = true;
+          out.rows = 1;
+        }
+      }
+    }
+    if (found && n_bits / B > SED_MAX_ROWS) found = false, out.rows = 0;
+    if (found) {
+      out.row_bits = B;
+      out.n_rows = n_bits / B;
+      out.row_mask = B == 64 ? ~(uint64_t)0 : (((uint64_t)1 << B) - 1);
+      out.rot_phase = phase[rot_g];
+      out.shift_phase = sh_g ? phase[sh_g] : 0u;
+      out.rot_mask.assign(2 * B, 0);
+      out.rot_rot.assign(2 * B, 0);
+      out.rot_exp.assign(B, 0);
+      out.sh_mask.assign(2 * out.n_rows, 0);
+      out.sh_rot.assign(2 * out.n_rows, 0);
+      out.sh_exp.assign(out.n_rows, 0);
+      bool ok = true;
+      std::vector<uint8_t> pw = elems[0];
+      for (unsigned a = 0; a < B && ok; ++a) {  // powers of the rotation generator
+        unsigned q = 0;
+        while (pw[q] != 0) ++q;  // where bit 0 of the source lands
+        unsigned const r = q % B;
+        std::vector<uint64_t> m;
+        std::vector<uint32_t> rr;
+        ok = q < B && shift_terms(pw, width, 2, m, rr);
+        if (ok) {
+          out.rot_exp[r] = a;
+          for (size_t t = 0; t < m.size(); ++t) {
+            out.rot_mask[2 * r + t] = m[t];
+            out.rot_rot[2 * r + t] = rr[t];
+          }
+        }
+        pw = compose(pw, elems[rot_g]);
+      }
+      pw = elems[0];
+      for (unsigned b = 0; b < out.n_rows && ok; ++b) {  // powers of the shift generator
+        unsigned q = 0;
+        while (pw[q] != 0) ++q;
+        unsigned const t = (out.n_rows - q / B) % out.n_rows;
+        std::vector<uint64_t> m;
+        std::vector<uint32_t> rr;
+        ok = shift_terms(pw, width, 2, m, rr);
+        if (ok) {
+          out.sh_exp[t] = b;
+          for (size_t k = 0; k < m.size(); ++k) {
+            out.sh_mask[2 * t + k] = m[k];
+            out.sh_rot[2 * t + k] = rr[k];
+          }
+        }
+        if (sh_g) pw = compose(pw, elems[sh_g]);
+      }
+      if (out.rows == 2) {  // no shift generator: the single "shift" is the identity
+        out.sh_mask[0] = out.mask;
+        out.sh_mask[1] = 0;
+        out.sh_rot[0] = out.sh_rot[1] = 0;
+        out.sh_exp[0] = 0;
+      }
+      if (out.rows == 1) {
+        unsigned const nv = 1u << B;
+        out.row_min.assign(nv, 0);
+        out.row_set.assign(nv, 0);
+        for (unsigned v = 0; v < nv; ++v) {
+          unsigned best = ~0u, set = 0;
+          for (unsigned r = 0; r < B; ++r) {
+            unsigned const w = r ? (((v << r) | (v >> (B - r))) & (nv - 1)) : v;
+            if (w < best) {
+              best = w;
+              set = 0;
+            }
+            if (w == best) set |= 1u << r;
+          }
+          out.row_min[v] = (uint16_t)best;
+          out.row_set[v] = (uint16_t)set;
+        }
+      }
+      if (!ok) out.rows = 0;
+    }
+  }
   if (out.cyc) {
     PlanView vx = out.view();
     PlanView ve = vx;
     ve.cyc = 0;
+    ve.rows = 0;
     uint64_t rng = 0x9E3779B97F4A7C15ull;
-    for (int t = 0; t < 256; ++t) {
+    for (int t = 0; t < 2048; ++t) {
       rng ^= rng << 13;
       rng ^= rng >> 7;
       rng ^= rng << 17;
@@ -398,20 +528,29 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
       bool same;
       if (width == 32) {
         auto c1 = canonicalize<uint32_t>((uint32_t)x, vx), c2 = canonicalize<uint32_t>((uint32_t)x, ve);
-        same = c1.rep == c2.rep && representative_weight<uint32_t>((uint32_t)x, vx) ==
-                                       representative_weight<uint32_t>((uint32_t)x, ve);
+        uint32_t const w1 = representative_weight<uint32_t>((uint32_t)x, vx);
+        uint32_t const w2 = representative_weight<uint32_t>((uint32_t)x, ve);
+        same = c1.rep == c2.rep && w1 == w2 &&
+               (representative_weight<uint32_t>(c2.rep, ve) == 0 || c1.phase == c2.phase);
+        uint32_t const r = c2.rep;  // the representative itself: weights must agree too
+        same = same && representative_weight<uint32_t>(r, vx) == representative_weight<uint32_t>(r, ve);
       } else {
         auto c1 = canonicalize<uint64_t>(x, vx), c2 = canonicalize<uint64_t>(x, ve);
-        same = c1.rep == c2.rep &&
-               representative_weight<uint64_t>(x, vx) == representative_weight<uint64_t>(x, ve);
+        uint32_t const w1 = representative_weight<uint64_t>(x, vx);
+        uint32_t const w2 = representative_weight<uint64_t>(x, ve);
+        same = c1.rep == c2.rep && w1 == w2 &&
+               (representative_weight<uint64_t>(c2.rep, ve) == 0 || c1.phase == c2.phase);
+        uint64_t const r = c2.rep;
+        same = same && representative_weight<uint64_t>(r, vx) == representative_weight<uint64_t>(r, ve);
       }
-      if (!same) return fail(LS_SYSTEM_ERROR, "cyclic subgroup walk disagrees with the explicit list");
+      if (!same) return fail(LS_SYSTEM_ERROR, "structured subgroup walk disagrees with the explicit list");
     }
   }
   if (logging_enabled())
-    log_line("symmetry plan: |G| = %u (x%u inversion), |H| = %u (cyclic product: %u), cosets = %u, "
-             "stages = %u, terms = %u",
-             G, spin_inversion ? 2u : 1u, out.n_h, out.cyc, out.n_cosets, out.n_stages, out.n_terms);
+    log_line("symmetry plan: |G| = %u (x%u inversion), |H| = %u (cyclic product: %u, rows: %u of %u bits, "
+             "mode %u), cosets = %u, stages = %u, terms = %u",
+             G, spin_inversion ? 2u : 1u, out.n_h, out.cyc, out.n_rows, out.row_bits, out.rows, out.n_cosets,
+             out.n_stages, out.n_terms);
   return LS_SUCCESS;
 }
 
@@ -432,6 +571,25 @@ PlanView SymPlanHost::view() const {
   v.h_rot = h_rot.data();
   v.coset_phase = coset_phase.data();
   v.h_phase = h_phase.data();
+  v.pos = pos.data();
+  v.fixed_nets = n_cosets <= SED_PARAM_COSETS ? 1u : 0u;
+  for (unsigned c = 0; c < SED_PARAM_COSETS; ++c)
+    for (unsigned st = 0; st < SED_MAX_STAGES; ++st)
+      v.nets[c][st] = (v.fixed_nets && c < n_cosets) ? full_nets[c * SED_MAX_STAGES + st] : 0;
+  v.rows = rows;
+  v.row_bits = row_bits;
+  v.n_rows = n_rows;
+  v.rot_phase = rot_phase;
+  v.shift_phase = shift_phase;
+  v.row_mask = row_mask;
+  v.row_min = row_min.data();
+  v.row_set = row_set.data();
+  v.rot_mask = rot_mask.data();
+  v.rot_rot = rot_rot.data();
+  v.rot_exp = rot_exp.data();
+  v.sh_mask = sh_mask.data();
+  v.sh_rot = sh_rot.data();
+  v.sh_exp = sh_exp.data();
   v.cyc = cyc;
   for (int q = 0; q < 2; ++q) {
     v.cyc_ord[q] = cyc_ord[q];

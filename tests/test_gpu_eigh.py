@@ -87,3 +87,22 @@ def test_start_vector_philox_parity(sed, oracle):
     res2 = sed.eigh(built.hamiltonian, start=v / np.linalg.norm(v))
     assert res.eigenvalues[0] == pytest.approx(res2.eigenvalues[0], rel=1e-12)
     assert res.iterations == res2.iterations
+
+
+@pytest.mark.parametrize("name,model", [
+    ("chain24", lattices.heisenberg_chain(24)),
+    ("chain20_j2", lattices.heisenberg_chain(20, j2=0.45)),
+    ("square4_inv-", lattices.heisenberg_square(4, spin_inversion=-1)),
+])
+def test_mixed_precision_matches_fp64_oracle(sed, oracle, name, model):
+    """FP32-stored Krylov cycles anchored on an FP64 vector: eigenvalue within
+    1e-10 relative of the FP64 oracle, residual <= 1e-8 (recomputed here)."""
+    from spined import _lib as L
+    built, ob, oop = both(sed, oracle, model)
+    A = oop.sparse()
+    ev, _, _, _ = oracle.lanczos_ground_state(lambda v: A @ v, oracle.start_vector(1234, A.shape[0]))
+    res = sed.eigh(built.hamiltonian, seed=1234, precision=L.SED_PRECISION_MIXED)
+    assert res.fp32_iterations > 0
+    assert res.eigenvalues[0] == pytest.approx(ev[0], rel=EV_RTOL)
+    assert res.residuals[0] <= RES_TOL
+    check_pair(oop, res.eigenvalues[0], res.eigenvectors[:, 0])
