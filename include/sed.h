@@ -274,6 +274,45 @@ SED_API int sed_basis_index(ls_spin_basis const* basis, uint64_t representative,
 SED_API int sed_basis_state_info(ls_spin_basis const* basis, uint64_t bits, uint64_t* representative,
                          unsigned* phase, unsigned* phase_modulus);
 
+/* ------------------------------------------------ learned start vector ---
+ * No counterpart in the reference, which always starts PRIMME from its own
+ * random vector (src/SpinED.hs:385-394). A small MLP over spin
+ * configurations, x_j = +1/-1 for spin j up/down:
+ *   h1 = tanh(W1 x + b1), h2 = tanh(W2 h1 + b2), (a, s) = W3 h2 + b3,
+ * a ~ log|psi(x)| and s the logit of "sign psi(x) = (-1)^popcount(x &
+ * sign_mask)". Weights: FP32 master copy (Adam), BF16 in the passes, FP32
+ * accumulation. Parameters are one FP32 blob in the order W1 [hidden x n],
+ * b1, W2 [hidden x hidden], b2, W3 [2 x hidden], b3 (row-major). The network
+ * lives on the current device. Host or device pointers are accepted
+ * everywhere below. */
+typedef struct sed_mlp sed_mlp;
+SED_API int sed_mlp_create(sed_mlp** out, unsigned n_inputs, unsigned hidden, uint64_t sign_mask, uint64_t seed);
+SED_API void sed_mlp_destroy(sed_mlp* mlp);
+SED_API uint64_t sed_mlp_num_params(sed_mlp const* mlp);
+SED_API int sed_mlp_get_params(sed_mlp const* mlp, float* out);
+SED_API int sed_mlp_set_params(sed_mlp* mlp, float const* in);
+/* out[2 i], out[2 i + 1] = (a, s) for states[i]. */
+SED_API int sed_mlp_forward(sed_mlp* mlp, uint64_t const* states, uint64_t n, float* out);
+/* Loss L = mean_i [(a_i - t_abs_i)^2 + BCE(s_i, y_i)], y_i = [t_sign_i (1 if
+ * psi_i > 0, else 0) agrees with the prior], and dL/dparams (same layout as
+ * the parameters; grads may be NULL). At most 2^20 samples. */
+SED_API int sed_mlp_loss_grad(sed_mlp* mlp, uint64_t const* states, float const* t_abs, float const* t_sign,
+                              uint64_t n, double* loss, float* grads);
+/* Adam (0.9, 0.999, 1e-8) on mini-batches of `batch` samples, reshuffled
+ * every epoch; final_loss (may be NULL) is the loss of the last batch. */
+SED_API int sed_mlp_train(sed_mlp* mlp, uint64_t const* states, float const* t_abs, float const* t_sign, uint64_t n,
+                          unsigned epochs, unsigned batch, float lr, uint64_t seed, double* final_loss);
+/* Training data from a real vector psi over the built basis: n representatives
+ * drawn with probability psi_r^2 / ||psi||^2 (Philox from `seed`), labelled
+ * t_abs = log|psi_r n_r| (the amplitude of the configuration itself, n_r =
+ * ||P r||) and t_sign = [psi_r > 0]. */
+SED_API int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, uint64_t seed,
+                           uint64_t* states, float* t_abs, float* t_sign);
+/* Start vector over the built basis: v_r = prior(r) sign(s_r) exp(a_r) / n_r,
+ * scaled so the largest configuration amplitude is 1; out holds D doubles.
+ * Pass it to sed_eigh as SED_START_GIVEN. */
+SED_API int sed_mlp_start_vector(sed_mlp* mlp, ls_spin_basis const* basis, double* out);
+
 /* Number of libsed kernels launched by this process so far (graph replays
  * count their kernel nodes). */
 SED_API uint64_t sed_kernel_launches(void);

@@ -202,53 +202,59 @@ SED_HD W rotr_n(W v, unsigned r, unsigned n, W mask) {
   return r ? (W)(((v >> r) | (v << (n - r))) & mask) : v;
 }
 
-// Rows of y (row k = bits [k B, (k+1) B)) and, per row and orientation, the
-// smallest rotation; returns the smallest top row over all H-images of y
-// (and ~y).
+// Row j (0 = top) of the candidate image that takes source row k of y to the
+// top with rotation r; rows come from y (and ~y when inv).
 template <class W>
-SED_HD uint32_t rows_scan(W y, PlanView const& P, RowTab const& T, uint32_t (&rv)[SED_MAX_ROWS]) {
+SED_HD uint32_t cand_row(W y, PlanView const& P, uint32_t k, uint32_t j, uint32_t r, uint32_t invm) {
+  uint32_t const src = k >= j ? k - j : k + P.n_rows - j;
+  uint32_t const B = P.row_bits, rm = (uint32_t)P.row_mask;
+  uint32_t const v = ((uint32_t)(y >> (src * B)) & rm) ^ invm;
+  return r ? (((v << r) | (v >> (B - r))) & rm) : v;
+}
+
+// Lexicographic comparison, from the top row down, of the candidate image
+// (source row k of y at the top, rotation r) with the word ref; rows 0..j0-1
+// are known to be equal. Returns -1, 0 or +1.
+template <class W>
+SED_HD int cand_compare(W y, PlanView const& P, uint32_t k, uint32_t r, uint32_t invm, W ref, uint32_t j0) {
+  uint32_t const B = P.row_bits, rm = (uint32_t)P.row_mask, R = P.n_rows;
+  for (uint32_t j = j0; j < R; ++j) {
+    uint32_t const a = cand_row<W>(y, P, k, j, r, invm);
+    uint32_t const b = (uint32_t)(ref >> ((R - 1 - j) * B)) & rm;
+    if (a != b) return a < b ? -1 : 1;
+  }
+  return 0;
+}
+
+// Full image for candidate (source row k to the top, rotation r, orientation).
+template <class W>
+SED_HD W cand_image(W y, W mask, PlanView const& P, uint32_t k, uint32_t r, uint32_t inv) {
+  uint32_t const t = k + 1 == P.n_rows ? 0u : k + 1;
+  W const yy = inv ? (W)(~y & mask) : y;
+  W z = apply2<W>(yy, P.rot_mask[2 * r], P.rot_mask[2 * r + 1], P.rot_rot[2 * r], P.rot_rot[2 * r + 1]);
+  return apply2<W>(z, P.sh_mask[2 * t], P.sh_mask[2 * t + 1], P.sh_rot[2 * t], P.sh_rot[2 * t + 1]);
+}
+
+// Smallest top row over the rows (and inverted rows) of y.
+template <class W>
+SED_HD uint32_t rows_min_top(W y, PlanView const& P, RowTab const& T) {
   uint32_t best = 0xFFFFFFFFu;
   uint32_t const rm = (uint32_t)P.row_mask;
   W v = y;
 #pragma unroll
   for (uint32_t k = 0; k < SED_MAX_ROWS; ++k) {
     if (k < P.n_rows) {
-      rv[k] = (uint32_t)v & rm;
+      uint32_t const row = (uint32_t)v & rm;
       v >>= P.row_bits;
-      uint32_t const a = T.min[rv[k]];
+      uint32_t const a = T.min[row];
       best = a < best ? a : best;
       if (P.inv) {
-        uint32_t const b = T.min[rv[k] ^ rm];
+        uint32_t const b = T.min[row ^ rm];
         best = b < best ? b : best;
       }
     }
   }
   return best;
-}
-
-template <class W, class F>
-SED_HD bool rows_top_each(W y, W mask, PlanView const& P, RowTab const& T, uint32_t top,
-                          uint32_t const (&rv)[SED_MAX_ROWS], F&& f) {
-  uint32_t const rm = (uint32_t)P.row_mask;
-#pragma unroll
-  for (uint32_t k = 0; k < SED_MAX_ROWS; ++k) {
-    if (k >= P.n_rows) break;
-    uint32_t const t = k + 1 == P.n_rows ? 0u : k + 1;  // the image's top row comes from row k
-    for (uint32_t inv = 0; inv <= (P.inv ? 1u : 0u); ++inv) {
-      uint32_t const v = inv ? (rv[k] ^ rm) : rv[k];
-      if (T.min[v] != top) continue;
-      W const yy = inv ? (W)(~y & mask) : y;
-      uint32_t set = T.set[v];
-      while (set) {
-        uint32_t const r = (uint32_t)__builtin_ctz_sed(set);
-        set &= set - 1;
-        W z = apply2<W>(yy, P.rot_mask[2 * r], P.rot_mask[2 * r + 1], P.rot_rot[2 * r], P.rot_rot[2 * r + 1]);
-        z = apply2<W>(z, P.sh_mask[2 * t], P.sh_mask[2 * t + 1], P.sh_rot[2 * t], P.sh_rot[2 * t + 1]);
-        if (!f(z, r, t, inv)) return false;
-      }
-    }
-  }
-  return true;
 }
 
 // Single row of n bits (chains): rotations of v that bring a longest circular
@@ -344,31 +350,76 @@ template <class W, class Img>
 SED_HD Canon<W> canonicalize_img(W x, PlanView const& P, RowTab const& T, Img&& img) {
   W best = x;
   W const mask = (W)P.mask;
-  if (P.rows) {
+  if (P.rows == 1) {
+    // Per coset: the smallest top row any rotation/shift can reach (from the
+    // row tables); cosets that cannot beat the best image's top row are
+    // skipped, the others build every image with that top row in full.
+    uint32_t const rm = (uint32_t)P.row_mask;
+    uint32_t const top_shift = (P.n_rows - 1) * P.row_bits;
     uint32_t bc = 0, br = 0, bt = 0, binv = 0;
     for (uint32_t c = 0; c < P.n_cosets; ++c) {
       W const y = img(c);
-      auto take = [&](W z, uint32_t r, uint32_t t, uint32_t inv) {
-        if (z < best) {
-          best = z;
-          bc = c;
-          br = r;
-          bt = t;
-          binv = inv;
+      uint32_t rv[SED_MAX_ROWS];
+      uint32_t top = 0xFFFFFFFFu;
+      {
+        W v = y;
+#pragma unroll
+        for (uint32_t k = 0; k < SED_MAX_ROWS; ++k) {
+          if (k < P.n_rows) {
+            rv[k] = (uint32_t)v & rm;
+            v >>= P.row_bits;
+            uint32_t const a = T.min[rv[k]];
+            top = a < top ? a : top;
+            if (P.inv) {
+              uint32_t const b = T.min[rv[k] ^ rm];
+              top = b < top ? b : top;
+            }
+          }
         }
-        return true;
-      };
-      if (P.rows == 1) {
-        uint32_t rv[SED_MAX_ROWS];
-        uint32_t const top = rows_scan<W>(y, P, T, rv);
-        if (top > (uint32_t)(best >> ((P.n_rows - 1) * P.row_bits))) continue;
-        rows_top_each<W>(y, mask, P, T, top, rv, take);
-      } else {
-        chain_each<W>(y, mask, P, take);
+      }
+      if (top > (uint32_t)(best >> top_shift)) continue;
+#pragma unroll
+      for (uint32_t k = 0; k < SED_MAX_ROWS; ++k) {
+        if (k >= P.n_rows) break;
+        for (uint32_t inv = 0; inv <= (P.inv ? 1u : 0u); ++inv) {
+          uint32_t const v = inv ? (rv[k] ^ rm) : rv[k];
+          if (T.min[v] != top) continue;
+          uint32_t set = T.set[v];
+          while (set) {
+            uint32_t const r = (uint32_t)__builtin_ctz_sed(set);
+            set &= set - 1;
+            W const z = cand_image<W>(y, mask, P, k, r, inv);
+            if (z < best) {
+              best = z;
+              bc = c;
+              br = r;
+              bt = k + 1 == P.n_rows ? 0u : k + 1;
+              binv = inv;
+            }
+          }
+        }
       }
     }
     uint64_t ph = (uint64_t)P.coset_phase[bc] + (uint64_t)P.rot_exp[br] * P.rot_phase +
                   (uint64_t)P.sh_exp[bt] * P.shift_phase;
+    if (binv) ph += P.inv_phase;
+    return {best, (uint32_t)(ph % P.L)};
+  }
+  if (P.rows == 2) {
+    uint32_t bc = 0, br = 0, binv = 0;
+    for (uint32_t c = 0; c < P.n_cosets; ++c) {
+      auto take = [&](W z, uint32_t r, uint32_t, uint32_t inv) {
+        if (z < best) {
+          best = z;
+          bc = c;
+          br = r;
+          binv = inv;
+        }
+        return true;
+      };
+      chain_each<W>(img(c), mask, P, take);
+    }
+    uint64_t ph = (uint64_t)P.coset_phase[bc] + (uint64_t)P.rot_exp[br] * P.rot_phase;
     if (binv) ph += P.inv_phase;
     return {best, (uint32_t)(ph % P.L)};
   }
@@ -437,18 +488,48 @@ template <class W>
 SED_HD uint32_t representative_weight(W x, PlanView const& P, RowTab const& T) {
   uint32_t S = 0;
   W const mask = (W)P.mask;
-  if (P.rows) {
+  if (P.rows == 1) {
+    uint32_t const rm = (uint32_t)P.row_mask;
+    uint32_t const xt = (uint32_t)(x >> ((P.n_rows - 1) * P.row_bits));
+    for (uint32_t c = 0; c < P.n_cosets; ++c)  // pass A with early rejection
+      if (rows_min_top<W>(coset_apply<W>(x, P, c), P, T) < xt) return 0;
+    for (uint32_t c = 0; c < P.n_cosets; ++c) {  // pass B: images whose top row equals x's
+      W const y = coset_apply<W>(x, P, c);
+      for (uint32_t k = 0; k < P.n_rows; ++k) {
+        uint32_t const row = (uint32_t)(y >> (k * P.row_bits)) & rm;
+        for (uint32_t inv = 0; inv <= (P.inv ? 1u : 0u); ++inv) {
+          uint32_t const v = inv ? (row ^ rm) : row;
+          if (T.min[v] != xt) continue;
+          uint32_t set = T.set[v];
+          while (set) {
+            uint32_t const r = (uint32_t)__builtin_ctz_sed(set);
+            set &= set - 1;
+            int const cmp = cand_compare<W>(y, P, k, r, inv ? rm : 0u, x, 1);
+            if (cmp < 0) return 0;
+            if (cmp == 0) {
+              uint32_t const t = k + 1 == P.n_rows ? 0u : k + 1;
+              uint64_t ph = (uint64_t)P.coset_phase[c] + (uint64_t)P.rot_exp[r] * P.rot_phase +
+                            (uint64_t)P.sh_exp[t] * P.shift_phase + (inv ? P.inv_phase : 0u);
+              if (ph % P.L != 0) return 0;
+              ++S;
+            }
+          }
+        }
+      }
+    }
+    return S;
+  }
+  if (P.rows == 2) {
     bool reject = false;
     for (uint32_t c = 0; c < P.n_cosets && !reject; ++c) {
-      W const y = coset_apply<W>(x, P, c);
-      auto visit = [&](W z, uint32_t r, uint32_t t, uint32_t inv) {
+      auto visit = [&](W z, uint32_t r, uint32_t, uint32_t inv) {
         if (z < x) {
           reject = true;
           return false;
         }
         if (z == x) {
           uint64_t ph = (uint64_t)P.coset_phase[c] + (uint64_t)P.rot_exp[r] * P.rot_phase +
-                        (uint64_t)P.sh_exp[t] * P.shift_phase + (inv ? P.inv_phase : 0u);
+                        (inv ? P.inv_phase : 0u);
           if (ph % P.L != 0) {
             reject = true;
             return false;
@@ -457,16 +538,7 @@ SED_HD uint32_t representative_weight(W x, PlanView const& P, RowTab const& T) {
         }
         return true;
       };
-      if (P.rows == 1) {
-        uint32_t rv[SED_MAX_ROWS];
-        uint32_t const top = rows_scan<W>(y, P, T, rv);
-        uint32_t const xt = (uint32_t)(x >> ((P.n_rows - 1) * P.row_bits));
-        if (top < xt) return 0;
-        if (top > xt) continue;
-        rows_top_each<W>(y, mask, P, T, top, rv, visit);
-      } else {
-        chain_each<W>(y, mask, P, visit);
-      }
+      chain_each<W>(coset_apply<W>(x, P, c), mask, P, visit);
     }
     return reject ? 0 : S;
   }

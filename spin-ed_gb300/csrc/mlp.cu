@@ -1,0 +1,670 @@
+// mlp.cu — the learned start vector: a small MLP over spin configurations,
+// trained and evaluated on the GPU by the kernels in this file.
+//
+// Network (n inputs -> h -> h -> 2), x_j = +1 / -1 for spin j up / down:
+//   h1 = tanh(W1 x + b1), h2 = tanh(W2 h1 + b2), (a, s) = W3 h2 + b3.
+// a models log|psi(x)|, s the logit of "sign psi(x) = prior(x)", with the
+// sign prior (-1)^popcount(x & sign_mask) (a Marshall-type sublattice rule
+// for bipartite lattices; sign_mask = 0 means no prior). Weights are kept as
+// an FP32 master copy for Adam and used in BF16 (round to nearest even) by the
+// forward and backward passes; products accumulate in FP32.
+//
+// The symmetric-basis amplitude of representative r relates to the amplitude
+// of the configuration itself by psi(r) = c_r * n_r, n_r = ||P r|| =
+// sqrt(S_r / |G|) (every orbit member carries |c_r n_r|). Training labels are
+// log|c_r n_r| and sign(c_r) for representatives drawn with probability
+// |c_r|^2 from ground states the solver computed at neighbouring couplings;
+// the start vector is v_r = prior(r) sign(s) exp(a) / n_r.
+//
+// GEMMs here are SIMT tiles (64 x 64 outputs per 256-thread block, 16-deep K
+// steps through shared memory, 4 x 4 outputs per thread) with arbitrary
+// strides, so one kernel serves every product of the forward and backward
+// passes.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <type_traits>
+
+#include "sed_internal.hpp"
+#include "util.cuh"
+
+namespace sed {
+namespace {
+
+constexpr int kTile = 64, kTK = 16;
+
+// C[m][n] (=|+=) act(sum_k A(m,k) B(k,n) + bias[n]) with arbitrary strides;
+// A is FP32, B is TB (float or bf16). act: 0 none, 1 tanh.
+template <class TB>
+__global__ void __launch_bounds__(256)
+    k_gemm(int M, int N, int K, float const* __restrict__ A, int64_t sam, int64_t sak,
+           TB const* __restrict__ B, int64_t sbk, int64_t sbn, float* __restrict__ C, int64_t ldc,
+           float const* __restrict__ bias, int act, int accumulate) {
+  __shared__ float As[kTK][kTile + 1];
+  __shared__ float Bs[kTK][kTile + 1];
+  int const tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  int const m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
+  // loads run along whichever of (m, k) has unit stride, for coalescing
+  bool const a_k_fast = sak == 1, b_n_fast = sbn == 1;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += kTK) {
+    for (int q = threadIdx.x; q < kTK * kTile; q += 256) {
+      int const kk = a_k_fast ? q % kTK : q / kTile, mm = a_k_fast ? q / kTK : q % kTile;
+      int const gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < M && gk < K) ? A[gm * sam + gk * sak] : 0.0f;
+    }
+    for (int q = threadIdx.x; q < kTK * kTile; q += 256) {
+      int const kk = b_n_fast ? q / kTile : q % kTK, nn = b_n_fast ? q % kTile : q / kTK;
+      int const gn = n0 + nn, gk = k0 + kk;
+      float bv = 0.0f;
+      if (gn < N && gk < K) {
+        if constexpr (std::is_same<TB, float>::value)
+          bv = B[gk * sbk + gn * sbn];
+        else
+          bv = __bfloat162float(B[gk * sbk + gn * sbn]);
+      }
+      Bs[kk][nn] = bv;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kTK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        a[i] = As[kk][ty * 4 + i];
+        b[i] = Bs[kk][tx * 4 + i];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int const gm = m0 + ty * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int const gn = n0 + tx * 4 + j;
+      if (gn >= N) continue;
+      float v = acc[i][j];
+      if (bias) v += bias[gn];
+      if (act == 1) v = tanhf(v);
+      float* c = C + (int64_t)gm * ldc + gn;
+      *c = accumulate ? *c + v : v;
+    }
+  }
+}
+
+// x[b][j] = +1 / -1 from the bits of states[b].
+__global__ void k_spins(uint64_t const* __restrict__ states, int64_t n, int bits, float* __restrict__ x) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n * bits;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int64_t const b = q / bits;
+    int const j = (int)(q % bits);
+    x[q] = ((states[b] >> j) & 1u) ? 1.0f : -1.0f;
+  }
+}
+
+__device__ __forceinline__ float prior_flip(uint64_t state, uint64_t mask) {
+  return (__popcll(state & mask) & 1) ? 1.0f : 0.0f;
+}
+
+// Output gradient of L = mean_b [(a_b - t_b)^2 + BCE(s_b, y_b)] with
+// y_b = [sign psi_b == prior(state_b)], and the loss partials.
+__global__ void k_out_grad(float const* __restrict__ out, uint64_t const* __restrict__ states, uint64_t sign_mask,
+                           float const* __restrict__ t_abs, float const* __restrict__ t_sign, int64_t n,
+                           float* __restrict__ dout, double* __restrict__ loss_partial) {
+  __shared__ double red[32];
+  double l = 0.0;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < n;
+       b += (int64_t)gridDim.x * blockDim.x) {
+    float const a = out[2 * b], s = out[2 * b + 1];
+    float const da = a - t_abs[b];
+    float const y = fabsf(t_sign[b] - prior_flip(states[b], sign_mask));
+    float const p = 1.0f / (1.0f + expf(-s));
+    dout[2 * b] = 2.0f * da / (float)n;
+    dout[2 * b + 1] = (p - y) / (float)n;
+    // BCE with logits in its stable form: max(s, 0) - s y + log(1 + e^-|s|)
+    l += (double)da * da + (double)(fmaxf(s, 0.0f) - s * y + log1pf(expf(-fabsf(s))));
+  }
+  double const tot = block_sum(l, red);
+  if (threadIdx.x == 0) loss_partial[blockIdx.x] = tot;
+}
+
+// g *= 1 - h^2 (tanh derivative, in place on the gradient)
+__global__ void k_tanh_back(float const* __restrict__ h, float* __restrict__ g, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    g[q] *= 1.0f - h[q] * h[q];
+}
+
+// db[j] += sum over rows b = blockIdx.y (mod gridDim.y) of g[b][j]; db must
+// be zeroed first.
+__global__ void k_colsum(float const* __restrict__ g, int64_t rows, int cols, float* __restrict__ db) {
+  int const j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cols) return;
+  float s = 0.0f;
+  for (int64_t b = blockIdx.y; b < rows; b += gridDim.y) s += g[b * cols + j];
+  atomicAdd(db + j, s);
+}
+
+__global__ void k_adam(float* __restrict__ p, float const* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, __nv_bfloat16* __restrict__ pb, int64_t n, float lr, float c1,
+                       float c2) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    float const gq = g[q];
+    float const mq = 0.9f * m[q] + 0.1f * gq;
+    float const vq = 0.999f * v[q] + 0.001f * gq * gq;
+    m[q] = mq;
+    v[q] = vq;
+    float const pq = p[q] - lr * (mq * c1) / (sqrtf(vq * c2) + 1e-8f);
+    p[q] = pq;
+    pb[q] = __float2bfloat16(pq);
+  }
+}
+
+__global__ void k_to_bf16(float const* __restrict__ p, __nv_bfloat16* __restrict__ pb, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    pb[q] = __float2bfloat16(p[q]);
+}
+
+// v_r = prior(r) sign(s) exp(a - a_max) / n_r, n_r = sqrt(S_r / |G|)
+__global__ void k_start_from_net(float const* __restrict__ out, uint64_t const* __restrict__ reps,
+                                 uint32_t const* __restrict__ weights, int64_t n, uint64_t sign_mask,
+                                 float a_max, double group_order, double* __restrict__ v) {
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += (int64_t)gridDim.x * blockDim.x) {
+    float const a = out[2 * b], s = out[2 * b + 1];
+    double const amp = exp((double)(a - a_max)) * sqrt(group_order / (double)weights[b]);
+    bool const neg = (s < 0.0f) != (prior_flip(reps[b], sign_mask) != 0.0f);
+    v[b] = neg ? -amp : amp;
+  }
+}
+
+__global__ void k_max_first(float const* __restrict__ out, int64_t n, float* __restrict__ part) {
+  __shared__ float red[256];
+  float m = -3.0e38f;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, out[2 * b]);
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// ------------------------------------------------------------- sampling ---
+constexpr int kChunk = 4096;  // elements per block of the prefix sum (256 threads x 16)
+
+__global__ void k_chunk_sums(double const* __restrict__ psi, uint64_t D, double* __restrict__ sums) {
+  __shared__ double red[32];
+  uint64_t const base = (uint64_t)blockIdx.x * kChunk;
+  double s = 0.0;
+  for (int q = threadIdx.x; q < kChunk; q += blockDim.x) {
+    uint64_t const i = base + q;
+    if (i < D) s += psi[i] * psi[i];
+  }
+  double const t = block_sum(s, red);
+  if (threadIdx.x == 0) sums[blockIdx.x] = t;
+}
+
+// prefix[i] = offset[chunk] + sum_{j <= i in chunk} psi_j^2
+__global__ void __launch_bounds__(256) k_chunk_prefix(double const* __restrict__ psi, uint64_t D,
+                                                       double const* __restrict__ offset,
+                                                       double* __restrict__ prefix) {
+  __shared__ double part[256];
+  uint64_t const base = (uint64_t)blockIdx.x * kChunk + threadIdx.x * 16;
+  double v[16];
+  double run = 0.0;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    uint64_t const i = base + q;
+    double const p = i < D ? psi[i] : 0.0;
+    run += p * p;
+    v[q] = run;
+  }
+  part[threadIdx.x] = run;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {  // Hillis-Steele inclusive scan of the thread totals
+    double const t = (int)threadIdx.x >= o ? part[threadIdx.x - o] : 0.0;
+    __syncthreads();
+    part[threadIdx.x] += t;
+    __syncthreads();
+  }
+  double const before = offset[blockIdx.x] + (threadIdx.x ? part[threadIdx.x - 1] : 0.0);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    uint64_t const i = base + q;
+    if (i < D) prefix[i] = before + v[q];
+  }
+}
+
+// Sample q: u = total * U[0,1) from Philox block (q, seed); its index is the
+// smallest i with prefix[i] > u.
+__global__ void k_draw(double const* __restrict__ prefix, uint64_t D, double total, uint64_t n, uint64_t seed,
+                       double const* __restrict__ psi, uint64_t const* __restrict__ reps,
+                       uint32_t const* __restrict__ weights, double group_order, uint64_t* __restrict__ states,
+                       float* __restrict__ t_abs, float* __restrict__ t_sign) {
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t c[4] = {(uint32_t)q, (uint32_t)(q >> 32), 0x5EEDu, 0u};
+    philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    double const u = u01_53(c[0], c[1]) * total;
+    uint64_t lo = 0, hi = D - 1;
+    while (lo < hi) {
+      uint64_t const mid = lo + (hi - lo) / 2;
+      if (prefix[mid] > u)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    double const p = psi[lo];
+    states[q] = reps[lo];
+    t_abs[q] = (float)(log(fabs(p)) + 0.5 * log((double)weights[lo] / group_order));
+    t_sign[q] = p > 0.0 ? 1.0f : 0.0f;
+  }
+}
+
+unsigned blocks_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+}  // namespace
+
+struct MlpData {
+  int device = -1;
+  unsigned n_in = 0, hidden = 0;
+  uint64_t sign_mask = 0;
+  uint64_t n_params = 0;
+  uint64_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0;  // offsets into the parameter blob
+  DeviceBuffer p, pb, g, m, v;  // FP32 master, BF16 copy, gradient, Adam moments
+  uint64_t step = 0;
+  cudaStream_t stream = nullptr;
+  DeviceBuffer x, h1, h2, out, d2, d1, dout, loss_part;  // activations of one batch
+  uint64_t cap = 0, cap_train = 0;
+  ~MlpData() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+template <class TB>
+void gemm(cudaStream_t s, int M, int N, int K, float const* A, int64_t sam, int64_t sak, TB const* B, int64_t sbk,
+          int64_t sbn, float* C, int64_t ldc, float const* bias, int act, int accumulate) {
+  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
+  { k_gemm<TB><<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, act, accumulate); note_launches(1); }
+}
+
+int ensure_batch(MlpData& d, uint64_t n, bool train) {
+  uint64_t const h = d.hidden;
+  if (n > d.cap) {
+    d.cap = 0;
+    if (int st = d.x.allocate(n * d.n_in * 4)) return st;
+    if (int st = d.h1.allocate(n * h * 4)) return st;
+    if (int st = d.h2.allocate(n * h * 4)) return st;
+    if (int st = d.out.allocate(n * 2 * 4)) return st;
+    if (int st = d.loss_part.allocate(152 * 16 * 8)) return st;
+    d.cap = n;
+  }
+  if (train && n > d.cap_train) {
+    d.cap_train = 0;
+    if (int st = d.d2.allocate(n * h * 4)) return st;
+    if (int st = d.d1.allocate(n * h * 4)) return st;
+    if (int st = d.dout.allocate(n * 2 * 4)) return st;
+    d.cap_train = n;
+  }
+  return LS_SUCCESS;
+}
+
+// forward pass for states[0..n) (device pointer); activations stay in d.x/h1/h2/out
+int forward(MlpData& d, uint64_t const* states, uint64_t n, bool train) {
+  if (int st = ensure_batch(d, n, train)) return st;
+  cudaStream_t s = d.stream;
+  int const N = (int)n, H = (int)d.hidden, I = (int)d.n_in;
+  __nv_bfloat16 const* W = d.pb.as<__nv_bfloat16>();
+  float const* P = d.p.as<float>();
+  { k_spins<<<blocks_for((int64_t)n * I), 256, 0, s>>>(states, (int64_t)n, I, d.x.as<float>()); note_launches(1); }
+  // h1 [N x H] = tanh(x W1^T + b1): B(k, n) = W1[n][k]
+  gemm<__nv_bfloat16>(s, N, H, I, d.x.as<float>(), I, 1, W + d.oW1, 1, I, d.h1.as<float>(), H, P + d.ob1, 1, 0);
+  gemm<__nv_bfloat16>(s, N, H, H, d.h1.as<float>(), H, 1, W + d.oW2, 1, H, d.h2.as<float>(), H, P + d.ob2, 1, 0);
+  gemm<__nv_bfloat16>(s, N, 2, H, d.h2.as<float>(), H, 1, W + d.oW3, 1, H, d.out.as<float>(), 2, P + d.ob3, 0, 0);
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
+// loss and gradient (into d.g) of one batch after forward(..., train = true)
+int backward(MlpData& d, uint64_t const* states, uint64_t n, float const* t_abs, float const* t_sign,
+             double* loss) {
+  cudaStream_t s = d.stream;
+  int const N = (int)n, H = (int)d.hidden, I = (int)d.n_in;
+  __nv_bfloat16 const* W = d.pb.as<__nv_bfloat16>();
+  float* G = d.g.as<float>();
+  unsigned const lb = blocks_for((int64_t)n);
+  SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, s));
+  { k_out_grad<<<lb, 256, 0, s>>>(d.out.as<float>(), states, d.sign_mask, t_abs, t_sign, (int64_t)n, d.dout.as<float>(), d.loss_part.as<double>()); note_launches(1); }
+  unsigned const ry = (unsigned)std::min<int64_t>(512, std::max<int64_t>(1, (int64_t)n / 64));
+  // dW3 [2 x H] = dout^T h2 ; db3 = colsum(dout)
+  gemm<float>(s, 2, H, N, d.dout.as<float>(), 1, 2, d.h2.as<float>(), H, 1, G + d.oW3, H, nullptr, 0, 0);
+  { k_colsum<<<dim3(1, ry), 32, 0, s>>>(d.dout.as<float>(), (int64_t)n, 2, G + d.ob3); note_launches(1); }
+  // dh2 [N x H] = dout W3, times tanh'
+  gemm<__nv_bfloat16>(s, N, H, 2, d.dout.as<float>(), 2, 1, W + d.oW3, H, 1, d.d2.as<float>(), H, nullptr, 0, 0);
+  { k_tanh_back<<<blocks_for((int64_t)n * H), 256, 0, s>>>(d.h2.as<float>(), d.d2.as<float>(), (int64_t)n * H); note_launches(1); }
+  // dW2 [H x H] = dh2^T h1 ; db2
+  gemm<float>(s, H, H, N, d.d2.as<float>(), 1, H, d.h1.as<float>(), H, 1, G + d.oW2, H, nullptr, 0, 0);
+  { k_colsum<<<dim3((H + 255) / 256, ry), 256, 0, s>>>(d.d2.as<float>(), (int64_t)n, H, G + d.ob2); note_launches(1); }
+  // dh1 [N x H] = dh2 W2, times tanh'
+  gemm<__nv_bfloat16>(s, N, H, H, d.d2.as<float>(), H, 1, W + d.oW2, H, 1, d.d1.as<float>(), H, nullptr, 0, 0);
+  { k_tanh_back<<<blocks_for((int64_t)n * H), 256, 0, s>>>(d.h1.as<float>(), d.d1.as<float>(), (int64_t)n * H); note_launches(1); }
+  // dW1 [H x I] = dh1^T x ; db1
+  gemm<float>(s, H, I, N, d.d1.as<float>(), 1, H, d.x.as<float>(), I, 1, G + d.oW1, I, nullptr, 0, 0);
+  { k_colsum<<<dim3((H + 255) / 256, ry), 256, 0, s>>>(d.d1.as<float>(), (int64_t)n, H, G + d.ob1); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  if (loss) {
+    std::vector<double> lp(lb);
+    SED_TRY_CUDA(cudaMemcpyAsync(lp.data(), d.loss_part.ptr, lb * 8, cudaMemcpyDeviceToHost, s));
+    SED_TRY_CUDA(cudaStreamSynchronize(s));
+    double t = 0.0;
+    for (double q : lp) t += q;
+    *loss = t / (double)n;
+  }
+  return LS_SUCCESS;
+}
+
+int refresh_bf16(MlpData& d) {
+  { k_to_bf16<<<blocks_for((int64_t)d.n_params), 256, 0, d.stream>>>(d.p.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
+// device copy of a host-or-device array
+int stage(DeviceBuffer& buf, void const* src, size_t bytes, cudaStream_t s) {
+  if (int st = buf.allocate(std::max<size_t>(bytes, 16))) return st;
+  SED_TRY_CUDA(cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyDefault, s));
+  return LS_SUCCESS;
+}
+
+}  // namespace
+}  // namespace sed
+
+struct sed_mlp {
+  sed::MlpData d;
+};
+
+using namespace sed;
+
+extern "C" {
+
+int sed_mlp_create(sed_mlp** out, unsigned n_inputs, unsigned hidden, uint64_t sign_mask, uint64_t seed) {
+  if (!out) return fail(LS_INVALID_ARGUMENT, "sed_mlp_create: NULL argument");
+  *out = nullptr;
+  if (n_inputs == 0 || n_inputs > 64 || hidden == 0 || hidden > 4096)
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_create: n_inputs must be 1..64 and hidden 1..4096");
+  if (n_inputs < 64 && (sign_mask >> n_inputs) != 0)
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_create: sign_mask has bits beyond n_inputs");
+  auto* m = new (std::nothrow) sed_mlp;
+  if (!m) return fail(LS_OUT_OF_MEMORY, "sed_mlp_create");
+  MlpData& d = m->d;
+  if (int st = current_device(&d.device)) {
+    delete m;
+    return st;
+  }
+  d.n_in = n_inputs;
+  d.hidden = hidden;
+  d.sign_mask = sign_mask;
+  uint64_t const I = n_inputs, H = hidden;
+  d.oW1 = 0;
+  d.ob1 = d.oW1 + H * I;
+  d.oW2 = d.ob1 + H;
+  d.ob2 = d.oW2 + H * H;
+  d.oW3 = d.ob2 + H;
+  d.ob3 = d.oW3 + 2 * H;
+  d.n_params = d.ob3 + 2;
+  // Gaussian init with variance 1/fan_in, biases zero (host mt19937_64, so a
+  // seed gives the same network on every machine)
+  std::vector<float> host(d.n_params, 0.0f);
+  std::mt19937_64 rng(seed);
+  auto init = [&](uint64_t off, uint64_t count, uint64_t fan_in) {
+    std::normal_distribution<double> nd(0.0, 1.0 / std::sqrt((double)fan_in));
+    for (uint64_t q = 0; q < count; ++q) host[off + q] = (float)nd(rng);
+  };
+  init(d.oW1, H * I, I);
+  init(d.oW2, H * H, H);
+  init(d.oW3, 2 * H, H);
+  int st = LS_SUCCESS;
+  if (cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    d.stream = nullptr;
+    st = fail(LS_CUDA_ERROR, "sed_mlp_create: cudaStreamCreate");
+  }
+  if (!st) st = d.p.allocate(d.n_params * 4);
+  if (!st) st = d.pb.allocate(d.n_params * 2);
+  if (!st) st = d.g.allocate(d.n_params * 4);
+  if (!st) st = d.m.allocate(d.n_params * 4);
+  if (!st) st = d.v.allocate(d.n_params * 4);
+  if (!st && cudaMemcpy(d.p.ptr, host.data(), d.n_params * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+    st = fail(LS_CUDA_ERROR, "sed_mlp_create: upload");
+  if (!st && (cudaMemset(d.m.ptr, 0, d.n_params * 4) != cudaSuccess ||
+              cudaMemset(d.v.ptr, 0, d.n_params * 4) != cudaSuccess))
+    st = fail(LS_CUDA_ERROR, "sed_mlp_create: cudaMemset");
+  if (!st) st = refresh_bf16(d);
+  if (!st && cudaStreamSynchronize(d.stream) != cudaSuccess)
+    st = fail(LS_CUDA_ERROR, "sed_mlp_create: initialisation");
+  if (st) {
+    delete m;
+    return st;
+  }
+  *out = m;
+  return LS_SUCCESS;
+}
+
+void sed_mlp_destroy(sed_mlp* m) {
+  if (!m) return;
+  ScopedDevice dev(m->d.device);
+  delete m;
+}
+
+uint64_t sed_mlp_num_params(sed_mlp const* m) { return m ? m->d.n_params : 0; }
+
+int sed_mlp_get_params(sed_mlp const* m, float* out) {
+  if (!m || !out) return fail(LS_INVALID_ARGUMENT, "sed_mlp_get_params: NULL argument");
+  ScopedDevice dev(m->d.device);
+  SED_TRY_CUDA(cudaMemcpy(out, m->d.p.ptr, m->d.n_params * 4, cudaMemcpyDefault));
+  return LS_SUCCESS;
+}
+
+int sed_mlp_set_params(sed_mlp* m, float const* in) {
+  if (!m || !in) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_params: NULL argument");
+  MlpData& d = m->d;
+  ScopedDevice dev(d.device);
+  SED_TRY_CUDA(cudaMemcpy(d.p.ptr, in, d.n_params * 4, cudaMemcpyDefault));
+  if (int st = refresh_bf16(d)) return st;
+  SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
+  return LS_SUCCESS;
+}
+
+int sed_mlp_forward(sed_mlp* m, uint64_t const* states, uint64_t n, float* out) {
+  if (!m || (n && (!states || !out))) return fail(LS_INVALID_ARGUMENT, "sed_mlp_forward: NULL argument");
+  MlpData& d = m->d;
+  ScopedDevice dev(d.device);
+  uint64_t const chunk = 1u << 18;
+  DeviceBuffer sbuf;
+  if (n)
+    if (int st = sbuf.allocate(std::min(chunk, n) * 8)) return st;
+  for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
+    uint64_t const nb = std::min(chunk, n - b0);
+    SED_TRY_CUDA(cudaMemcpyAsync(sbuf.ptr, states + b0, nb * 8, cudaMemcpyDefault, d.stream));
+    if (int st = forward(d, sbuf.as<uint64_t>(), nb, false)) return st;
+    SED_TRY_CUDA(cudaMemcpyAsync(out + 2 * b0, d.out.ptr, nb * 8, cudaMemcpyDefault, d.stream));
+  }
+  SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
+  return LS_SUCCESS;
+}
+
+int sed_mlp_loss_grad(sed_mlp* m, uint64_t const* states, float const* t_abs, float const* t_sign, uint64_t n,
+                      double* loss, float* grads) {
+  if (!m || !n || !states || !t_abs || !t_sign) return fail(LS_INVALID_ARGUMENT, "sed_mlp_loss_grad: bad argument");
+  if (n > (1u << 20)) return fail(LS_INVALID_ARGUMENT, "sed_mlp_loss_grad: at most 2^20 samples per call");
+  MlpData& d = m->d;
+  ScopedDevice dev(d.device);
+  DeviceBuffer sb, ta, ts;
+  if (int st = stage(sb, states, n * 8, d.stream)) return st;
+  if (int st = stage(ta, t_abs, n * 4, d.stream)) return st;
+  if (int st = stage(ts, t_sign, n * 4, d.stream)) return st;
+  if (int st = forward(d, sb.as<uint64_t>(), n, true)) return st;
+  if (int st = backward(d, sb.as<uint64_t>(), n, ta.as<float>(), ts.as<float>(), loss)) return st;
+  if (grads) SED_TRY_CUDA(cudaMemcpyAsync(grads, d.g.ptr, d.n_params * 4, cudaMemcpyDefault, d.stream));
+  SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
+  return LS_SUCCESS;
+}
+
+int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float const* t_sign, uint64_t n,
+                  unsigned epochs, unsigned batch, float lr, uint64_t seed, double* final_loss) {
+  if (!m || !n || !states || !t_abs || !t_sign || !batch || !(lr > 0.0f))
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_train: bad argument");
+  if (batch > (1u << 20)) return fail(LS_INVALID_ARGUMENT, "sed_mlp_train: batch must be <= 2^20");
+  MlpData& d = m->d;
+  ScopedDevice dev(d.device);
+  // the data set is shuffled on the host once per epoch (an index permutation
+  // from mt19937_64(seed)) and uploaded; batches are contiguous slices of it
+  std::vector<uint64_t> hs(n);
+  std::vector<float> ha(n), hg(n);
+  SED_TRY_CUDA(cudaMemcpy(hs.data(), states, n * 8, cudaMemcpyDefault));
+  SED_TRY_CUDA(cudaMemcpy(ha.data(), t_abs, n * 4, cudaMemcpyDefault));
+  SED_TRY_CUDA(cudaMemcpy(hg.data(), t_sign, n * 4, cudaMemcpyDefault));
+  DeviceBuffer sb, ta, ts;
+  if (int st = sb.allocate(n * 8)) return st;
+  if (int st = ta.allocate(n * 4)) return st;
+  if (int st = ts.allocate(n * 4)) return st;
+  std::vector<uint64_t> order(n);
+  for (uint64_t q = 0; q < n; ++q) order[q] = q;
+  std::mt19937_64 rng(seed);
+  std::vector<uint64_t> bs(n);
+  std::vector<float> ba(n), bg(n);
+  uint64_t const bsz = std::min<uint64_t>(batch, n);
+  uint64_t const nb = n / bsz;
+  double loss = 0.0;
+  for (unsigned ep = 0; ep < epochs; ++ep) {
+    std::shuffle(order.begin(), order.end(), rng);
+    for (uint64_t q = 0; q < n; ++q) {
+      bs[q] = hs[order[q]];
+      ba[q] = ha[order[q]];
+      bg[q] = hg[order[q]];
+    }
+    SED_TRY_CUDA(cudaMemcpyAsync(sb.ptr, bs.data(), n * 8, cudaMemcpyHostToDevice, d.stream));
+    SED_TRY_CUDA(cudaMemcpyAsync(ta.ptr, ba.data(), n * 4, cudaMemcpyHostToDevice, d.stream));
+    SED_TRY_CUDA(cudaMemcpyAsync(ts.ptr, bg.data(), n * 4, cudaMemcpyHostToDevice, d.stream));
+    for (uint64_t bi = 0; bi < nb; ++bi) {
+      uint64_t const b0 = bi * bsz;
+      if (int st = forward(d, sb.as<uint64_t>() + b0, bsz, true)) return st;
+      bool const last = ep + 1 == epochs && bi + 1 == nb;
+      if (int st = backward(d, sb.as<uint64_t>() + b0, bsz, ta.as<float>() + b0, ts.as<float>() + b0,
+                            last ? &loss : nullptr))
+        return st;
+      ++d.step;
+      float const c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)d.step)));
+      float const c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)d.step)));
+      { k_adam<<<blocks_for((int64_t)d.n_params), 256, 0, d.stream>>>(d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2); note_launches(1); }
+    }
+    SED_TRY_CUDA(cudaGetLastError());
+    // the host staging buffers are rewritten next epoch: wait for the uploads
+    SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
+  }
+  if (final_loss) *final_loss = loss;
+  return LS_SUCCESS;
+}
+
+int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, uint64_t seed, uint64_t* states,
+                   float* t_abs, float* t_sign) {
+  if (!basis || !psi || (n && (!states || !t_abs || !t_sign)))
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_sample: NULL argument");
+  BasisData& b = *basis->d;
+  if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  if (b.D == 0) return fail(LS_INVALID_ARGUMENT, "sed_mlp_sample: empty basis");
+  if (n == 0) return LS_SUCCESS;
+  ScopedDevice dev(b.device);
+  cudaStream_t s = nullptr;
+  SED_TRY_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } guard{s};
+  uint64_t const D = b.D, chunks = (D + kChunk - 1) / kChunk;
+  DeviceBuffer dpsi, sums, offs, prefix, os, oa, og;
+  if (int st = stage(dpsi, psi, D * 8, s)) return st;
+  if (int st = sums.allocate(chunks * 8)) return st;
+  if (int st = offs.allocate(chunks * 8)) return st;
+  if (int st = prefix.allocate(D * 8)) return st;
+  if (int st = os.allocate(n * 8)) return st;
+  if (int st = oa.allocate(n * 4)) return st;
+  if (int st = og.allocate(n * 4)) return st;
+  { k_chunk_sums<<<(unsigned)chunks, 256, 0, s>>>(dpsi.as<double>(), D, sums.as<double>()); note_launches(1); }
+  std::vector<double> hs(chunks);
+  SED_TRY_CUDA(cudaMemcpyAsync(hs.data(), sums.ptr, chunks * 8, cudaMemcpyDeviceToHost, s));
+  SED_TRY_CUDA(cudaStreamSynchronize(s));
+  double total = 0.0;
+  for (uint64_t c = 0; c < chunks; ++c) {
+    double const t = hs[c];
+    hs[c] = total;
+    total += t;
+  }
+  if (!(total > 0.0) || !std::isfinite(total))
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_sample: psi has no finite nonzero weight");
+  SED_TRY_CUDA(cudaMemcpyAsync(offs.ptr, hs.data(), chunks * 8, cudaMemcpyHostToDevice, s));
+  { k_chunk_prefix<<<(unsigned)chunks, 256, 0, s>>>(dpsi.as<double>(), D, offs.as<double>(), prefix.as<double>()); note_launches(1); }
+  // draw below the last prefix value, which may differ from total by rounding
+  double last = 0.0;
+  SED_TRY_CUDA(cudaMemcpyAsync(&last, prefix.as<double>() + (D - 1), 8, cudaMemcpyDeviceToHost, s));
+  SED_TRY_CUDA(cudaStreamSynchronize(s));
+  { k_draw<<<blocks_for((int64_t)n), 256, 0, s>>>(prefix.as<double>(), D, last, n, seed, dpsi.as<double>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>(), (double)b.plan.group_order, os.as<uint64_t>(), oa.as<float>(), og.as<float>()); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  SED_TRY_CUDA(cudaMemcpyAsync(states, os.ptr, n * 8, cudaMemcpyDefault, s));
+  SED_TRY_CUDA(cudaMemcpyAsync(t_abs, oa.ptr, n * 4, cudaMemcpyDefault, s));
+  SED_TRY_CUDA(cudaMemcpyAsync(t_sign, og.ptr, n * 4, cudaMemcpyDefault, s));
+  SED_TRY_CUDA(cudaStreamSynchronize(s));
+  return LS_SUCCESS;
+}
+
+int sed_mlp_start_vector(sed_mlp* m, ls_spin_basis const* basis, double* out) {
+  if (!m || !basis || !out) return fail(LS_INVALID_ARGUMENT, "sed_mlp_start_vector: NULL argument");
+  MlpData& d = m->d;
+  BasisData& b = *basis->d;
+  if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+  if (b.n != d.n_in) return fail(LS_DIMENSION_MISMATCH, "sed_mlp_start_vector: network inputs != number of spins");
+  if (b.D == 0) return LS_SUCCESS;
+  ScopedDevice dev(d.device);
+  uint64_t const D = b.D, chunk = 1u << 18;
+  DeviceBuffer amp, part, vout;
+  if (int st = amp.allocate(D * 8)) return st;  // (a, s) pairs
+  if (int st = part.allocate(152 * 16 * 4)) return st;
+  for (uint64_t b0 = 0; b0 < D; b0 += chunk) {
+    uint64_t const nb = std::min(chunk, D - b0);
+    if (int st = forward(d, b.reps.as<uint64_t>() + b0, nb, false)) return st;
+    SED_TRY_CUDA(cudaMemcpyAsync(amp.as<float>() + 2 * b0, d.out.ptr, nb * 8, cudaMemcpyDeviceToDevice, d.stream));
+  }
+  unsigned const lb = blocks_for((int64_t)D);
+  { k_max_first<<<lb, 256, 0, d.stream>>>(amp.as<float>(), (int64_t)D, part.as<float>()); note_launches(1); }
+  std::vector<float> hp(lb);
+  SED_TRY_CUDA(cudaMemcpyAsync(hp.data(), part.ptr, lb * 4, cudaMemcpyDeviceToHost, d.stream));
+  SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
+  float amax = -3.0e38f;
+  for (float q : hp) amax = std::max(amax, q);
+  cudaPointerAttributes attr{};
+  bool const dev_out = cudaPointerGetAttributes(&attr, out) == cudaSuccess &&
+                       (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged);
+  (void)cudaGetLastError();
+  double* dst = out;
+  if (!dev_out) {
+    if (int st = vout.allocate(D * 8)) return st;
+    dst = vout.as<double>();
+  }
+  { k_start_from_net<<<lb, 256, 0, d.stream>>>(amp.as<float>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>(), (int64_t)D, d.sign_mask, amax, (double)b.plan.group_order, dst); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  if (!dev_out) SED_TRY_CUDA(cudaMemcpyAsync(out, dst, D * 8, cudaMemcpyDeviceToHost, d.stream));
+  SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
+  return LS_SUCCESS;
+}
+
+}  // extern "C"

@@ -219,6 +219,46 @@ __global__ void __launch_bounds__(kBlock) k_spmv(StreamView S, uint64_t D, X con
   }
 }
 
+// Block form: K columns per pass, each recorded element decoded once and
+// applied to all K columns (the block matvec of src/SpinED.hs:172's
+// max_primme_block_size). Per column the sum and its order are those of
+// k_spmv, so results are bit-identical to K single-column calls.
+template <class X, bool RealOp, bool Packed, int K>
+__global__ void __launch_bounds__(kBlock) k_spmv_block(StreamView S, uint64_t D, X const* __restrict__ x,
+                                                       uint64_t ldx, X* __restrict__ y, uint64_t ldy) {
+  using V = typename Store<X>::V;
+  extern __shared__ unsigned char smem_raw[];
+  void const* table = stage_table<RealOp>(S, smem_raw);
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  if ((s << 5) >= D) return;
+  uint32_t const lane = threadIdx.x & 31;
+  uint64_t const base = S.slice_ptr[s];
+  uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
+  uint32_t const col_mask = Packed ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
+  V acc[K];
+#pragma unroll
+  for (int c = 0; c < K; ++c) acc[c] = zero<V>();
+  uint32_t const* ent = S.entries + base + lane;
+  for (uint32_t e = 0; e < width; ++e) {
+    uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
+    if (v != kNull) {
+      uint32_t const col = v & col_mask;
+      uint32_t const code = Packed ? (v >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)e * 32);
+      V const t = load_table<V>(table, code, RealOp);
+#pragma unroll
+      for (int c = 0; c < K; ++c) mac(acc[c], t, Store<X>::load(x + c * ldx, col));
+    }
+  }
+  if (i < D) {
+    double const f = S.inv_sqrt_s[S.row_class[i]];
+    V const dg = stream_diag<V, RealOp>(S, i);
+#pragma unroll
+    for (int c = 0; c < K; ++c)
+      Store<X>::store(y + c * ldy, i, row_value<V>(mulv(dg, Store<X>::load(x + c * ldx, i)), f, acc[c]));
+  }
+}
+
 // On-the-fly matvec: same sum, same order, recomputing every element.
 template <class W, class X, bool RealOp>
 __global__ void __launch_bounds__(kBlock)
@@ -664,6 +704,47 @@ int launch_apply(OperatorData& op, X const* x, X* y, cudaStream_t stream, bool u
 
 }  // namespace
 
+namespace {
+
+template <class X, bool R, bool Pk>
+void launch_block_k(unsigned K, StreamView const& S, uint64_t D, X const* x, uint64_t ldx, X* y, uint64_t ldy,
+                    unsigned grid, size_t smem, cudaStream_t stream) {
+  switch (K) {
+    case 16: { k_spmv_block<X, R, Pk, 16><<<grid, kBlock, smem, stream>>>(S, D, x, ldx, y, ldy); note_launches(1); } break;
+    case 8: { k_spmv_block<X, R, Pk, 8><<<grid, kBlock, smem, stream>>>(S, D, x, ldx, y, ldy); note_launches(1); } break;
+    case 4: { k_spmv_block<X, R, Pk, 4><<<grid, kBlock, smem, stream>>>(S, D, x, ldx, y, ldy); note_launches(1); } break;
+    default: { k_spmv_block<X, R, Pk, 2><<<grid, kBlock, smem, stream>>>(S, D, x, ldx, y, ldy); note_launches(1); } break;
+  }
+}
+
+template <class X>
+int launch_block(OperatorData& op, unsigned K, X const* x, uint64_t ldx, X* y, uint64_t ldy, cudaStream_t stream) {
+  using V = typename Store<X>::V;
+  constexpr bool complex_storage = std::is_same<V, cplx>::value;
+  StreamForm const& sf = op.stream;
+  StreamView const S = stream_view(op);
+  OperatorTables const& tb = *op.tables;
+  bool const real_tab = op.is_real;
+  unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
+  size_t const smem = std::min<size_t>(32768, (size_t)tb.n_codes * (real_tab ? 8 : 16));
+  uint64_t const D = op.basis->D;
+  if (real_tab) {
+    if (sf.packed) launch_block_k<X, true, true>(K, S, D, x, ldx, y, ldy, grid, smem, stream);
+    else launch_block_k<X, true, false>(K, S, D, x, ldx, y, ldy, grid, smem, stream);
+  } else {
+    if constexpr (complex_storage) {
+      if (sf.packed) launch_block_k<X, false, true>(K, S, D, x, ldx, y, ldy, grid, smem, stream);
+      else launch_block_k<X, false, false>(K, S, D, x, ldx, y, ldy, grid, smem, stream);
+    } else {
+      return fail(LS_OPERATOR_IS_COMPLEX, "complex operator applied to real vectors");
+    }
+  }
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
+}  // namespace
+
 int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void const* x,
                           uint64_t ldx, void* y, uint64_t ldy, cudaStream_t stream, int form) {
   if (int st = operator_ensure_ready(op)) return st;
@@ -677,7 +758,25 @@ int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void cons
     else if (form == SED_FORM_STREAM) return st;  // AUTO falls back to on-the-fly
   }
   size_t const es = (size_t)elem_size(dtype);
-  for (uint64_t c = 0; c < block; ++c) {
+  uint64_t c0 = 0;
+  if (use_stream && block > 1) {
+    // K-column passes over the stream form (K = 16, 8, 4, 2)
+    while (block - c0 >= 2) {
+      unsigned const K = block - c0 >= 16 ? 16 : block - c0 >= 8 ? 8 : block - c0 >= 4 ? 4 : 2;
+      void const* xc = static_cast<char const*>(x) + c0 * ldx * es;
+      void* yc = static_cast<char*>(y) + c0 * ldy * es;
+      int st;
+      switch (dtype) {
+        case 0: st = launch_block<float>(op, K, (float const*)xc, ldx, (float*)yc, ldy, stream); break;
+        case 1: st = launch_block<double>(op, K, (double const*)xc, ldx, (double*)yc, ldy, stream); break;
+        case 2: st = launch_block<float2>(op, K, (float2 const*)xc, ldx, (float2*)yc, ldy, stream); break;
+        default: st = launch_block<double2>(op, K, (double2 const*)xc, ldx, (double2*)yc, ldy, stream); break;
+      }
+      if (st) return st;
+      c0 += K;
+    }
+  }
+  for (uint64_t c = c0; c < block; ++c) {
     void const* xc = static_cast<char const*>(x) + c * ldx * es;
     void* yc = static_cast<char*>(y) + c * ldy * es;
     int st;
@@ -708,7 +807,7 @@ __global__ void __launch_bounds__(kBlock)
     k_spmv32(StreamView S, float const* __restrict__ table_f, float const* __restrict__ diag_f,
              float const* __restrict__ invs_f, uint64_t D, float const* __restrict__ x,
              float* __restrict__ y, Indirect ind) {
-  __shared__ float tab[8192];
+  extern __shared__ float tab[];  // value table, n_codes entries when it fits (dynamic size)
   __shared__ double red[kBlock / 32];
   if (ind.stop && *ind.stop) return;
   if (ind.k) {
@@ -782,10 +881,12 @@ int launch32(OperatorData& op, float const* x, float* y, Indirect ind, cudaStrea
   StreamView const S = stream_view(op);
   unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
   if (blocks) *blocks = grid;
+  // size the table to the codes: a large carve-out would shrink L1 for the gathers
+  size_t const smem = S.n_codes <= 8192u ? (size_t)S.n_codes * 4 : 0;
   if (sf.packed)
-    { k_spmv32<true><<<grid, kBlock, 0, stream>>>(S, sf.table_f.as<float>(), sf.diag_f.as<float>(), sf.invs_f.as<float>(), op.basis->D, x, y, ind); note_launches(1); }
+    { k_spmv32<true><<<grid, kBlock, smem, stream>>>(S, sf.table_f.as<float>(), sf.diag_f.as<float>(), sf.invs_f.as<float>(), op.basis->D, x, y, ind); note_launches(1); }
   else
-    { k_spmv32<false><<<grid, kBlock, 0, stream>>>(S, sf.table_f.as<float>(), sf.diag_f.as<float>(), sf.invs_f.as<float>(), op.basis->D, x, y, ind); note_launches(1); }
+    { k_spmv32<false><<<grid, kBlock, smem, stream>>>(S, sf.table_f.as<float>(), sf.diag_f.as<float>(), sf.invs_f.as<float>(), op.basis->D, x, y, ind); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   return LS_SUCCESS;
 }

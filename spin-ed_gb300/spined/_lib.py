@@ -119,6 +119,16 @@ SIGNATURES = [
     ("sed_basis_device_states", _P, [_P]),
     ("sed_basis_index", _I, [_P, _U64, C.POINTER(_U64)]),
     ("sed_basis_state_info", _I, [_P, _U64, C.POINTER(_U64), C.POINTER(_U), C.POINTER(_U)]),
+    ("sed_mlp_create", _I, [C.POINTER(_P), _U, _U, _U64, _U64]),
+    ("sed_mlp_destroy", None, [_P]),
+    ("sed_mlp_num_params", _U64, [_P]),
+    ("sed_mlp_get_params", _I, [_P, _P]),
+    ("sed_mlp_set_params", _I, [_P, _P]),
+    ("sed_mlp_forward", _I, [_P, _P, _U64, _P]),
+    ("sed_mlp_loss_grad", _I, [_P, _P, _P, _P, _U64, C.POINTER(_D), _P]),
+    ("sed_mlp_train", _I, [_P, _P, _P, _P, _U64, _U, _U, C.c_float, _U64, C.POINTER(_D)]),
+    ("sed_mlp_sample", _I, [_P, _P, _U64, _U64, _P, _P, _P]),
+    ("sed_mlp_start_vector", _I, [_P, _P, _P]),
     ("sed_kernel_launches", _U64, []),
     ("sed_version", C.c_char_p, []),
 ]

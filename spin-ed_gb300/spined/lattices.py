@@ -107,3 +107,14 @@ def j1j2_chains(count: int = 128, seed: int = 2024) -> list[Model]:
     ns = rng.choice(np.arange(16, 29, 2), size=count)
     j2s = rng.uniform(0.0, 0.6, size=count)
     return [heisenberg_chain(int(n), j2=float(j)) for n, j in zip(ns, j2s)]
+
+
+def square_sublattice_mask(L: int) -> int:
+    """Bits of the sites with x + y even (one sublattice of the bipartite
+    L x L torus, L even): the mask of the Marshall sign prior."""
+    return sum(1 << ((y % L) * L + (x % L)) for y in range(L) for x in range(L) if (x + y) % 2 == 0)
+
+
+def chain_sublattice_mask(n: int) -> int:
+    """Even sites of a ring of even length n."""
+    return sum(1 << i for i in range(0, n, 2))

@@ -1,0 +1,122 @@
+"""The learned start vector (sed_mlp_*): forward pass, loss and gradients of
+the GPU kernels against the FP64 CPU oracle (oracle/mlp_oracle.py), the
+|psi|^2 sampler against the vector it samples, and what a trained network
+gains over the random start of the plain method."""
+import numpy as np
+import pytest
+
+import mlp_oracle as M
+from spined import lattices
+from spined.model import build_model
+
+pytestmark = pytest.mark.gpu
+
+
+def _net(n, h, mask=0, seed=3):
+    from spined.learned import Mlp
+    return Mlp(n, h, sign_mask=mask, seed=seed)
+
+
+def _random_states(rng, n, N):
+    return rng.integers(0, 2 ** min(n, 63), size=N, dtype=np.uint64)
+
+
+@pytest.mark.parametrize("n,h", [(20, 64), (36, 512)])
+def test_forward_matches_oracle(n, h):
+    rng = np.random.default_rng(n)
+    net = _net(n, h)
+    p = net.get_params()
+    p[h * n:h * n + h] = rng.normal(scale=0.1, size=h)  # nonzero biases
+    net.set_params(p)
+    st = _random_states(rng, n, 3000)
+    got = net.forward(st)
+    _, _, _, want = M.forward(p, n, h, st)
+    # FP32 accumulation of up to 512 BF16 x FP32 products against FP64
+    np.testing.assert_allclose(got, want, rtol=0, atol=2e-5 * max(1.0, np.abs(want).max()))
+
+
+@pytest.mark.parametrize("n,h,mask", [(16, 64, 0), (36, 512, lattices.square_sublattice_mask(6))])
+def test_gradients_match_oracle(n, h, mask):
+    from spined.learned import Samples
+    rng = np.random.default_rng(7)
+    net = _net(n, h, mask)
+    p = net.get_params()
+    N = 1500
+    s = Samples(_random_states(rng, n, N), rng.normal(size=N).astype(np.float32),
+                rng.integers(0, 2, size=N).astype(np.float32))
+    loss, g = net.loss_grad(s)
+    want_loss, want_g = M.loss_grad(p, n, h, s.states, s.t_abs.astype(np.float64), s.t_sign, mask)
+    assert loss == pytest.approx(want_loss, rel=1e-5)
+    # per-block tolerance: FP32 sums over N samples against FP64
+    o = 0
+    for name, k in [("W1", h * n), ("b1", h), ("W2", h * h), ("b2", h), ("W3", 2 * h), ("b3", 2)]:
+        gg, ww = g[o:o + k], want_g[o:o + k]
+        np.testing.assert_allclose(gg, ww, rtol=0, atol=2e-4 * np.abs(ww).max() + 1e-9, err_msg=name)
+        o += k
+
+
+def test_training_lowers_the_loss():
+    from spined.learned import Samples
+    rng = np.random.default_rng(11)
+    n, h, N = 16, 64, 1 << 14
+    st = _random_states(rng, n, N)
+    # a smooth target: log-amplitude = 0.1 * (number of up spins), sign = bit 0
+    ones = np.array([bin(int(v)).count("1") for v in st], dtype=np.float32)
+    s = Samples(st, 0.1 * ones, (st & np.uint64(1)).astype(np.float32))
+    net = _net(n, h)
+    l0, _ = net.loss_grad(s)
+    l1 = net.train(s, epochs=20, batch=1024, lr=3e-3, seed=1)
+    l2, _ = net.loss_grad(s)
+    assert l2 < 0.1 * l0, (l0, l1, l2)
+
+
+def test_sampler_labels_and_frequencies(sed):
+    from spined.learned import sample
+    b = build_model(lattices.heisenberg_chain(16))
+    res = sed.eigh(b.hamiltonian)
+    psi = res.eigenvectors[:, 0]
+    reps = sed.basis_get_states(b.basis)
+    norms = np.zeros(len(reps))
+    import ctypes as C
+    from spined import _lib as L
+    assert L.load().sed_basis_get_norms(b.basis.ptr, C.c_void_p(norms.ctypes.data)) == 0
+    n = 1 << 18
+    s = sample(b.basis, psi, n, seed=9)
+    idx = np.searchsorted(reps, s.states)
+    assert np.all(reps[idx] == s.states)
+    np.testing.assert_allclose(s.t_abs, np.log(np.abs(psi[idx]) * norms[idx]), rtol=0, atol=1e-5)
+    np.testing.assert_array_equal(s.t_sign, (psi[idx] > 0).astype(np.float32))
+    # frequencies against psi^2: every representative within 5 sigma
+    p = psi ** 2 / np.sum(psi ** 2)
+    counts = np.bincount(idx, minlength=len(reps))
+    sigma = np.sqrt(n * p * (1 - p)) + 1
+    assert np.all(np.abs(counts - n * p) <= 5 * sigma)
+    # the same seed gives the same samples
+    s2 = sample(b.basis, psi, 1000, seed=9)
+    np.testing.assert_array_equal(s2.states, s.states[:1000])
+
+
+def test_learned_start_beats_random_start(sed):
+    """J1-J2 ring of 24 spins: ground states at J2 = 0, 0.1, 0.2 train the
+    network; at J2 = 0.3 its start vector must need fewer Lanczos steps than
+    the plain method's random start, and both must reach the same eigenpair."""
+    from spined.learned import Mlp, Samples, sample
+    n = 24
+    parts = []
+    for k, j2 in enumerate([0.0, 0.1, 0.2]):
+        b = build_model(lattices.heisenberg_chain(n, j2=j2))
+        r = sed.eigh(b.hamiltonian)
+        parts.append(sample(b.basis, r.eigenvectors[:, 0], 1 << 16, seed=k))
+    data = Samples.concat(parts)
+    net = Mlp(n, 128, sign_mask=lattices.chain_sublattice_mask(n), seed=5)
+    net.train(data, epochs=30, batch=2048, lr=2e-3, seed=2)
+    target = build_model(lattices.heisenberg_chain(n, j2=0.3))
+    v = net.start_vector(target.basis)
+    rand = sed.eigh(target.hamiltonian, seed=1234)
+    learned = sed.eigh(target.hamiltonian, start=v / np.linalg.norm(v))
+    psi = rand.eigenvectors[:, 0]
+    overlap = abs(np.dot(v, psi)) / np.linalg.norm(v)
+    assert overlap > 0.9, overlap
+    assert learned.eigenvalues[0] == pytest.approx(rand.eigenvalues[0], rel=1e-10)
+    assert learned.residuals[0] <= 1e-8
+    assert learned.iterations < rand.iterations, (learned.iterations, rand.iterations)
