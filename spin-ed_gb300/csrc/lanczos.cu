@@ -65,8 +65,15 @@ __global__ void k_reduce(double const* __restrict__ partial, unsigned n, LzHeade
                          double* __restrict__ arr, int mode) {
   __shared__ double red[kRedThreads / 32];
   if (h->stop) return;
-  double s = 0.0;
-  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+  // eight independent sums per thread keep eight loads in flight (the
+  // partials of a one-row-per-thread SpMV number D / 256); fixed order
+  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  unsigned i = threadIdx.x;
+  for (; i + 7 * blockDim.x < n; i += 8 * blockDim.x)
+#pragma unroll
+    for (unsigned q = 0; q < 8; ++q) a[q] += partial[i + q * blockDim.x];
+  for (; i < n; i += blockDim.x) a[0] += partial[i];
+  double s = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
   s = block_sum(s, red);
   if (threadIdx.x == 0) {
     uint32_t const k = h->k;

@@ -831,7 +831,30 @@ __global__ void __launch_bounds__(kBlock)
     uint32_t const col_mask = Packed ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
     float acc = 0.0f;
     uint32_t const* ent = S.entries + base + lane;
-    for (uint32_t e = 0; e < width; ++e) {
+    // Four entries per step: their loads, then their gathers, are issued
+    // back to back (padding reads x[0] with a zero value); the sum keeps
+    // entry order.
+    constexpr uint32_t U = 4;
+    uint32_t e = 0;
+    for (; e + U <= width; e += U) {
+      uint32_t v[U];
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) v[q] = __ldcs(ent + (uint64_t)(e + q) * 32);
+      float xv[U], tv[U];
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) {
+        bool const ok = v[q] != kNull;
+        uint32_t const col = ok ? (v[q] & col_mask) : 0u;
+        uint32_t code = 0;
+        if (ok)
+          code = Packed ? (v[q] >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)(e + q) * 32);
+        xv[q] = x[col];
+        tv[q] = ok ? tb[code] : 0.0f;
+      }
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) acc = fmaf(tv[q], xv[q], acc);
+    }
+    for (; e < width; ++e) {
       uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
       if (v != kNull) {
         uint32_t const col = v & col_mask;
