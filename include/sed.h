@@ -305,13 +305,29 @@ SED_API int sed_mlp_train(sed_mlp* mlp, uint64_t const* states, float const* t_a
 /* Training data from a real vector psi over the built basis: n representatives
  * drawn with probability psi_r^2 / ||psi||^2 (Philox from `seed`), labelled
  * t_abs = log|psi_r n_r| (the amplitude of the configuration itself, n_r =
- * ||P r||) and t_sign = [psi_r > 0]. */
+ * ||P r||) and t_sign = [sigma psi_r > 0]. An eigenvector's global sign is
+ * arbitrary, so sigma = +1 or -1 is chosen to make
+ * sum_r prior(r) sigma psi_r |psi_r| >= 0 with prior(r) =
+ * (-1)^popcount(r & sign_mask): data sets sampled from several ground states
+ * then agree on the sign (pass the network's sign_mask). */
 SED_API int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, uint64_t seed,
-                           uint64_t* states, float* t_abs, float* t_sign);
+                           uint64_t sign_mask, uint64_t* states, float* t_abs, float* t_sign);
 /* Start vector over the built basis: v_r = prior(r) sign(s_r) exp(a_r) / n_r,
  * scaled so the largest configuration amplitude is 1; out holds D doubles.
  * Pass it to sed_eigh as SED_START_GIVEN. */
 SED_API int sed_mlp_start_vector(sed_mlp* mlp, ls_spin_basis const* basis, double* out);
+
+/* Inference path of sed_mlp_forward and sed_mlp_start_vector. AUTO runs the
+ * whole network on the tensor cores (tcgen05, BF16 operands, FP32
+ * accumulation in tensor memory, one fused kernel per 128 states) when
+ * n_inputs <= 64 and hidden is 128, 256 or 512; there the hidden activations
+ * h1 are rounded to BF16 between the layers and tanh is the hardware
+ * approximation. SIMT keeps every product on the CUDA cores with FP32
+ * activations (the path training uses). */
+enum { SED_MLP_PATH_AUTO = 0, SED_MLP_PATH_SIMT = 1 };
+SED_API int sed_mlp_set_path(sed_mlp* mlp, int path);
+/* 1 if inference runs on the tensor cores, else 0. */
+SED_API int sed_mlp_uses_tensor_cores(sed_mlp const* mlp);
 
 /* Number of libsed kernels launched by this process so far (graph replays
  * count their kernel nodes). */

@@ -48,11 +48,15 @@ def parity(states: np.ndarray, mask: int) -> np.ndarray:
     return (c & 1).astype(np.float64)
 
 
-def forward(p, n, h, states):
+def forward(p, n, h, states, act_bf16=False):
+    """Activations and outputs. act_bf16 rounds h1 to BF16 before the second
+    layer, as the tensor-core inference path stores it."""
     w = unpack(p, n, h)
     W1, W2, W3 = bf16(w["W1"]), bf16(w["W2"]), bf16(w["W3"])
     x = spins(states, n)
     h1 = np.tanh(x @ W1.T + w["b1"])
+    if act_bf16:
+        h1 = bf16(h1.astype(np.float32))
     h2 = np.tanh(h1 @ W2.T + w["b2"])
     out = h2 @ W3.T + w["b3"]
     return x, h1, h2, out

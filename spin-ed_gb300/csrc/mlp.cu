@@ -29,6 +29,7 @@
 #include <type_traits>
 
 #include "sed_internal.hpp"
+#include "tc.cuh"
 #include "util.cuh"
 
 namespace sed {
@@ -202,16 +203,28 @@ __global__ void k_max_first(float const* __restrict__ out, int64_t n, float* __r
 // ------------------------------------------------------------- sampling ---
 constexpr int kChunk = 4096;  // elements per block of the prefix sum (256 threads x 16)
 
-__global__ void k_chunk_sums(double const* __restrict__ psi, uint64_t D, double* __restrict__ sums) {
+// Per chunk: sum of psi^2 and of prior(r) psi_r |psi_r| (the weight with which
+// psi agrees with the sign prior, used to fix psi's global sign).
+__global__ void k_chunk_sums(double const* __restrict__ psi, uint64_t const* __restrict__ reps, uint64_t D,
+                             uint64_t sign_mask, double* __restrict__ sums) {
   __shared__ double red[32];
   uint64_t const base = (uint64_t)blockIdx.x * kChunk;
-  double s = 0.0;
+  double s = 0.0, a = 0.0;
   for (int q = threadIdx.x; q < kChunk; q += blockDim.x) {
     uint64_t const i = base + q;
-    if (i < D) s += psi[i] * psi[i];
+    if (i < D) {
+      double const w = psi[i] * psi[i];
+      s += w;
+      bool const neg = (psi[i] < 0.0) != (prior_flip(reps[i], sign_mask) != 0.0f);
+      a += neg ? -w : w;
+    }
   }
   double const t = block_sum(s, red);
-  if (threadIdx.x == 0) sums[blockIdx.x] = t;
+  double const u = block_sum(a, red);
+  if (threadIdx.x == 0) {
+    sums[blockIdx.x] = t;
+    sums[gridDim.x + blockIdx.x] = u;
+  }
 }
 
 // prefix[i] = offset[chunk] + sum_{j <= i in chunk} psi_j^2
@@ -248,7 +261,7 @@ __global__ void __launch_bounds__(256) k_chunk_prefix(double const* __restrict__
 // Sample q: u = total * U[0,1) from Philox block (q, seed); its index is the
 // smallest i with prefix[i] > u.
 __global__ void k_draw(double const* __restrict__ prefix, uint64_t D, double total, uint64_t n, uint64_t seed,
-                       double const* __restrict__ psi, uint64_t const* __restrict__ reps,
+                       double sign, double const* __restrict__ psi, uint64_t const* __restrict__ reps,
                        uint32_t const* __restrict__ weights, double group_order, uint64_t* __restrict__ states,
                        float* __restrict__ t_abs, float* __restrict__ t_sign) {
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (uint64_t)gridDim.x * blockDim.x) {
@@ -263,7 +276,7 @@ __global__ void k_draw(double const* __restrict__ prefix, uint64_t D, double tot
       else
         lo = mid + 1;
     }
-    double const p = psi[lo];
+    double const p = sign * psi[lo];
     states[q] = reps[lo];
     t_abs[q] = (float)(log(fabs(p)) + 0.5 * log((double)weights[lo] / group_order));
     t_sign[q] = p > 0.0 ? 1.0f : 0.0f;
@@ -271,6 +284,244 @@ __global__ void k_draw(double const* __restrict__ prefix, uint64_t D, double tot
 }
 
 unsigned blocks_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+// ------------------------------------------------ tensor-core inference ---
+// The whole network for 128 states per CTA on the 5th-generation tensor
+// cores, for n <= 64 inputs and hidden = 128, 256 or 512:
+//   X [128 x 64] (spins built in shared memory from the state bits, zero
+//   padded), h1 = tanh(X W1^T + b1) -> TMEM (FP32) -> BF16 in shared memory,
+//   h2 = tanh(h1 W2^T + b2) -> TMEM, (a, s) = W3 h2 + b3 in registers.
+// Weights come from pre-swizzled images in global memory (L2-resident, a
+// few hundred KB) through bulk asynchronous copies, two stages of N x 64
+// columns; one thread issues the copies and the MMAs, four warps run the
+// epilogues (warp w owns TMEM lanes / rows 32 w .. 32 w + 31).
+constexpr int kTcRows = 128;
+constexpr uint64_t kTcWaitNs = 1000000000ull;  // 1 s per wait: far beyond any MMA or copy
+
+struct MlpTcArgs {
+  uint64_t const* states;
+  int64_t n;
+  int n_in, hidden;
+  uint8_t const* w1img;  // hidden rows x 128 B (K = 64, zero padded), swizzled
+  uint8_t const* w2img;  // hidden/64 tiles of hidden rows x 128 B, swizzled
+  float const* b1;
+  float const* b2;
+  __nv_bfloat16 const* W3;  // [2][hidden]
+  float const* b3;
+  float* out;  // [n][2]
+  int* error;
+};
+
+size_t tc_smem_bytes(int hidden) {
+  int const nm = hidden < 256 ? hidden : 256;
+  return (size_t)kTcRows * hidden * 2 + 2 * (size_t)nm * 128 + 1024;
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(MlpTcArgs p) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full1[2], full[2], empty[2], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  uint8_t* const smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  int const H = p.hidden, NM = H < 256 ? H : 256, halves = H / NM;
+  uint32_t const stage_bytes = (uint32_t)NM * 128;
+  uint8_t* const A = smem;  // H/64 tiles of 128 rows x 128 B
+  uint8_t* const B0 = smem + (size_t)kTcRows * H * 2;
+  uint8_t* const Bs[2] = {B0, B0 + stage_bytes};
+  int const t = threadIdx.x, warp = t >> 5, r = t;
+  int64_t const row = (int64_t)blockIdx.x * kTcRows + r;
+  uint32_t const idesc = tc::idesc_bf16_f32(128, (uint32_t)NM);
+
+  if (t == 0) {
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&full1[i], 1);
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
+    tc::mbar_init(&done, 1);
+    abort_flag = 0;
+    tc::fence_mbar_init();
+  }
+  __syncwarp();
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)H);
+  // X tile: row r, input j -> BF16 +1 / -1, zero for j >= n_in
+  {
+    uint64_t const s = row < p.n ? p.states[row] : 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      uint32_t w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        int const j = 8 * c + 2 * q;
+        uint32_t const lo = j < p.n_in ? (((s >> j) & 1) ? 0x3F80u : 0xBF80u) : 0u;
+        uint32_t const hi = j + 1 < p.n_in ? (((s >> (j + 1)) & 1) ? 0x3F80u : 0xBF80u) : 0u;
+        w[q] = lo | (hi << 16);
+      }
+      *reinterpret_cast<uint4*>(A + r * 128 + ((c ^ (r & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  uint32_t const tmem = tmem_slot;
+
+  // ---- layer 1: both N halves of W1 at once, 4 MMAs (K = 16 each) per half
+  if (t == 0) {
+    for (int h = 0; h < halves; ++h) {
+      tc::mbar_expect_tx(&full1[h], stage_bytes);
+      tc::bulk_g2s(Bs[h], p.w1img + (size_t)h * stage_bytes, stage_bytes, &full1[h]);
+    }
+    bool ok = true;
+    for (int h = 0; h < halves && ok; ++h) {
+      ok = tc::mbar_wait(&full1[h], 0, kTcWaitNs);
+      if (!ok) break;
+      tc::fence_after_sync();
+      uint32_t const a0 = tc::smem_u32(A), b0 = tc::smem_u32(Bs[h]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        tc::mma_bf16(tmem + (uint32_t)(h * NM), tc::desc_sw128(a0 + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
+                     k > 0);
+    }
+    if (ok) tc::mma_commit(&done);
+    else abort_flag = 1;
+  }
+  __syncwarp();
+  __syncthreads();
+  bool ok = abort_flag == 0;
+  if (ok) ok = tc::mbar_wait(&done, 0, kTcWaitNs);
+  tc::fence_after_sync();
+  int const tiles2 = H / 64, jobs = tiles2 * halves;
+  // stages are free again: start streaming W2 (jobs (tile, half), two ahead)
+  if (t == 0 && ok)
+    for (int j = 0; j < 2 && j < jobs; ++j) {
+      int const kb = j / halves, h = j % halves;
+      tc::mbar_expect_tx(&full[j], stage_bytes);
+      tc::bulk_g2s(Bs[j], p.w2img + ((size_t)kb * H + (size_t)h * NM) * 128, stage_bytes, &full[j]);
+    }
+  __syncwarp();
+  // ---- epilogue 1: h1 = tanh(acc + b1) -> BF16 -> A tiles (row r)
+  if (ok) {
+    uint32_t const lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int cc = 0; cc < H / 32; ++cc) {
+      float v[32];
+      tc::tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
+      uint32_t pk[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        int const c = cc * 32 + 2 * q;
+        pk[q] = tc::pack_bf16x2(tc::tanh_fast(v[2 * q] + __ldg(p.b1 + c)),
+                                tc::tanh_fast(v[2 * q + 1] + __ldg(p.b1 + c + 1)));
+      }
+      uint8_t* const tile = A + (size_t)(cc >> 1) * (kTcRows * 128) + r * 128;
+#pragma unroll
+      for (int q4 = 0; q4 < 4; ++q4) {
+        int const chunk = ((cc & 1) * 4 + q4) ^ (r & 7);
+        *reinterpret_cast<uint4*>(tile + (chunk << 4)) =
+            make_uint4(pk[4 * q4], pk[4 * q4 + 1], pk[4 * q4 + 2], pk[4 * q4 + 3]);
+      }
+    }
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (!ok) abort_flag = 1;
+  __syncthreads();
+  ok = abort_flag == 0;
+
+  // ---- layer 2: job j = (K tile j / halves, N half j % halves) in stage j & 1
+  if (t == 0 && ok) {
+    uint32_t const a0 = tc::smem_u32(A);
+    for (int j = 0; j < jobs && ok; ++j) {
+      int const s = j & 1, kb = j / halves, h = j % halves;
+      ok = tc::mbar_wait(&full[s], (uint32_t)(j >> 1) & 1, kTcWaitNs);
+      if (!ok) break;
+      tc::fence_after_sync();
+      uint32_t const b0 = tc::smem_u32(Bs[s]), at = a0 + (uint32_t)(kb * kTcRows * 128);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        tc::mma_bf16(tmem + (uint32_t)(h * NM), tc::desc_sw128(at + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
+                     (kb > 0 || k > 0) ? 1u : 0u);
+      tc::mma_commit(&empty[s]);
+      // refill the stage of job j - 1 with job j + 1 once its MMAs are done
+      if (j >= 1 && j + 1 < jobs) {
+        int const sp = (j - 1) & 1;
+        ok = tc::mbar_wait(&empty[sp], (uint32_t)((j - 1) >> 1) & 1, kTcWaitNs);
+        if (!ok) break;
+        int const kn = (j + 1) / halves, hn = (j + 1) % halves;
+        tc::mbar_expect_tx(&full[sp], stage_bytes);
+        tc::bulk_g2s(Bs[sp], p.w2img + ((size_t)kn * H + (size_t)hn * NM) * 128, stage_bytes, &full[sp]);
+      }
+    }
+    if (ok) tc::mma_commit(&done);
+    else abort_flag = 1;
+  }
+  __syncwarp();
+  __syncthreads();
+  ok = abort_flag == 0;
+  if (ok) ok = tc::mbar_wait(&done, 1, kTcWaitNs);
+  tc::fence_after_sync();
+  __syncwarp();
+  // ---- epilogue 2: h2 = tanh(acc + b2); (a, s) = W3 h2 + b3
+  if (ok) {
+    uint32_t const lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    float a = __ldg(p.b3), sg = __ldg(p.b3 + 1);
+    for (int cc = 0; cc < H / 32; ++cc) {
+      float v[32];
+      tc::tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        int const c = cc * 32 + q;
+        float const hq = tc::tanh_fast(v[q] + __ldg(p.b2 + c));
+        a = fmaf(__bfloat162float(p.W3[c]), hq, a);
+        sg = fmaf(__bfloat162float(p.W3[H + c]), hq, sg);
+      }
+    }
+    if (row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(a, sg);
+  }
+  if (!ok && (t & 31) == 0) atomicExch(p.error, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, (uint32_t)H);
+  }
+}
+
+// Weight images for k_mlp_forward_tc from the BF16 parameters: W1 [H][n_in]
+// (zero padded to 64 columns) and W2 [H][H], swizzled as the MMA reads them.
+__global__ void k_mlp_images(__nv_bfloat16 const* __restrict__ W1, __nv_bfloat16 const* __restrict__ W2, int n_in,
+                             int H, uint8_t* __restrict__ w1img, uint8_t* __restrict__ w2img) {
+  int64_t const n1 = (int64_t)H * 8, n2 = (int64_t)(H / 64) * H * 8;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n1 + n2; q += (int64_t)gridDim.x * blockDim.x) {
+    uint16_t e[8];
+    uint8_t* dst;
+    if (q < n1) {
+      int const R = (int)(q >> 3), c = (int)(q & 7);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        int const j = 8 * c + i;
+        e[i] = j < n_in ? __bfloat16_as_ushort(W1[(int64_t)R * n_in + j]) : (uint16_t)0;
+      }
+      dst = w1img + (int64_t)R * 128 + ((c ^ (R & 7)) << 4);
+    } else {
+      int64_t const u = q - n1;
+      int const c = (int)(u & 7);
+      int64_t const rr = u >> 3;
+      int const R = (int)(rr % H), kb = (int)(rr / H);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) e[i] = __bfloat16_as_ushort(W2[(int64_t)R * H + kb * 64 + 8 * c + i]);
+      dst = w2img + ((int64_t)kb * H + R) * 128 + ((c ^ (R & 7)) << 4);
+    }
+    uint4 v;
+    v.x = e[0] | ((uint32_t)e[1] << 16);
+    v.y = e[2] | ((uint32_t)e[3] << 16);
+    v.z = e[4] | ((uint32_t)e[5] << 16);
+    v.w = e[6] | ((uint32_t)e[7] << 16);
+    *reinterpret_cast<uint4*>(dst) = v;
+  }
+}
 
 }  // namespace
 
@@ -285,6 +536,11 @@ struct MlpData {
   cudaStream_t stream = nullptr;
   DeviceBuffer x, h1, h2, out, d2, d1, dout, loss_part;  // activations of one batch
   uint64_t cap = 0, cap_train = 0;
+  // tensor-core inference: swizzled weight images (rebuilt when the BF16
+  // weights change) and a device error flag
+  DeviceBuffer wimg, tc_error;
+  bool img_valid = false;
+  int path = 0;  // SED_MLP_PATH_*
   ~MlpData() {
     if (stream) cudaStreamDestroy(stream);
   }
@@ -374,7 +630,54 @@ int backward(MlpData& d, uint64_t const* states, uint64_t n, float const* t_abs,
   return LS_SUCCESS;
 }
 
+bool tc_eligible(MlpData const& d) {
+  return d.path != SED_MLP_PATH_SIMT && d.n_in <= 64 && (d.hidden == 128 || d.hidden == 256 || d.hidden == 512);
+}
+
+// (a, s) for states[0..n) (device pointer) into out[2 n] (device), on the
+// tensor cores.
+int forward_tc(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
+  cudaStream_t s = d.stream;
+  int const H = (int)d.hidden;
+  size_t const img1 = (size_t)H * 128, img2 = (size_t)H * H * 2;
+  if (!d.img_valid) {
+    if (int st = d.wimg.allocate(img1 + img2)) return st;
+    if (!d.tc_error.ptr)
+      if (int st = d.tc_error.allocate(16)) return st;
+    __nv_bfloat16 const* W = d.pb.as<__nv_bfloat16>();
+    { k_mlp_images<<<blocks_for((int64_t)(H * 8 + H * H / 8)), 256, 0, s>>>(W + d.oW1, W + d.oW2, (int)d.n_in, H, d.wimg.as<uint8_t>(), d.wimg.as<uint8_t>() + img1); note_launches(1); }
+    SED_TRY_CUDA(cudaGetLastError());
+    d.img_valid = true;
+  }
+  if (n == 0) return LS_SUCCESS;
+  size_t const smem = tc_smem_bytes(H);
+  SED_TRY_CUDA(cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SED_TRY_CUDA(cudaMemsetAsync(d.tc_error.ptr, 0, 4, s));
+  MlpTcArgs a;
+  a.states = states;
+  a.n = (int64_t)n;
+  a.n_in = (int)d.n_in;
+  a.hidden = H;
+  a.w1img = d.wimg.as<uint8_t>();
+  a.w2img = d.wimg.as<uint8_t>() + img1;
+  a.b1 = d.p.as<float>() + d.ob1;
+  a.b2 = d.p.as<float>() + d.ob2;
+  a.W3 = d.pb.as<__nv_bfloat16>() + d.oW3;
+  a.b3 = d.p.as<float>() + d.ob3;
+  a.out = out;
+  a.error = d.tc_error.as<int>();
+  unsigned const grid = (unsigned)((n + kTcRows - 1) / kTcRows);
+  { k_mlp_forward_tc<<<grid, 128, smem, s>>>(a); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  int err = 0;
+  SED_TRY_CUDA(cudaMemcpyAsync(&err, d.tc_error.ptr, 4, cudaMemcpyDeviceToHost, s));
+  SED_TRY_CUDA(cudaStreamSynchronize(s));
+  if (err) return fail(LS_DEVICE_TIMEOUT, "MLP tensor-core forward: a wait on the tensor cores timed out");
+  return LS_SUCCESS;
+}
+
 int refresh_bf16(MlpData& d) {
+  d.img_valid = false;
   { k_to_bf16<<<blocks_for((int64_t)d.n_params), 256, 0, d.stream>>>(d.p.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   return LS_SUCCESS;
@@ -468,6 +771,16 @@ void sed_mlp_destroy(sed_mlp* m) {
 
 uint64_t sed_mlp_num_params(sed_mlp const* m) { return m ? m->d.n_params : 0; }
 
+int sed_mlp_set_path(sed_mlp* m, int path) {
+  if (!m) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_path: NULL argument");
+  if (path != SED_MLP_PATH_AUTO && path != SED_MLP_PATH_SIMT)
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_path: unknown path");
+  m->d.path = path;
+  return LS_SUCCESS;
+}
+
+int sed_mlp_uses_tensor_cores(sed_mlp const* m) { return m && tc_eligible(m->d) ? 1 : 0; }
+
 int sed_mlp_get_params(sed_mlp const* m, float* out) {
   if (!m || !out) return fail(LS_INVALID_ARGUMENT, "sed_mlp_get_params: NULL argument");
   ScopedDevice dev(m->d.device);
@@ -493,10 +806,16 @@ int sed_mlp_forward(sed_mlp* m, uint64_t const* states, uint64_t n, float* out) 
   DeviceBuffer sbuf;
   if (n)
     if (int st = sbuf.allocate(std::min(chunk, n) * 8)) return st;
+  bool const tc_path = tc_eligible(d);
   for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
     uint64_t const nb = std::min(chunk, n - b0);
     SED_TRY_CUDA(cudaMemcpyAsync(sbuf.ptr, states + b0, nb * 8, cudaMemcpyDefault, d.stream));
-    if (int st = forward(d, sbuf.as<uint64_t>(), nb, false)) return st;
+    if (tc_path) {
+      if (int st = ensure_batch(d, nb, false)) return st;
+      if (int st = forward_tc(d, sbuf.as<uint64_t>(), nb, d.out.as<float>())) return st;
+    } else if (int st = forward(d, sbuf.as<uint64_t>(), nb, false)) {
+      return st;
+    }
     SED_TRY_CUDA(cudaMemcpyAsync(out + 2 * b0, d.out.ptr, nb * 8, cudaMemcpyDefault, d.stream));
   }
   SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
@@ -568,6 +887,7 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
       float const c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)d.step)));
       { k_adam<<<blocks_for((int64_t)d.n_params), 256, 0, d.stream>>>(d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2); note_launches(1); }
     }
+    d.img_valid = false;
     SED_TRY_CUDA(cudaGetLastError());
     // the host staging buffers are rewritten next epoch: wait for the uploads
     SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
@@ -576,8 +896,8 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
   return LS_SUCCESS;
 }
 
-int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, uint64_t seed, uint64_t* states,
-                   float* t_abs, float* t_sign) {
+int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, uint64_t seed, uint64_t sign_mask,
+                   uint64_t* states, float* t_abs, float* t_sign) {
   if (!basis || !psi || (n && (!states || !t_abs || !t_sign)))
     return fail(LS_INVALID_ARGUMENT, "sed_mlp_sample: NULL argument");
   BasisData& b = *basis->d;
@@ -594,22 +914,25 @@ int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, ui
   uint64_t const D = b.D, chunks = (D + kChunk - 1) / kChunk;
   DeviceBuffer dpsi, sums, offs, prefix, os, oa, og;
   if (int st = stage(dpsi, psi, D * 8, s)) return st;
-  if (int st = sums.allocate(chunks * 8)) return st;
+  if (int st = sums.allocate(2 * chunks * 8)) return st;
   if (int st = offs.allocate(chunks * 8)) return st;
   if (int st = prefix.allocate(D * 8)) return st;
   if (int st = os.allocate(n * 8)) return st;
   if (int st = oa.allocate(n * 4)) return st;
   if (int st = og.allocate(n * 4)) return st;
-  { k_chunk_sums<<<(unsigned)chunks, 256, 0, s>>>(dpsi.as<double>(), D, sums.as<double>()); note_launches(1); }
-  std::vector<double> hs(chunks);
-  SED_TRY_CUDA(cudaMemcpyAsync(hs.data(), sums.ptr, chunks * 8, cudaMemcpyDeviceToHost, s));
+  { k_chunk_sums<<<(unsigned)chunks, 256, 0, s>>>(dpsi.as<double>(), b.reps.as<uint64_t>(), D, sign_mask, sums.as<double>()); note_launches(1); }
+  std::vector<double> hs(2 * chunks);
+  SED_TRY_CUDA(cudaMemcpyAsync(hs.data(), sums.ptr, 2 * chunks * 8, cudaMemcpyDeviceToHost, s));
   SED_TRY_CUDA(cudaStreamSynchronize(s));
-  double total = 0.0;
+  double total = 0.0, agree = 0.0;
   for (uint64_t c = 0; c < chunks; ++c) {
     double const t = hs[c];
     hs[c] = total;
     total += t;
+    agree += hs[chunks + c];
   }
+  hs.resize(chunks);
+  double const sign = agree < 0.0 ? -1.0 : 1.0;
   if (!(total > 0.0) || !std::isfinite(total))
     return fail(LS_INVALID_ARGUMENT, "sed_mlp_sample: psi has no finite nonzero weight");
   SED_TRY_CUDA(cudaMemcpyAsync(offs.ptr, hs.data(), chunks * 8, cudaMemcpyHostToDevice, s));
@@ -618,7 +941,7 @@ int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, ui
   double last = 0.0;
   SED_TRY_CUDA(cudaMemcpyAsync(&last, prefix.as<double>() + (D - 1), 8, cudaMemcpyDeviceToHost, s));
   SED_TRY_CUDA(cudaStreamSynchronize(s));
-  { k_draw<<<blocks_for((int64_t)n), 256, 0, s>>>(prefix.as<double>(), D, last, n, seed, dpsi.as<double>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>(), (double)b.plan.group_order, os.as<uint64_t>(), oa.as<float>(), og.as<float>()); note_launches(1); }
+  { k_draw<<<blocks_for((int64_t)n), 256, 0, s>>>(prefix.as<double>(), D, last, n, seed, sign, dpsi.as<double>(), b.reps.as<uint64_t>(), b.weights.as<uint32_t>(), (double)b.plan.group_order, os.as<uint64_t>(), oa.as<float>(), og.as<float>()); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   SED_TRY_CUDA(cudaMemcpyAsync(states, os.ptr, n * 8, cudaMemcpyDefault, s));
   SED_TRY_CUDA(cudaMemcpyAsync(t_abs, oa.ptr, n * 4, cudaMemcpyDefault, s));
@@ -639,10 +962,14 @@ int sed_mlp_start_vector(sed_mlp* m, ls_spin_basis const* basis, double* out) {
   DeviceBuffer amp, part, vout;
   if (int st = amp.allocate(D * 8)) return st;  // (a, s) pairs
   if (int st = part.allocate(152 * 16 * 4)) return st;
-  for (uint64_t b0 = 0; b0 < D; b0 += chunk) {
-    uint64_t const nb = std::min(chunk, D - b0);
-    if (int st = forward(d, b.reps.as<uint64_t>() + b0, nb, false)) return st;
-    SED_TRY_CUDA(cudaMemcpyAsync(amp.as<float>() + 2 * b0, d.out.ptr, nb * 8, cudaMemcpyDeviceToDevice, d.stream));
+  if (tc_eligible(d)) {
+    if (int st = forward_tc(d, b.reps.as<uint64_t>(), D, amp.as<float>())) return st;
+  } else {
+    for (uint64_t b0 = 0; b0 < D; b0 += chunk) {
+      uint64_t const nb = std::min(chunk, D - b0);
+      if (int st = forward(d, b.reps.as<uint64_t>() + b0, nb, false)) return st;
+      SED_TRY_CUDA(cudaMemcpyAsync(amp.as<float>() + 2 * b0, d.out.ptr, nb * 8, cudaMemcpyDeviceToDevice, d.stream));
+    }
   }
   unsigned const lb = blocks_for((int64_t)D);
   { k_max_first<<<lb, 256, 0, d.stream>>>(amp.as<float>(), (int64_t)D, part.as<float>()); note_launches(1); }

@@ -40,12 +40,13 @@ class Samples:
                        np.concatenate([p.t_sign for p in parts]))
 
 
-def sample(basis: Basis, psi, n: int, seed: int = 0) -> Samples:
-    """n representatives drawn with probability psi_r^2 (psi real, host or device)."""
+def sample(basis: Basis, psi, n: int, seed: int = 0, sign_mask: int = 0) -> Samples:
+    """n representatives drawn with probability psi_r^2 (psi real, host or
+    device); psi's global sign is fixed against the sign prior of sign_mask."""
     if isinstance(psi, np.ndarray):
         psi = np.ascontiguousarray(psi, dtype=np.float64)
     out = Samples(np.zeros(n, np.uint64), np.zeros(n, np.float32), np.zeros(n, np.float32))
-    check_status(L.load().sed_mlp_sample(basis.ptr, _ptr(psi), n, seed, _ptr(out.states), _ptr(out.t_abs),
+    check_status(L.load().sed_mlp_sample(basis.ptr, _ptr(psi), n, seed, sign_mask, _ptr(out.states), _ptr(out.t_abs),
                                          _ptr(out.t_sign)))
     return out
 
@@ -82,6 +83,15 @@ class Mlp(_Handle):
             out[name] = p[o:o + k].reshape(shp)
             o += k
         return out
+
+    def set_path(self, path: int) -> None:
+        """L.SED_MLP_PATH_AUTO (tensor cores where the shape allows) or
+        L.SED_MLP_PATH_SIMT (CUDA cores, FP32 activations)."""
+        check_status(L.load().sed_mlp_set_path(self.ptr, path))
+
+    @property
+    def uses_tensor_cores(self) -> bool:
+        return bool(L.load().sed_mlp_uses_tensor_cores(self.ptr))
 
     def forward(self, states: np.ndarray) -> np.ndarray:
         states = np.ascontiguousarray(states, dtype=np.uint64)

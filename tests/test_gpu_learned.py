@@ -23,8 +23,10 @@ def _random_states(rng, n, N):
 
 @pytest.mark.parametrize("n,h", [(20, 64), (36, 512)])
 def test_forward_matches_oracle(n, h):
+    from spined import _lib as L
     rng = np.random.default_rng(n)
     net = _net(n, h)
+    net.set_path(L.SED_MLP_PATH_SIMT)  # the CUDA-core path training uses
     p = net.get_params()
     p[h * n:h * n + h] = rng.normal(scale=0.1, size=h)  # nonzero biases
     net.set_params(p)
@@ -33,6 +35,49 @@ def test_forward_matches_oracle(n, h):
     _, _, _, want = M.forward(p, n, h, st)
     # FP32 accumulation of up to 512 BF16 x FP32 products against FP64
     np.testing.assert_allclose(got, want, rtol=0, atol=2e-5 * max(1.0, np.abs(want).max()))
+
+
+@pytest.mark.parametrize("n,h,count", [(36, 512, 3000), (20, 256, 129), (64, 128, 77), (24, 512, 1 << 15)])
+def test_tensor_core_forward_matches_oracle(n, h, count):
+    """The fused tcgen05 inference kernel against the FP64 oracle with h1
+    rounded to BF16 as the kernel stores it; ragged last tiles included.
+    Tolerance: the hardware tanh (relative error about 2^-11) and FP32
+    accumulation in tensor memory, 4e-3 of the output scale."""
+    rng = np.random.default_rng(count)
+    net = _net(n, h, seed=count)
+    assert net.uses_tensor_cores
+    p = net.get_params()
+    p[h * n:h * n + h] = rng.normal(scale=0.1, size=h)  # nonzero biases
+    p[h * n + h + h * h:h * n + 2 * h + h * h] = rng.normal(scale=0.1, size=h)
+    net.set_params(p)
+    st = _random_states(rng, n, count)
+    got = net.forward(st)
+    _, _, _, want = M.forward(p, n, h, st, act_bf16=True)
+    scale = max(1.0, np.abs(want).max())
+    np.testing.assert_allclose(got, want, rtol=0, atol=4e-3 * scale)
+    # and against the CUDA-core path (FP32 activations) to the same bound
+    from spined import _lib as L
+    net.set_path(L.SED_MLP_PATH_SIMT)
+    assert not net.uses_tensor_cores
+    np.testing.assert_allclose(got, net.forward(st), rtol=0, atol=4e-3 * scale)
+    assert net.forward(st[:0]).shape == (0, 2)
+
+
+def test_tensor_core_start_vector_matches_simt():
+    """sed_mlp_start_vector over a built basis: the tensor-core inference and
+    the CUDA-core path give the same vector up to the activation rounding."""
+    from spined import _lib as L
+    from spined.learned import Mlp
+    b = build_model(lattices.heisenberg_chain(20))
+    net = Mlp(20, 256, sign_mask=lattices.chain_sublattice_mask(20), seed=8)
+    p = net.get_params()
+    net.set_params(0.5 * p)  # small outputs: exp(a) stays well conditioned
+    v_tc = net.start_vector(b.basis)
+    net.set_path(L.SED_MLP_PATH_SIMT)
+    v_simt = net.start_vector(b.basis)
+    # signs come from the sign logit: they may differ only where it is ~0
+    assert np.mean(np.sign(v_tc) != np.sign(v_simt)) < 1e-3
+    np.testing.assert_allclose(np.abs(v_tc), np.abs(v_simt), rtol=2e-2, atol=1e-3 * np.abs(v_simt).max())
 
 
 @pytest.mark.parametrize("n,h,mask", [(16, 64, 0), (36, 512, lattices.square_sublattice_mask(6))])
@@ -85,7 +130,17 @@ def test_sampler_labels_and_frequencies(sed):
     idx = np.searchsorted(reps, s.states)
     assert np.all(reps[idx] == s.states)
     np.testing.assert_allclose(s.t_abs, np.log(np.abs(psi[idx]) * norms[idx]), rtol=0, atol=1e-5)
-    np.testing.assert_array_equal(s.t_sign, (psi[idx] > 0).astype(np.float32))
+    sigma = 1.0 if np.sum(psi * np.abs(psi)) >= 0 else -1.0  # global sign fixed (sign_mask 0)
+    np.testing.assert_array_equal(s.t_sign, (sigma * psi[idx] > 0).astype(np.float32))
+    # -psi is the same eigenvector: same samples, same labels
+    s_neg = sample(b.basis, -psi, 1000, seed=9)
+    np.testing.assert_array_equal(s_neg.t_sign, s.t_sign[:1000])
+    # with a sublattice sign prior the sign is fixed against the prior
+    mask = lattices.chain_sublattice_mask(16)
+    prior = np.array([(-1) ** bin(int(r) & mask).count("1") for r in reps])
+    sig_m = 1.0 if np.sum(prior * psi * np.abs(psi)) >= 0 else -1.0
+    s_m = sample(b.basis, -psi, 1000, seed=9, sign_mask=mask)
+    np.testing.assert_array_equal(s_m.t_sign, (sig_m * psi[idx[:1000]] > 0).astype(np.float32))
     # frequencies against psi^2: every representative within 5 sigma
     p = psi ** 2 / np.sum(psi ** 2)
     counts = np.bincount(idx, minlength=len(reps))
@@ -106,7 +161,8 @@ def test_learned_start_beats_random_start(sed):
     for k, j2 in enumerate([0.0, 0.1, 0.2]):
         b = build_model(lattices.heisenberg_chain(n, j2=j2))
         r = sed.eigh(b.hamiltonian)
-        parts.append(sample(b.basis, r.eigenvectors[:, 0], 1 << 16, seed=k))
+        parts.append(sample(b.basis, r.eigenvectors[:, 0], 1 << 16, seed=k,
+                            sign_mask=lattices.chain_sublattice_mask(n)))
     data = Samples.concat(parts)
     net = Mlp(n, 128, sign_mask=lattices.chain_sublattice_mask(n), seed=5)
     net.train(data, epochs=30, batch=2048, lr=2e-3, seed=2)
