@@ -264,6 +264,36 @@ SED_API int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, u
                                              uint64_t block_size, void const* x, uint64_t x_stride,
                                              void* y, uint64_t y_stride, void* out);
 
+/* Many Hamiltonians in one persistent launch. No counterpart in the
+ * reference, which solves one operator per run. The lowest opts->nev (<= 4)
+ * eigenpairs of every operator by block Lanczos with block size 4 in FP64
+ * (opts->block_size 0 or 4; opts->max_basis / 4 stored blocks per cycle, at
+ * most 16, default 12; opts->tol; opts->seed; opts->max_iter bounds the
+ * matvec columns per problem). All operators must be real, built and on the
+ * current device; their stream forms are recorded if needed. One cooperative
+ * kernel solves all of them: its CTAs form groups, one problem per group at a
+ * time, with CTAs given in proportion to each problem's work; the launch
+ * shape (CTAs per SM) is picked by timing short trial runs on the first call
+ * for a given set of sizes (cached afterwards). eigenvalues and residuals are
+ * count x nev host arrays (row i for operator i; residuals may be NULL);
+ * eigenvectors[i] (host or device, may be NULL, or the array itself NULL) is
+ * D_i x nev column-major with stride ldv[i] (ldv NULL: D_i). */
+typedef struct sed_batch_info {
+  uint64_t block_steps_max;  /* block Lanczos steps of the slowest problem */
+  uint64_t restarts_max;
+  double seconds_total;
+  double seconds_setup;      /* stream-form recording */
+  double seconds_solve;      /* the persistent launch and the result copies */
+  double kernel_ms;          /* CUDA-event time of the persistent launch */
+  uint32_t grid;             /* CTAs available to the launch */
+  uint32_t ctas_per_sm;
+  uint32_t threads_per_cta;
+  uint32_t reserved;
+} sed_batch_info;
+SED_API int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options const* opts,
+                             double* eigenvalues, double* residuals, void* const eigenvectors[],
+                             uint64_t const ldv[], sed_batch_info* info);
+
 /* Norms ||P r|| = sqrt(S / |G|) of the representatives (host array). */
 SED_API int sed_basis_get_norms(ls_spin_basis const* basis, double* out);
 /* Device pointer to the representatives (valid while the basis lives). */

@@ -1,0 +1,1088 @@
+// batch.cu — many Hamiltonians of uneven size solved in one persistent launch
+// (sed_eigh_batched): the lowest nev <= 4 eigenpairs of every operator by
+// block Lanczos with block size 4 in FP64.
+//
+// One cooperative kernel runs the whole solve for all problems. Its CTAs are
+// split into groups; a group owns one problem at a time (several small
+// problems are queued on one group when there are more problems than CTAs)
+// and synchronises through a bounded barrier in global memory. Within a
+// group the rows of the problem are split by SELL-32 slices.
+//
+// Per problem, with Krylov blocks V_j stored row-interleaved ([D][4], so the
+// SpMV gathers one 32-byte sector per element for all four columns):
+//   V_0 = QR(start block)                                  (CholQR2)
+//   W = H V_j ; C_i = V_i^T W, W -= V_i C_i for i <= j      (CGS2, two passes)
+//   W = V_{j+1} B_j                                          (CholQR2)
+//   T: diagonal blocks A_j = sym(C_j), sub-diagonal blocks B_j
+// Every `rr_every` steps (and at the end of a cycle) the group's first CTA
+// diagonalises T (cyclic Jacobi with parallel round-robin rotations in shared
+// memory) and estimates the Ritz residuals ||B_j y_last||; the cycle ends when
+// all nev estimates are below tol / 2 or the basis is full. Ritz vectors
+// Psi = V Y are then formed, their true residuals ||H psi - theta psi|| are
+// computed, and the problem is done when all are below tol; otherwise block
+// Lanczos restarts from Psi.
+//
+// Cross-CTA data (partial sums, T, decisions, the gathered x of the SpMV) is
+// read with ld.global.cg so that no stale L1 line is used after a barrier.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <mutex>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+#include "operator_impl.cuh"
+#include "tc.cuh"
+
+namespace sed {
+namespace {
+
+constexpr int kB = 4;               // block size
+constexpr int kMaxBlocks = 16;      // stored Krylov blocks per cycle (n <= 64)
+constexpr int kMaxN = kB * kMaxBlocks;
+constexpr int kPart = 16 * (kMaxBlocks + 1);  // partial sums per CTA and slot
+constexpr uint64_t kBarrierNs = 20000000000ull;  // 20 s per barrier: far beyond any phase
+constexpr size_t kStatsOff = 12 * 8;                // per-problem output record: out[12], stats[4], flag[4]
+constexpr size_t kOutBytes = kStatsOff + 32;
+
+struct ChainDesc {
+  StreamView S;       // real operator, FP64 stream form
+  uint64_t D, n_slices;
+  double* V;          // (m_blocks + 1) blocks of [D][4]
+  double* W;          // [D][4]
+  double* part;       // [2][ncta][kPart]
+  double* W2;         // [D][4] second scratch block (thick restart)
+  double* Tc;         // [kMaxBlocks][kMaxN * 4]: step j's projections C_i = V_i^T H V_j, i <= j
+  double* Bblk;       // [kMaxBlocks][16] sub-diagonal blocks (upper triangular)
+  double* Y;          // [kMaxN][8] Ritz vectors of T (row q, column i)
+  double* out;        // theta[8], residual[4]
+  uint32_t* stats;    // block steps, restarts, matvecs, status (0 running, 1 done, 2 not converged, 3 breakdown)
+  uint32_t* flag;     // [4]: decision words written by the leader CTA
+  uint32_t m_blocks;
+  uint32_t nev;
+  uint32_t packed;    // stream entries hold col | code << col_bits
+  uint64_t seed;
+};
+
+struct GroupDesc {
+  uint32_t cta0, ncta, first, count;  // CTAs [cta0, cta0 + ncta); chains order[first .. first + count)
+  uint32_t* bar;                      // [2]: arrivals, generation
+};
+
+struct BatchArgs {
+  ChainDesc const* chains;
+  GroupDesc const* groups;
+  uint32_t const* cta_group;
+  uint32_t const* order;
+  double tol;
+  uint32_t max_steps;     // block steps per problem in total
+  uint32_t rr_every;
+  int* error;
+};
+
+// One row of a [D][4] block (32 bytes, one sector).
+struct alignas(32) Row4 {
+  double x, y, z, w;
+};
+__device__ __forceinline__ Row4 mk4(double a, double b, double c, double d) { return Row4{a, b, c, d}; }
+
+__device__ __forceinline__ double ldcg(double const* p) { return __ldcg(p); }
+__device__ __forceinline__ uint32_t ldcg(uint32_t const* p) { return __ldcg(p); }
+__device__ __forceinline__ Row4 ldcg4(double const* p) {
+  double2 const a = __ldcg(reinterpret_cast<double2 const*>(p));
+  double2 const b = __ldcg(reinterpret_cast<double2 const*>(p) + 1);
+  return mk4(a.x, a.y, b.x, b.y);
+}
+
+// Bounded barrier of the `n` CTAs of a group; false (and *error = 2) if it
+// timed out. Every thread of the CTA must call it.
+__device__ bool group_barrier(uint32_t* bar, uint32_t n, int* error) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    if (n > 1) {
+      volatile uint32_t* gen = bar + 1;
+      uint32_t const g = *gen;
+      __threadfence();
+      if (atomicAdd(bar, 1u) == n - 1) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        atomicAdd(bar + 1, 1u);
+      } else {
+        uint64_t const t0 = tc::global_ns();
+        while (*gen == g) {
+          if (tc::global_ns() - t0 > kBarrierNs) {
+            ok = 0;
+            atomicExch(error, 2);
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
+    }
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// Sums K per-thread values over the CTA; thread k < K of the CTA gets total k
+// in out[k] (shared). red: [warps][K] shared scratch.
+template <int K>
+__device__ __forceinline__ void cta_sum(double (&v)[K], double* red, double* out) {
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp * K + k] = x;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < K) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += red[w * K + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+struct Ctx {
+  ChainDesc const& c;
+  uint32_t rank, ncta;
+  uint32_t* bar;
+  int* error;
+  uint64_t r0, r1;      // own rows
+  uint64_t s0, s1;      // own slices
+  uint32_t slot;        // partial-sum double buffer
+  double* red;          // shared [warps][16]
+  double* tmp;          // shared [kPart]
+};
+
+// Publishes this CTA's K partial sums (in shared `local`), waits for the group
+// and leaves the group totals in shared `total` (same order on every CTA).
+__device__ bool group_sum(Ctx& x, double const* local, int K, double* total) {
+  double* mine = x.c.part + ((size_t)x.slot * x.ncta + x.rank) * kPart;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) mine[k] = local[k];
+  __threadfence();
+  if (!group_barrier(x.bar, x.ncta, x.error)) return false;
+  double const* all = x.c.part + (size_t)x.slot * x.ncta * kPart;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double s = 0.0;
+    for (uint32_t r = 0; r < x.ncta; ++r) s += ldcg(all + (size_t)r * kPart + k);
+    total[k] = s;
+  }
+  x.slot ^= 1u;
+  __syncthreads();
+  return true;
+}
+
+// Cholesky of the 4x4 Gram matrix G (row-major) -> upper R with G = R^T R.
+// Returns false on a pivot below eps * trace (rank deficiency).
+__device__ bool chol4(double const* G, double* R) {
+  double const tr = G[0] + G[5] + G[10] + G[15];
+  for (int i = 0; i < 16; ++i) R[i] = 0.0;
+  for (int j = 0; j < 4; ++j) {
+    double d = G[j * 4 + j];
+    for (int k = 0; k < j; ++k) d -= R[k * 4 + j] * R[k * 4 + j];
+    if (!(d > 1e-24 * tr) || !(tr > 0.0)) return false;
+    double const rjj = sqrt(d);
+    R[j * 4 + j] = rjj;
+    for (int i = j + 1; i < 4; ++i) {
+      double s = G[j * 4 + i];
+      for (int k = 0; k < j; ++k) s -= R[k * 4 + j] * R[k * 4 + i];
+      R[j * 4 + i] = s / rjj;
+    }
+  }
+  return true;
+}
+
+// In place X <- X R^{-1} on own rows (X = [D][4]); y R = x by forward
+// substitution.
+__device__ void apply_rinv(Ctx& x, double* X, double const* R) {
+  for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+    Row4 const v = *reinterpret_cast<Row4 const*>(X + r * 4);
+    double const a[4] = {v.x, v.y, v.z, v.w};
+    double y[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      double s = a[j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) s -= y[k] * R[k * 4 + j];
+      y[j] = s / R[j * 4 + j];
+    }
+    *reinterpret_cast<Row4*>(X + r * 4) = mk4(y[0], y[1], y[2], y[3]);
+  }
+}
+
+// CholQR2 of the block X in place; Rtot (shared, 16) = R2 R1. false on
+// breakdown or barrier failure (ok distinguishes them).
+__device__ bool block_qr(Ctx& x, double* X, double* Rtot, bool& ok) {
+  __shared__ double G[16], R[16], P[16];
+  ok = true;
+  for (int pass = 0; pass < 2; ++pass) {
+    double g[10] = {};
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      Row4 const v = *reinterpret_cast<Row4 const*>(X + r * 4);
+      double const a[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i; j < 4; ++j) {
+          int const q = i * 4 - i * (i - 1) / 2 + (j - i);  // packed upper triangle
+          g[q] = fma(a[i], a[j], g[q]);
+        }
+    }
+    cta_sum<10>(g, x.red, x.tmp);
+    if (!group_sum(x, x.tmp, 10, x.tmp + 16)) {
+      ok = false;
+      return false;
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 4; ++i)
+        for (int j = i; j < 4; ++j) {
+          int const q = i * 4 - i * (i - 1) / 2 + (j - i);
+          G[i * 4 + j] = G[j * 4 + i] = x.tmp[16 + q];
+        }
+    }
+    __syncthreads();
+    __shared__ int good;
+    if (threadIdx.x == 0) good = chol4(G, R) ? 1 : 0;
+    __syncthreads();
+    if (!good) return false;
+    apply_rinv(x, X, R);
+    if (threadIdx.x == 0) {
+      if (pass == 0) {
+        for (int i = 0; i < 16; ++i) Rtot[i] = R[i];
+      } else {  // Rtot = R2 * R1
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += R[i * 4 + k] * Rtot[k * 4 + j];
+            P[i * 4 + j] = s;
+          }
+        for (int i = 0; i < 16; ++i) Rtot[i] = P[i];
+      }
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// W = H X on own rows (X, W: [D][4]); gathers of X go through L2.
+__device__ void block_spmv(Ctx& x, double const* X, double* W) {
+  StreamView const& S = x.c.S;
+  uint32_t const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t const col_mask = S.col_bits < 32 ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
+  bool const packed = x.c.packed != 0;
+  double const* table = static_cast<double const*>(S.table);
+  for (uint64_t s = x.s0 + warp; s < x.s1; s += nw) {
+    uint64_t const base = S.slice_ptr[s];
+    uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    uint32_t const* ent = S.entries + base + lane;
+    for (uint32_t e = 0; e < width; ++e) {
+      uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
+      if (v != kNull) {
+        uint32_t const col = v & col_mask;
+        uint32_t const code = packed ? (v >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)e * 32);
+        double const t = __ldg(table + code);
+        Row4 const xv = ldcg4(X + (uint64_t)col * 4);
+        a0 = fma(t, xv.x, a0);
+        a1 = fma(t, xv.y, a1);
+        a2 = fma(t, xv.z, a2);
+        a3 = fma(t, xv.w, a3);
+      }
+    }
+    uint64_t const i = s * 32 + lane;
+    if (i < x.c.D) {
+      double const f = S.inv_sqrt_s[S.row_class[i]];
+      double const dg = static_cast<double const*>(S.diag)[i];
+      Row4 const xi = ldcg4(X + i * 4);
+      *reinterpret_cast<Row4*>(W + i * 4) =
+          mk4(fma(f, a0, dg * xi.x), fma(f, a1, dg * xi.y), fma(f, a2, dg * xi.z), fma(f, a3, dg * xi.w));
+    }
+  }
+}
+
+// X -= sum_{i<nb} V_i C_i (two passes of classical Gram-Schmidt). C (shared,
+// nb * 16, row-major a*4+c per block, may be null) receives the summed
+// coefficients; norms2 (shared, may be null) the squared column norms of X
+// before the projection.
+__device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2) {
+  double const* V = x.c.V;
+  uint64_t const D = x.c.D;
+  int const K = (int)nb * 16;
+  if (C)
+    for (int k = threadIdx.x; k < K; k += blockDim.x) C[k] = 0.0;
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    for (uint32_t i = 0; i < nb; ++i) {
+      double p[16] = {};
+      double const* Vi = V + (uint64_t)i * D * 4;
+      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+        Row4 const a = *reinterpret_cast<Row4 const*>(Vi + r * 4);
+        Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
+        double const av[4] = {a.x, a.y, a.z, a.w}, wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+#pragma unroll
+          for (int t = 0; t < 4; ++t) p[s * 4 + t] = fma(av[s], wv[t], p[s * 4 + t]);
+      }
+      cta_sum<16>(p, x.red, x.tmp + 16 * i);
+    }
+    int Kp = K;
+    if (pass == 0 && norms2) {
+      double q[4] = {};
+      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+        Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
+        q[0] = fma(w.x, w.x, q[0]);
+        q[1] = fma(w.y, w.y, q[1]);
+        q[2] = fma(w.z, w.z, q[2]);
+        q[3] = fma(w.w, w.w, q[3]);
+      }
+      cta_sum<4>(q, x.red, x.tmp + K);
+      Kp = K + 4;
+    }
+    double* tot = x.tmp + kPart;
+    if (!group_sum(x, x.tmp, Kp, tot)) return false;
+    if (C)
+      for (int k = threadIdx.x; k < K; k += blockDim.x) C[k] += tot[k];
+    if (Kp > K && threadIdx.x < 4) norms2[threadIdx.x] = tot[K + threadIdx.x];
+    // X -= sum_i V_i tot_i
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      Row4 w = *reinterpret_cast<Row4 const*>(X + r * 4);
+      for (uint32_t i = 0; i < nb; ++i) {
+        Row4 const a = *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4);
+        double const* c = tot + 16 * i;
+        w.x -= a.x * c[0] + a.y * c[4] + a.z * c[8] + a.w * c[12];
+        w.y -= a.x * c[1] + a.y * c[5] + a.z * c[9] + a.w * c[13];
+        w.z -= a.x * c[2] + a.y * c[6] + a.z * c[10] + a.w * c[14];
+        w.w -= a.x * c[3] + a.y * c[7] + a.z * c[11] + a.w * c[15];
+      }
+      *reinterpret_cast<Row4*>(X + r * 4) = w;
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// QR of the new Krylov block X (already projected against V_0 .. V_{nb-1})
+// with deflation: a column whose norm fell below 1e-10 of its norm before the
+// projection (norms2), or that is numerically dependent on the others, means
+// the block Krylov space lost a direction there (typically a converged Ritz
+// vector of the restart block). Such columns are replaced by random vectors,
+// projected against the basis, and the block is factored by CholQR2. Rb gets
+// R with the replaced columns zeroed (their coupling to H V_j is below the
+// threshold). Returns false on barrier failure or if the replacement fails.
+__device__ bool lanczos_qr(Ctx& x, double* X, uint32_t nb, double* norms2, double* Rb, uint32_t step) {
+  __shared__ double R[16];
+  __shared__ int mask_s, total_mask_s;
+  if (threadIdx.x == 0) total_mask_s = 0;
+  __syncthreads();
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    double g[4] = {};
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      Row4 const v = *reinterpret_cast<Row4 const*>(X + r * 4);
+      g[0] = fma(v.x, v.x, g[0]);
+      g[1] = fma(v.y, v.y, g[1]);
+      g[2] = fma(v.z, v.z, g[2]);
+      g[3] = fma(v.w, v.w, g[3]);
+    }
+    cta_sum<4>(g, x.red, x.tmp);
+    if (!group_sum(x, x.tmp, 4, x.tmp + 16)) return false;
+    if (threadIdx.x == 0) {
+      int m = 0;
+      for (int c = 0; c < 4; ++c)
+        if (!(x.tmp[16 + c] > 1e-20 * norms2[c])) m |= 1 << c;
+      mask_s = m;
+      total_mask_s |= m;
+    }
+    __syncthreads();
+    int const m = mask_s;
+    if (m == 0) break;
+    if (attempt == 2) return false;
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      uint32_t cnt[4] = {(uint32_t)r, (uint32_t)(r >> 32), 0xDEF1u + step, (uint32_t)attempt};
+      philox(cnt, (uint32_t)x.c.seed, (uint32_t)(x.c.seed >> 32));
+      double* row = X + r * 4;
+      for (int c = 0; c < 4; ++c)
+        if (m & (1 << c)) row[c] = 2.0 * ((double)cnt[c] * (1.0 / 4294967296.0)) - 1.0;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && (m & (1 << threadIdx.x))) norms2[threadIdx.x] = (double)x.c.D;
+    __syncthreads();
+    if (!cgs2(x, X, nb, nullptr, nullptr)) return false;
+  }
+  bool ok;
+  if (!block_qr(x, X, R, ok)) return false;  // dependent columns that are not small: a breakdown
+  if (threadIdx.x < 16) {
+    int const col = threadIdx.x & 3;
+    Rb[threadIdx.x] = (total_mask_s & (1 << col)) ? 0.0 : R[threadIdx.x];
+  }
+  __syncthreads();
+  return true;
+}
+
+// Cyclic Jacobi on the symmetric n x n matrix A (shared, row-major, n even)
+// with parallel round-robin rotations; Q (shared) receives the eigenvectors
+// as columns. Eigenvalues end on the diagonal of A.
+__device__ void jacobi(double* A, double* Q, int n) {
+  __shared__ double cs[kMaxN / 2][2];
+  __shared__ int pp[kMaxN / 2][2];
+  __shared__ int done;
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) Q[k] = (k / n == k % n) ? 1.0 : 0.0;
+  __syncthreads();
+  int const half = n / 2;
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    if (threadIdx.x == 0) {
+      double off = 0.0, dia = 0.0;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          if (i == j) dia += A[i * n + j] * A[i * n + j];
+          else off += A[i * n + j] * A[i * n + j];
+        }
+      done = off <= 1e-30 * dia || off == 0.0;
+    }
+    __syncthreads();
+    if (done) break;
+    for (int round = 0; round < n - 1; ++round) {
+      // round-robin pairing: player 0 fixed, the others rotate
+      if ((int)threadIdx.x < half) {
+        int const k = threadIdx.x;
+        auto pos = [&](int q) { return q == 0 ? 0 : 1 + ((q - 1 + round) % (n - 1)); };
+        int p = pos(k), q = pos(n - 1 - k);
+        if (p > q) {
+          int const t = p;
+          p = q;
+          q = t;
+        }
+        double const apq = A[p * n + q];
+        double c = 1.0, s = 0.0;
+        if (apq != 0.0) {
+          double const tau = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+          double const t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+          c = 1.0 / sqrt(1.0 + t * t);
+          s = t * c;
+        }
+        cs[k][0] = c;
+        cs[k][1] = s;
+        pp[k][0] = p;
+        pp[k][1] = q;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int e = threadIdx.x; e < half * n; e += blockDim.x) {
+        int const k = e / n, col = e % n;
+        int const p = pp[k][0], q = pp[k][1];
+        double const c = cs[k][0], s = cs[k][1];
+        double const ap = A[p * n + col], aq = A[q * n + col];
+        A[p * n + col] = c * ap - s * aq;
+        A[q * n + col] = s * ap + c * aq;
+      }
+      __syncthreads();
+      // columns: A <- A J, Q <- Q J
+      for (int e = threadIdx.x; e < half * n; e += blockDim.x) {
+        int const k = e / n, row = e % n;
+        int const p = pp[k][0], q = pp[k][1];
+        double const c = cs[k][0], s = cs[k][1];
+        double const ap = A[row * n + p], aq = A[row * n + q];
+        A[row * n + p] = c * ap - s * aq;
+        A[row * n + q] = s * ap + c * aq;
+        double const qp = Q[row * n + p], qq = Q[row * n + q];
+        Q[row * n + p] = c * qp - s * qq;
+        Q[row * n + q] = s * qp + c * qq;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Rayleigh-Ritz of T (n = 4 (j + 1)) by the leader CTA. T is assembled from
+// the projections of every step (T[block p][block q] = C_p of step q for
+// p <= q), which also covers the arrowhead couplings after a thick restart.
+// The lowest min(8, n) Ritz values go to c.out[0..8), their vectors to c.Y,
+// the residual estimates ||B_j y_last|| of the lowest four to c.out[8..12).
+// Returns the largest estimate over the nev wanted pairs.
+__device__ double rayleigh_ritz(ChainDesc const& c, uint32_t j, bool have_B, double* A, double* Q) {
+  int const n = 4 * (int)(j + 1);
+  constexpr int kStride = kMaxN * 4;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int const r = e / n, q = e % n;
+    int const br = r / 4, bq = q / 4, a = r % 4, b = q % 4;
+    double v;
+    if (br == bq)
+      v = 0.5 * (ldcg(c.Tc + bq * kStride + br * 16 + a * 4 + b) + ldcg(c.Tc + bq * kStride + br * 16 + b * 4 + a));
+    else if (br < bq)
+      v = ldcg(c.Tc + bq * kStride + br * 16 + a * 4 + b);
+    else
+      v = ldcg(c.Tc + br * kStride + bq * 16 + b * 4 + a);
+    A[e] = v;
+  }
+  __syncthreads();
+  jacobi(A, Q, n);
+  __shared__ int idx[8];
+  __shared__ double worst;
+  int const nk = n < 8 ? n : 8;
+  if (threadIdx.x == 0) {
+    // selection of the nk smallest diagonal entries, ascending
+    bool used[kMaxN] = {};
+    for (int i = 0; i < nk; ++i) {
+      int best = -1;
+      for (int q = 0; q < n; ++q)
+        if (!used[q] && (best < 0 || A[q * n + q] < A[best * n + best])) best = q;
+      used[best] = true;
+      idx[i] = best;
+      c.out[i] = A[best * n + best];
+    }
+    worst = 0.0;
+    for (int i = 0; i < kB; ++i) {
+      double r2 = 0.0;
+      if (have_B) {
+        for (int a = 0; a < 4; ++a) {
+          double s = 0.0;
+          for (int b = 0; b < 4; ++b) s += ldcg(c.Bblk + j * 16 + a * 4 + b) * Q[(4 * (int)j + b) * n + idx[i]];
+          r2 += s * s;
+        }
+      }
+      c.out[8 + i] = sqrt(r2);
+      if (i < (int)c.nev) worst = fmax(worst, sqrt(r2));
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * 8; e += blockDim.x) {
+    int const q = e / 8, i = e % 8;
+    c.Y[q * 8 + i] = i < nk ? Q[q * n + idx[i]] : 0.0;
+  }
+  __syncthreads();
+  return worst;
+}
+
+// Ritz vectors Psi = V Y over the basis blocks 0..j (own rows): the lowest
+// four into W, the next four into W2 when `both`.
+__device__ void ritz_vectors(Ctx& x, uint32_t j, double* Ys, bool both) {
+  int const n = 4 * (int)(j + 1);
+  for (int e = threadIdx.x; e < n * 8; e += blockDim.x) Ys[e] = ldcg(x.c.Y + e);
+  __syncthreads();
+  uint64_t const D = x.c.D;
+  for (int half = 0; half < (both ? 2 : 1); ++half) {
+    double* out = half ? x.c.W2 : x.c.W;
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      double o[4] = {};
+      for (int b = 0; b <= (int)j; ++b) {
+        Row4 const a = *reinterpret_cast<Row4 const*>(x.c.V + (uint64_t)b * D * 4 + r * 4);
+        double const av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) o[i] = fma(av[s], Ys[(4 * b + s) * 8 + 4 * half + i], o[i]);
+      }
+      *reinterpret_cast<Row4*>(out + r * 4) = mk4(o[0], o[1], o[2], o[3]);
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void copy_block(Ctx& x, double* dst, double const* src) {
+  for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x)
+    *reinterpret_cast<Row4*>(dst + r * 4) = *reinterpret_cast<Row4 const*>(src + r * 4);
+  __syncthreads();
+}
+
+__device__ void random_block(Ctx& x) {
+  for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+    uint32_t c[4] = {(uint32_t)r, (uint32_t)(r >> 32), 0xB10Cu, 0u};
+    philox(c, (uint32_t)x.c.seed, (uint32_t)(x.c.seed >> 32));
+    double v[4];
+    for (int k = 0; k < 4; ++k) v[k] = 2.0 * ((double)c[k] * (1.0 / 4294967296.0)) - 1.0;
+    *reinterpret_cast<Row4*>(x.c.V + r * 4) = mk4(v[0], v[1], v[2], v[3]);
+  }
+  __syncthreads();
+}
+
+// Whole solve of one problem by the CTAs of its group. Cycles end when the
+// basis is full or the Ritz estimates converge; the lowest eight Ritz vectors
+// and the last Lanczos block then seed the next cycle (thick restart: T starts
+// as diag(theta_1..8) and the next step's projections supply the arrowhead
+// couplings), or, after a breakdown, the lowest four alone (explicit restart).
+__device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, uint32_t* bar, BatchArgs const& a,
+                            double* red, double* tmp, double* C, double* A, double* Q) {
+  Ctx x{c, rank, ncta, bar, a.error, 0, 0, 0, 0, 0, red, tmp};
+  x.s0 = c.n_slices * rank / ncta;
+  x.s1 = c.n_slices * (rank + 1) / ncta;
+  x.r0 = std::min<uint64_t>(c.D, x.s0 * 32);
+  x.r1 = std::min<uint64_t>(c.D, x.s1 * 32);
+  bool const leader = rank == 0;
+  constexpr int kStride = kMaxN * 4;
+  __shared__ double Rb[16], norms2[4];
+  uint32_t steps = 0, restarts = 0, matvecs = 0, status = 2;
+  double const tol = a.tol;
+  random_block(x);
+  bool qr_ok;
+  if (!block_qr(x, c.V, Rb, qr_ok)) {
+    if (!qr_ok) return;
+    status = 3;
+  }
+  uint32_t j0 = 0;
+  while (status != 3) {
+    uint32_t j = j0;
+    bool broke = false;
+    for (;; ++j) {
+      double* Vj = c.V + (uint64_t)j * c.D * 4;
+      if (!group_barrier(bar, ncta, a.error)) return;  // V_j complete on every CTA before the gathers
+      block_spmv(x, Vj, c.W);
+      ++matvecs;
+      __syncthreads();
+      if (!cgs2(x, c.W, j + 1, C, norms2)) return;
+      if (leader)
+        for (int k = threadIdx.x; k < 16 * (int)(j + 1); k += blockDim.x) c.Tc[j * kStride + k] = C[k];
+      ++steps;
+      // QR of W -> V_{j+1}, B_j (with deflation of lost directions)
+      double* Vn = c.V + (uint64_t)(j + 1) * c.D * 4;
+      copy_block(x, Vn, c.W);
+      broke = !lanczos_qr(x, Vn, j + 1, norms2, Rb, steps);
+      if (*(volatile int*)a.error) return;
+      if (leader)
+        for (int k = threadIdx.x; k < 16; k += blockDim.x) c.Bblk[j * 16 + k] = broke ? 0.0 : Rb[k];
+      bool const full = j + 1 >= c.m_blocks || steps >= a.max_steps || broke;
+      if (full || (j + 1) % a.rr_every == 0) {
+        __threadfence();
+        if (!group_barrier(bar, ncta, a.error)) return;  // T and B visible to the leader
+        if (leader) {
+          double const worst = rayleigh_ritz(c, j, !broke, A, Q);
+          if (threadIdx.x == 0) {
+            c.flag[0] = (worst <= 0.5 * tol) ? 1u : 0u;
+            __threadfence();
+          }
+        }
+        if (!group_barrier(bar, ncta, a.error)) return;
+        if (ldcg(c.flag) != 0u || full) break;
+      }
+    }
+    bool const thick = !broke && j >= 1 && c.m_blocks >= 3;
+    ritz_vectors(x, j, A, thick);  // A: the dynamic shared area, free outside the Jacobi solve
+    if (!group_barrier(bar, ncta, a.error)) return;  // every CTA done reading the old basis
+    if (thick && j + 1 != 2) copy_block(x, c.V + 2 * c.D * 4, c.V + (uint64_t)(j + 1) * c.D * 4);
+    copy_block(x, c.V, c.W);
+    if (thick) copy_block(x, c.V + c.D * 4, c.W2);
+    if (!group_barrier(bar, ncta, a.error)) return;  // Psi rows visible to every CTA's SpMV gathers
+    // true residuals of the lowest four Ritz pairs
+    block_spmv(x, c.V, c.W);
+    ++matvecs;
+    __syncthreads();
+    double th[8];
+    for (int i = 0; i < 8; ++i) th[i] = ldcg(c.out + i);
+    {
+      double p[4] = {};
+      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+        Row4 const w = *reinterpret_cast<Row4 const*>(c.W + r * 4);
+        Row4 const v = *reinterpret_cast<Row4 const*>(c.V + r * 4);
+        double const d[4] = {w.x - th[0] * v.x, w.y - th[1] * v.y, w.z - th[2] * v.z, w.w - th[3] * v.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) p[i] = fma(d[i], d[i], p[i]);
+      }
+      cta_sum<4>(p, red, tmp);
+      if (!group_sum(x, tmp, 4, tmp + 16)) return;
+    }
+    bool all = true;
+    for (uint32_t i = 0; i < c.nev; ++i) all = all && sqrt(tmp[16 + i]) <= tol;
+    __syncthreads();
+    if (leader && threadIdx.x == 0)
+      for (uint32_t i = 0; i < 4; ++i) c.out[8 + i] = sqrt(tmp[16 + i]);
+    if (all) {
+      status = 1;
+      break;
+    }
+    if (steps >= a.max_steps) break;
+    ++restarts;
+    if (thick) {
+      // T of the new cycle: diag(theta_1..8) on blocks 0 and 1
+      if (leader) {
+        for (int k = threadIdx.x; k < 2 * kStride; k += blockDim.x) c.Tc[k] = 0.0;
+        __syncthreads();
+        if (threadIdx.x < 8) {
+          int const i = threadIdx.x, b = i / 4, a4 = i % 4;
+          c.Tc[b * kStride + b * 16 + a4 * 4 + a4] = th[i];
+        }
+        __threadfence();
+      }
+      j0 = 2;
+    } else {
+      if (!block_qr(x, c.V, Rb, qr_ok)) {
+        if (!qr_ok) return;
+        status = 3;
+        break;
+      }
+      j0 = 0;
+    }
+  }
+  if (leader && threadIdx.x == 0) {
+    c.stats[0] = steps;
+    c.stats[1] = restarts;
+    c.stats[2] = matvecs;
+    c.stats[3] = status;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_batch_lanczos(BatchArgs a) {
+  __shared__ double red[8 * 16];
+  __shared__ double tmp[2 * kPart];
+  __shared__ double C[kPart];
+  extern __shared__ double dyn[];  // A [kMaxN^2], Q [kMaxN^2] (leader work)
+  uint32_t const gi = a.cta_group[blockIdx.x];
+  GroupDesc const g = a.groups[gi];
+  uint32_t const rank = blockIdx.x - g.cta0;
+  for (uint32_t q = 0; q < g.count; ++q) {
+    ChainDesc const& c = a.chains[a.order[g.first + q]];
+    solve_chain(c, rank, g.ncta, g.bar, a, red, tmp, C, dyn, dyn + kMaxN * kMaxN);
+    if (*(volatile int*)a.error) return;
+    if (!group_barrier(g.bar, g.ncta, a.error)) return;
+  }
+}
+
+// [D][4] block -> column-major D x nev with stride ld
+__global__ void k_unpack_block(double const* __restrict__ V, uint64_t D, uint32_t nev, double* __restrict__ out,
+                               uint64_t ld) {
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < D * nev; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t const i = e % D, c = e / D;
+    out[c * ld + i] = V[i * 4 + c];
+  }
+}
+
+// ------------------------------------------------------------ host side ---
+
+struct Plan {
+  unsigned threads = 256, ctas_per_sm = 1;
+};
+
+std::mutex g_tune_mu;
+std::map<std::tuple<int, unsigned, uint64_t>, Plan> g_tuned;
+
+size_t dyn_smem() { return 2 * (size_t)kMaxN * kMaxN * sizeof(double); }
+
+}  // namespace
+}  // namespace sed
+
+using namespace sed;
+
+extern "C" {
+
+int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options const* opts, double* eigenvalues,
+                     double* residuals, void* const eigenvectors[], uint64_t const ldv[], sed_batch_info* info) {
+  auto t_start = std::chrono::steady_clock::now();
+  if (count == 0) return LS_SUCCESS;
+  if (!ops || !opts || !eigenvalues) return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: NULL argument");
+  sed_eigh_options o{};
+  sed_eigh_options_init(&o);
+  std::memcpy(&o, opts, std::min<size_t>(sizeof(o), opts->struct_size ? opts->struct_size : sizeof(o)));
+  uint32_t const nev = o.nev ? o.nev : 1;
+  if (nev > (uint32_t)kB) return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: nev must be 1..4");
+  if (o.block_size != 0 && o.block_size != 1 && o.block_size != (uint32_t)kB)
+    return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: block_size must be 4");
+  double const tol = o.tol > 0 ? o.tol : 1e-8;
+  uint32_t const m_req = o.max_basis ? std::max<uint32_t>(2, o.max_basis / kB) : 12;
+  int device = -1;
+  if (int st = current_device(&device)) return st;
+  std::vector<OperatorData*> od(count);
+  for (unsigned i = 0; i < count; ++i) {
+    if (!ops[i]) return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: NULL operator");
+    od[i] = ops[i]->d.get();
+    OperatorData& op = *od[i];
+    if (!op.basis->built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
+    if (op.basis->device != device) return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: operators on another device");
+    if (!op.is_real) return fail(LS_OPERATOR_IS_COMPLEX, "sed_eigh_batched: operators must be real");
+    if (op.basis->D < 2 * (uint64_t)kB) return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: dimension below 8");
+    if (int st = operator_ensure_ready(op)) return st;
+    if (!op.stream.ready)
+      if (int st = operator_record_stream(op, op.cuda_stream)) return st;
+  }
+  for (unsigned i = 0; i < count; ++i) SED_TRY_CUDA(cudaStreamSynchronize(od[i]->cuda_stream));
+  auto t_setup = std::chrono::steady_clock::now();
+  cudaStream_t stream = nullptr;
+  SED_TRY_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sguard{stream};
+
+  int sms = 0, coop = 0;
+  SED_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  SED_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+  if (!coop) return fail(LS_CUDA_ERROR, "sed_eigh_batched: device lacks cooperative launch");
+  SED_TRY_CUDA(cudaFuncSetAttribute(k_batch_lanczos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem()));
+  int max_per_sm = 0;
+  SED_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, k_batch_lanczos, 256, dyn_smem()));
+  if (max_per_sm < 1) return fail(LS_CUDA_ERROR, "sed_eigh_batched: kernel does not fit on an SM");
+
+  // work model per problem: streamed bytes of a block matvec plus the FP64
+  // reorthogonalisation (rows x stored columns)
+  std::vector<double> work(count);
+  for (unsigned i = 0; i < count; ++i) {
+    double const D = (double)od[i]->basis->D, E = (double)od[i]->stream.n_entries;
+    work[i] = E * 4.0 + D * 40.0 + D * 16.0 * m_req * 6.0;
+  }
+
+  // Per-problem device arena
+  std::vector<uint32_t> m_blocks(count);
+  std::vector<size_t> off_V(count), off_W(count), off_W2(count), off_T(count), off_B(count), off_Y(count), off_out(count);
+  size_t total = 0;
+  auto take = [&](size_t bytes) {
+    size_t const o = total;
+    total += (bytes + 255) & ~size_t(255);
+    return o;
+  };
+  for (unsigned i = 0; i < count; ++i) {
+    uint64_t const D = od[i]->basis->D;
+    uint32_t m = std::min<uint32_t>(std::min<uint32_t>(m_req, kMaxBlocks), (uint32_t)std::min<uint64_t>(kMaxBlocks, D / kB - 1));
+    m = std::max<uint32_t>(m, 1);
+    m_blocks[i] = m;
+    off_V[i] = take((size_t)(m + 1) * D * kB * 8);
+    off_W[i] = take((size_t)D * kB * 8);
+    off_W2[i] = take((size_t)D * kB * 8);
+    off_T[i] = take((size_t)kMaxBlocks * kMaxN * 4 * 8);
+    off_B[i] = take((size_t)kMaxBlocks * 16 * 8);
+    off_Y[i] = take((size_t)kMaxN * 8 * 8);
+    off_out[i] = take(kOutBytes);
+  }
+
+  // Candidate launch shapes; the autotuner times each on a short trial (two
+  // block steps of every problem) and keeps the fastest per (device, count, size).
+  std::vector<Plan> cands;
+  for (unsigned per = 1; per <= (unsigned)std::min(max_per_sm, 2); ++per) cands.push_back(Plan{256, per});
+  uint64_t sumD = 0;
+  for (unsigned i = 0; i < count; ++i) sumD += od[i]->basis->D;
+  auto key = std::make_tuple(device, count, sumD);
+  Plan plan = cands[0];
+  bool tuned = false;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      plan = it->second;
+      tuned = true;
+    }
+  }
+
+  // group layout for a given grid
+  struct Layout {
+    std::vector<GroupDesc> groups;
+    std::vector<uint32_t> cta_group, order;
+    std::vector<uint32_t> group_of_chain;
+  };
+  auto make_layout = [&](unsigned grid) {
+    Layout L;
+    std::vector<uint32_t> idx(count);
+    std::iota(idx.begin(), idx.end(), 0u);
+    std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return work[a] > work[b]; });
+    L.group_of_chain.assign(count, 0);
+    if (count <= grid) {
+      // one group per problem, CTAs in proportion to work (largest remainders)
+      double const W = std::accumulate(work.begin(), work.end(), 0.0);
+      std::vector<uint32_t> n(count, 1);
+      unsigned left = grid - count;
+      std::vector<std::pair<double, uint32_t>> rem;
+      for (unsigned i = 0; i < count; ++i) {
+        double const want = std::max(0.0, work[i] / W * grid - 1.0);
+        uint32_t const add = std::min<uint32_t>((uint32_t)want, left);
+        n[i] += add;
+        left -= add;
+        rem.push_back({want - add, i});
+      }
+      std::sort(rem.begin(), rem.end(), [](auto& a, auto& b) { return a.first > b.first; });
+      for (size_t q = 0; q < rem.size() && left > 0; ++q, --left) n[rem[q].second] += 1;
+      // a group never has more CTAs than slices
+      for (unsigned i = 0; i < count; ++i)
+        n[i] = std::max<uint32_t>(1, std::min<uint32_t>(n[i], (uint32_t)od[i]->stream.n_slices));
+      uint32_t cta = 0;
+      for (unsigned q = 0; q < count; ++q) {
+        uint32_t const i = idx[q];
+        L.groups.push_back(GroupDesc{cta, n[i], q, 1, nullptr});
+        L.order.push_back(i);
+        L.group_of_chain[i] = q;
+        cta += n[i];
+      }
+    } else {
+      // more problems than CTAs: one CTA per group, longest-processing-time
+      std::vector<double> load(grid, 0.0);
+      std::vector<std::vector<uint32_t>> lists(grid);
+      for (uint32_t i : idx) {
+        unsigned const g = (unsigned)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[g] += work[i];
+        lists[g].push_back(i);
+      }
+      for (unsigned g = 0; g < grid; ++g) {
+        L.groups.push_back(GroupDesc{g, 1, (uint32_t)L.order.size(), (uint32_t)lists[g].size(), nullptr});
+        for (uint32_t i : lists[g]) {
+          L.group_of_chain[i] = g;
+          L.order.push_back(i);
+        }
+      }
+    }
+    for (uint32_t g = 0; g < L.groups.size(); ++g)
+      for (uint32_t k = 0; k < L.groups[g].ncta; ++k) L.cta_group.push_back(g);
+    return L;
+  };
+
+  unsigned const max_grid = (unsigned)sms * (unsigned)std::min(max_per_sm, 2);
+  size_t const part_bytes = 2 * (size_t)max_grid * kPart * 8;
+  std::vector<size_t> off_part(count);
+  for (unsigned i = 0; i < count; ++i) off_part[i] = take(part_bytes);  // enough for any group size
+  size_t const off_groups = take(sizeof(GroupDesc) * max_grid);
+  size_t const off_ctag = take(4 * (size_t)max_grid);
+  size_t const off_order = take(4 * (size_t)count);
+  size_t const off_bars = take(8 * (size_t)max_grid);
+  size_t const off_chains = take(sizeof(ChainDesc) * count);
+  size_t const off_err = take(16);
+  DeviceBuffer arena;
+  if (int st = arena.allocate(total)) return st;
+  char* base = arena.as<char>();
+
+  std::vector<ChainDesc> chains(count);
+  for (unsigned i = 0; i < count; ++i) {
+    OperatorData& op = *od[i];
+    ChainDesc& c = chains[i];
+    c.S = stream_view(op);
+    c.D = op.basis->D;
+    c.n_slices = op.stream.n_slices;
+    c.V = reinterpret_cast<double*>(base + off_V[i]);
+    c.W = reinterpret_cast<double*>(base + off_W[i]);
+    c.part = reinterpret_cast<double*>(base + off_part[i]);
+    c.W2 = reinterpret_cast<double*>(base + off_W2[i]);
+    c.Tc = reinterpret_cast<double*>(base + off_T[i]);
+    c.Bblk = reinterpret_cast<double*>(base + off_B[i]);
+    c.Y = reinterpret_cast<double*>(base + off_Y[i]);
+    c.out = reinterpret_cast<double*>(base + off_out[i]);
+    c.stats = reinterpret_cast<uint32_t*>(base + off_out[i] + kStatsOff);
+    c.flag = reinterpret_cast<uint32_t*>(base + off_out[i] + kStatsOff + 16);
+    c.m_blocks = m_blocks[i];
+    c.nev = nev;
+    c.packed = op.stream.packed ? 1u : 0u;
+    c.seed = o.seed + 0x9E3779B97F4A7C15ull * (i + 1);
+  }
+  SED_TRY_CUDA(cudaMemcpyAsync(base + off_chains, chains.data(), sizeof(ChainDesc) * count, cudaMemcpyHostToDevice, stream));
+
+  uint32_t const max_steps_total = o.max_iter ? std::max<uint32_t>(1, o.max_iter / kB) : 2000;
+  auto run = [&](Plan const& p, uint32_t max_steps, float* ms) -> int {
+    unsigned const grid = (unsigned)sms * p.ctas_per_sm;
+    Layout L = make_layout(grid);
+    for (auto& g : L.groups) g.bar = reinterpret_cast<uint32_t*>(base + off_bars) + 2 * (&g - L.groups.data());
+    unsigned const used = (unsigned)L.cta_group.size();
+    SED_TRY_CUDA(cudaMemcpyAsync(base + off_groups, L.groups.data(), sizeof(GroupDesc) * L.groups.size(), cudaMemcpyHostToDevice, stream));
+    SED_TRY_CUDA(cudaMemcpyAsync(base + off_ctag, L.cta_group.data(), 4 * (size_t)used, cudaMemcpyHostToDevice, stream));
+    SED_TRY_CUDA(cudaMemcpyAsync(base + off_order, L.order.data(), 4 * (size_t)count, cudaMemcpyHostToDevice, stream));
+    SED_TRY_CUDA(cudaMemsetAsync(base + off_bars, 0, 8 * (size_t)max_grid, stream));
+    SED_TRY_CUDA(cudaMemsetAsync(base + off_err, 0, 16, stream));
+    for (unsigned i = 0; i < count; ++i) SED_TRY_CUDA(cudaMemsetAsync(base + off_out[i], 0, kOutBytes, stream));
+    BatchArgs a;
+    a.chains = reinterpret_cast<ChainDesc const*>(base + off_chains);
+    a.groups = reinterpret_cast<GroupDesc const*>(base + off_groups);
+    a.cta_group = reinterpret_cast<uint32_t const*>(base + off_ctag);
+    a.order = reinterpret_cast<uint32_t const*>(base + off_order);
+    a.tol = tol;
+    a.max_steps = max_steps;
+    a.rr_every = 2;
+    a.error = reinterpret_cast<int*>(base + off_err);
+    cudaEvent_t e0, e1;
+    SED_TRY_CUDA(cudaEventCreate(&e0));
+    SED_TRY_CUDA(cudaEventCreate(&e1));
+    void* kargs[] = {&a};
+    SED_TRY_CUDA(cudaEventRecord(e0, stream));
+    cudaError_t le = cudaLaunchCooperativeKernel((void const*)k_batch_lanczos, dim3(used), dim3(p.threads), kargs,
+                                                 dyn_smem(), stream);
+    note_launches(1);
+    SED_TRY_CUDA(cudaEventRecord(e1, stream));
+    int err = 0;
+    SED_TRY_CUDA(cudaMemcpyAsync(&err, base + off_err, 4, cudaMemcpyDeviceToHost, stream));
+    cudaError_t se = cudaStreamSynchronize(stream);
+    if (ms) cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SED_TRY_CUDA(le);
+    SED_TRY_CUDA(se);
+    if (err) return fail(LS_DEVICE_TIMEOUT, "sed_eigh_batched: a group barrier timed out");
+    return LS_SUCCESS;
+  };
+
+  if (!tuned && cands.size() > 1) {
+    float best = 3e38f;
+    for (Plan const& p : cands) {
+      float ms = 0;
+      if (int st = run(p, 2, &ms)) return st;
+      if (ms < best) {
+        best = ms;
+        plan = p;
+      }
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = plan;
+  }
+  auto t_solve0 = std::chrono::steady_clock::now();
+  float solve_ms = 0;
+  if (int st = run(plan, max_steps_total, &solve_ms)) return st;
+
+  // results
+  std::vector<double> outs(12);
+  std::vector<uint32_t> stats(4);
+  bool all_ok = true;
+  uint64_t max_steps = 0, max_restarts = 0, breakdowns = 0;
+  std::string first_bad;
+  for (unsigned i = 0; i < count; ++i) {
+    SED_TRY_CUDA(cudaMemcpy(outs.data(), base + off_out[i], 96, cudaMemcpyDeviceToHost));
+    SED_TRY_CUDA(cudaMemcpy(stats.data(), base + off_out[i] + kStatsOff, 16, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < nev; ++k) {
+      eigenvalues[(size_t)i * nev + k] = outs[k];
+      if (residuals) residuals[(size_t)i * nev + k] = outs[8 + k];
+    }
+    max_steps = std::max<uint64_t>(max_steps, stats[0]);
+    max_restarts = std::max<uint64_t>(max_restarts, stats[1]);
+    if (stats[3] != 1) {
+      if (all_ok) {
+        char buf[256];
+        std::snprintf(buf, sizeof buf, " (first: problem %u, D = %llu, %u block steps, %u restarts, status %u, "
+                      "residuals %.2e %.2e %.2e %.2e)", i, (unsigned long long)od[i]->basis->D, stats[0], stats[1],
+                      stats[3], outs[8], outs[9], outs[10], outs[11]);
+        first_bad = buf;
+      }
+      all_ok = false;
+    }
+    if (stats[3] == 3) ++breakdowns;
+    if (eigenvectors && eigenvectors[i]) {
+      uint64_t const D = od[i]->basis->D;
+      uint64_t const ld = ldv ? ldv[i] : D;
+      if (ld < D) return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: ldv below the dimension");
+      DeviceBuffer tmpv;
+      if (int st = tmpv.allocate((size_t)ld * nev * 8)) return st;
+      { k_unpack_block<<<grid_size(D * nev, device), kBlock, 0, stream>>>(reinterpret_cast<double const*>(base + off_V[i]), D, nev, tmpv.as<double>(), ld); note_launches(1); }
+      SED_TRY_CUDA(cudaMemcpyAsync(eigenvectors[i], tmpv.ptr, ((size_t)ld * (nev - 1) + D) * 8, cudaMemcpyDefault, stream));
+      SED_TRY_CUDA(cudaStreamSynchronize(stream));
+    }
+  }
+  auto t_end = std::chrono::steady_clock::now();
+  if (info) {
+    info->block_steps_max = max_steps;
+    info->restarts_max = max_restarts;
+    info->seconds_total = std::chrono::duration<double>(t_end - t_start).count();
+    info->seconds_setup = std::chrono::duration<double>(t_setup - t_start).count();
+    info->seconds_solve = std::chrono::duration<double>(t_end - t_solve0).count();
+    info->kernel_ms = solve_ms;
+    info->ctas_per_sm = plan.ctas_per_sm;
+    info->threads_per_cta = plan.threads;
+    info->grid = (uint32_t)(sms * plan.ctas_per_sm);
+  }
+  if (logging_enabled())
+    log_line("sed_eigh_batched: %u problems, %.3f ms in one launch (%u CTAs/SM), max %llu block steps", count,
+             solve_ms, plan.ctas_per_sm, (unsigned long long)max_steps);
+  if (!all_ok)
+    return fail(LS_NOT_CONVERGED, std::string(breakdowns ? "sed_eigh_batched: Krylov breakdown in some problems"
+                                                         : "sed_eigh_batched: some problems did not converge") +
+                                      first_bad);
+  return LS_SUCCESS;
+}
+
+}  // extern "C"

@@ -296,6 +296,7 @@ unsigned blocks_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<
 // columns; one thread issues the copies and the MMAs, four warps run the
 // epilogues (warp w owns TMEM lanes / rows 32 w .. 32 w + 31).
 constexpr int kTcRows = 128;
+constexpr int kTcThreads = 512;  // 16 warps: 4 per TMEM lane quarter
 constexpr uint64_t kTcWaitNs = 1000000000ull;  // 1 s per wait: far beyond any MMA or copy
 
 struct MlpTcArgs {
@@ -312,12 +313,14 @@ struct MlpTcArgs {
   int* error;
 };
 
+// dynamic shared memory: A tiles, two B stages, b1, b2, W3 (FP32), partials
 size_t tc_smem_bytes(int hidden) {
   int const nm = hidden < 256 ? hidden : 256;
-  return (size_t)kTcRows * hidden * 2 + 2 * (size_t)nm * 128 + 1024;
+  return (size_t)kTcRows * hidden * 2 + 2 * (size_t)nm * 128 + 4 * (size_t)hidden * 4 +
+         (size_t)kTcThreads * 2 * 4 + 1024;
 }
 
-__global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(MlpTcArgs p) {
+__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full1[2], full[2], empty[2], done;
   __shared__ uint32_t tmem_slot;
@@ -328,8 +331,14 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(MlpTcArgs p) {
   uint8_t* const A = smem;  // H/64 tiles of 128 rows x 128 B
   uint8_t* const B0 = smem + (size_t)kTcRows * H * 2;
   uint8_t* const Bs[2] = {B0, B0 + stage_bytes};
-  int const t = threadIdx.x, warp = t >> 5, r = t;
-  int64_t const row = (int64_t)blockIdx.x * kTcRows + r;
+  float* const sb1 = reinterpret_cast<float*>(B0 + 2 * (size_t)stage_bytes);
+  float* const sb2 = sb1 + H;
+  float* const sw3 = sb2 + H;  // [2][H]
+  float* const spart = sw3 + 2 * H;  // [4 column quarters][128 rows][2]
+  int const t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  int const quarter = warp & 3, cq = warp >> 2;  // TMEM lane quarter, column quarter
+  int const r = quarter * 32 + lane;             // row of this thread in the epilogues
+  int const cols = H / 4, c_begin = cq * cols;
   uint32_t const idesc = tc::idesc_bf16_f32(128, (uint32_t)NM);
 
   if (t == 0) {
@@ -344,11 +353,21 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(MlpTcArgs p) {
   }
   __syncwarp();
   if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)H);
-  // X tile: row r, input j -> BF16 +1 / -1, zero for j >= n_in
+  for (int c = t; c < H; c += kTcThreads) {
+    sb1[c] = __ldg(p.b1 + c);
+    sb2[c] = __ldg(p.b2 + c);
+    sw3[c] = __bfloat162float(p.W3[c]);
+    sw3[H + c] = __bfloat162float(p.W3[H + c]);
+  }
+  // X tile: row xr, input j -> BF16 +1 / -1, zero for j >= n_in; four threads
+  // per row, two 16-byte chunks each
   {
-    uint64_t const s = row < p.n ? p.states[row] : 0;
+    int const xr = t & 127, part = t >> 7;
+    int64_t const xrow = (int64_t)blockIdx.x * kTcRows + xr;
+    uint64_t const s = xrow < p.n ? p.states[xrow] : 0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
+    for (int cc = 0; cc < 2; ++cc) {
+      int const c = 2 * part + cc;
       uint32_t w[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -357,7 +376,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(MlpTcArgs p) {
         uint32_t const hi = j + 1 < p.n_in ? (((s >> (j + 1)) & 1) ? 0x3F80u : 0xBF80u) : 0u;
         w[q] = lo | (hi << 16);
       }
-      *reinterpret_cast<uint4*>(A + r * 128 + ((c ^ (r & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
+      *reinterpret_cast<uint4*>(A + xr * 128 + ((c ^ (xr & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
   tc::fence_proxy_async_smem();
@@ -400,23 +419,21 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(MlpTcArgs p) {
       tc::bulk_g2s(Bs[j], p.w2img + ((size_t)kb * H + (size_t)h * NM) * 128, stage_bytes, &full[j]);
     }
   __syncwarp();
-  // ---- epilogue 1: h1 = tanh(acc + b1) -> BF16 -> A tiles (row r)
+  uint32_t const lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+  // ---- epilogue 1: h1 = tanh(acc + b1) -> BF16 -> A tiles (row r, this
+  // warp's column quarter, 32 columns = four 16-byte chunks per load)
   if (ok) {
-    uint32_t const lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int cc = 0; cc < H / 32; ++cc) {
+    for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
       float v[32];
-      tc::tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
+      tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
       uint32_t pk[16];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        int const c = cc * 32 + 2 * q;
-        pk[q] = tc::pack_bf16x2(tc::tanh_fast(v[2 * q] + __ldg(p.b1 + c)),
-                                tc::tanh_fast(v[2 * q + 1] + __ldg(p.b1 + c + 1)));
-      }
-      uint8_t* const tile = A + (size_t)(cc >> 1) * (kTcRows * 128) + r * 128;
+      for (int q = 0; q < 16; ++q)
+        pk[q] = tc::pack_bf16x2(tc::tanh_fast(v[2 * q] + sb1[c0 + 2 * q]), tc::tanh_fast(v[2 * q + 1] + sb1[c0 + 2 * q + 1]));
+      uint8_t* const tile = A + (size_t)(c0 >> 6) * (kTcRows * 128) + r * 128;
 #pragma unroll
       for (int q4 = 0; q4 < 4; ++q4) {
-        int const chunk = ((cc & 1) * 4 + q4) ^ (r & 7);
+        int const chunk = (((c0 & 63) >> 3) + q4) ^ (r & 7);
         *reinterpret_cast<uint4*>(tile + (chunk << 4)) =
             make_uint4(pk[4 * q4], pk[4 * q4 + 1], pk[4 * q4 + 2], pk[4 * q4 + 3]);
       }
@@ -463,26 +480,36 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(MlpTcArgs p) {
   if (ok) ok = tc::mbar_wait(&done, 1, kTcWaitNs);
   tc::fence_after_sync();
   __syncwarp();
-  // ---- epilogue 2: h2 = tanh(acc + b2); (a, s) = W3 h2 + b3
+  // ---- epilogue 2: h2 = tanh(acc + b2); partial (a, s) = W3 h2 over this
+  // warp's column quarter, summed over the quarters through shared memory
+  float a = 0.0f, sg = 0.0f;
   if (ok) {
-    uint32_t const lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    float a = __ldg(p.b3), sg = __ldg(p.b3 + 1);
-    for (int cc = 0; cc < H / 32; ++cc) {
+    for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
       float v[32];
-      tc::tmem_ld32(lane_addr + (uint32_t)(cc * 32), v);
+      tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
 #pragma unroll
       for (int q = 0; q < 32; ++q) {
-        int const c = cc * 32 + q;
-        float const hq = tc::tanh_fast(v[q] + __ldg(p.b2 + c));
-        a = fmaf(__bfloat162float(p.W3[c]), hq, a);
-        sg = fmaf(__bfloat162float(p.W3[H + c]), hq, sg);
+        float const hq = tc::tanh_fast(v[q] + sb2[c0 + q]);
+        a = fmaf(sw3[c0 + q], hq, a);
+        sg = fmaf(sw3[H + c0 + q], hq, sg);
       }
     }
-    if (row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(a, sg);
   }
-  if (!ok && (t & 31) == 0) atomicExch(p.error, 1);
+  spart[(cq * kTcRows + r) * 2] = a;
+  spart[(cq * kTcRows + r) * 2 + 1] = sg;
   tc::fence_before_sync();
   __syncthreads();
+  if (ok && t < kTcRows) {
+    int64_t const row = (int64_t)blockIdx.x * kTcRows + t;
+    float sa = __ldg(p.b3), ss = __ldg(p.b3 + 1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      sa += spart[(q * kTcRows + t) * 2];
+      ss += spart[(q * kTcRows + t) * 2 + 1];
+    }
+    if (row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
+  }
+  if (!ok && (t & 31) == 0) atomicExch(p.error, 1);
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, (uint32_t)H);
@@ -667,7 +694,7 @@ int forward_tc(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
   a.out = out;
   a.error = d.tc_error.as<int>();
   unsigned const grid = (unsigned)((n + kTcRows - 1) / kTcRows);
-  { k_mlp_forward_tc<<<grid, 128, smem, s>>>(a); note_launches(1); }
+  { k_mlp_forward_tc<<<grid, kTcThreads, smem, s>>>(a); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   int err = 0;
   SED_TRY_CUDA(cudaMemcpyAsync(&err, d.tc_error.ptr, 4, cudaMemcpyDeviceToHost, s));

@@ -74,6 +74,21 @@ class EighInfo(C.Structure):
     ]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("block_steps_max", C.c_uint64),
+        ("restarts_max", C.c_uint64),
+        ("seconds_total", C.c_double),
+        ("seconds_setup", C.c_double),
+        ("seconds_solve", C.c_double),
+        ("kernel_ms", C.c_double),
+        ("grid", C.c_uint32),
+        ("ctas_per_sm", C.c_uint32),
+        ("threads_per_cta", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
 # (name, restype, argtypes)
 _P, _U, _I, _U64, _D, _B = C.c_void_p, C.c_uint, C.c_int, C.c_uint64, C.c_double, C.c_bool
 SIGNATURES = [
@@ -111,6 +126,7 @@ SIGNATURES = [
     ("ls_operator_is_real", _B, [_P]),
     ("sed_eigh_options_init", None, [C.POINTER(EighOptions)]),
     ("sed_eigh", _I, [_P, _I, C.POINTER(EighOptions), _P, _P, _U64, _P, C.POINTER(EighInfo)]),
+    ("sed_eigh_batched", _I, [_U, _P, C.POINTER(EighOptions), _P, _P, _P, _P, C.POINTER(BatchInfo)]),
     ("sed_operator_prepare", _I, [_P, _I]),
     ("sed_operator_stream_bytes", _U64, [_P]),
     ("sed_operator_stream_elements", _U64, [_P]),

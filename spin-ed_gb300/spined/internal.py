@@ -388,3 +388,41 @@ def eigh(op: Operator, nev: int = 1, tol: float = 1e-8, dtype=np.float64, out=No
     del keep
     return EighResult(evals, out, res, info.iterations, info.matvecs, info.restarts, info.fp32_iterations,
                       info.seconds_total, info.seconds_setup, info.seconds_solve)
+
+
+@dataclass
+class BatchResult:
+    eigenvalues: np.ndarray      # [count, nev]
+    residuals: np.ndarray        # [count, nev]
+    eigenvectors: list           # per operator [D_i, nev] (or None)
+    block_steps_max: int
+    restarts_max: int
+    kernel_ms: float
+    seconds_total: float
+    seconds_setup: float
+    ctas_per_sm: int
+    grid: int
+
+
+def eigh_batched(ops: Sequence[Operator], nev: int = 4, tol: float = 1e-8, max_basis: int = 0,
+                 seed: int = 1234, max_iter: int = 0, vectors: bool = True) -> BatchResult:
+    """Lowest nev (<= 4) eigenpairs of every operator by block Lanczos (block
+    size 4, FP64), all operators in one persistent launch (sed_eigh_batched)."""
+    count = len(ops)
+    opts, _ = eigh_options(nev=nev, tol=tol, max_iter=max_iter, max_basis=max_basis, block_size=4, seed=seed)
+    evals = np.zeros((count, nev), dtype=np.float64)
+    res = np.zeros((count, nev), dtype=np.float64)
+    arr = (C.c_void_p * count)(*[op.ptr.value for op in ops])
+    vecs, vptr, lds = None, None, None
+    if vectors:
+        vecs = [np.zeros((get_number_states(op.basis), nev), dtype=np.float64, order="F") for op in ops]
+        vptr = (C.c_void_p * count)(*[v.ctypes.data for v in vecs])
+        lds = (C.c_uint64 * count)(*[v.shape[0] for v in vecs])
+    info = L.BatchInfo()
+    check_status(L.load().sed_eigh_batched(count, C.cast(arr, C.c_void_p), C.byref(opts),
+                                           C.c_void_p(evals.ctypes.data), C.c_void_p(res.ctypes.data),
+                                           C.cast(vptr, C.c_void_p) if vptr is not None else None,
+                                           C.cast(lds, C.c_void_p) if lds is not None else None,
+                                           C.byref(info)))
+    return BatchResult(evals, res, vecs, info.block_steps_max, info.restarts_max, info.kernel_ms,
+                       info.seconds_total, info.seconds_setup, info.ctas_per_sm, info.grid)
