@@ -1197,6 +1197,8 @@ int sed_eigh(ls_operator const* op, int dtype, sed_eigh_options const* opts, dou
     ScopedDevice dev(d.basis->device);
     if (int st = operator_ensure_ready(d)) return st;
     if (dtype >= 2 || !d.is_real) return solve<double2>(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);
+    if (o.max_basis > 0 && o.max_basis <= 32 && o.block_size <= 1)
+      return solve_thick(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);
     if (o.precision == SED_PRECISION_MIXED && o.nev == 1 && o.form != SED_FORM_ON_THE_FLY)
       return solve_mixed(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);
     return solve<double>(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);

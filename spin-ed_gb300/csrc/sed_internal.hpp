@@ -210,6 +210,10 @@ int operator_prepare_fp32(OperatorData& op, cudaStream_t stream);
 
 bool characters_real(BasisData const& b);
 
+// sed_eigh's thick-restart solver (real operators, 0 < max_basis <= 32).
+int solve_thick(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* evals, void* evecs, uint64_t ldv,
+                double* rnorms, sed_eigh_info* info);
+
 // Kernel-launch accounting (sed_kernel_launches): every launch site calls
 // note_launches(1); launches made while capturing a graph are not counted,
 // the graph's kernel nodes are counted at each replay instead.

@@ -106,3 +106,39 @@ def test_mixed_precision_matches_fp64_oracle(sed, oracle, name, model):
     assert res.eigenvalues[0] == pytest.approx(ev[0], rel=EV_RTOL)
     assert res.residuals[0] <= RES_TOL
     check_pair(oop, res.eigenvalues[0], res.eigenvectors[:, 0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name,model,m", [
+    ("chain24", lattices.heisenberg_chain(24), 16),
+    ("chain20_j2", lattices.heisenberg_chain(20, j2=0.45), 8),
+    ("square4", lattices.heisenberg_square(4), 6),
+])
+def test_thick_restart_matches_fp64_oracle(sed, oracle, name, model, m, precision):
+    """Thick-restart Lanczos with at most m stored vectors (max_basis <= 32),
+    FP64 or FP32-stored with an FP64 refinement: eigenvalue within 1e-10
+    relative of the FP64 oracle, residual <= 1e-8 (recomputed here)."""
+    from spined import _lib as L
+    built, ob, oop = both(sed, oracle, model)
+    A = oop.sparse()
+    ev, _, _, _ = oracle.lanczos_ground_state(lambda v: A @ v, oracle.start_vector(1234, A.shape[0]))
+    p = L.SED_PRECISION_FP64 if precision == "fp64" else L.SED_PRECISION_MIXED
+    res = sed.eigh(built.hamiltonian, seed=1234, max_basis=m, precision=p)
+    if precision == "mixed":
+        assert res.fp32_iterations > 0
+    if A.shape[0] > m:
+        assert res.restarts > 0  # the basis really was recycled
+    assert res.eigenvalues[0] == pytest.approx(ev[0], rel=EV_RTOL)
+    assert res.residuals[0] <= RES_TOL
+    check_pair(oop, res.eigenvalues[0], res.eigenvectors[:, 0])
+
+
+def test_thick_restart_lowest_three(sed, oracle):
+    import scipy.sparse.linalg as sla
+    built, ob, oop = both(sed, oracle, lattices.heisenberg_chain(18, j2=0.3))
+    want = np.sort(sla.eigsh(oop.sparse(), k=3, which="SA")[0])
+    res = sed.eigh(built.hamiltonian, nev=3, max_basis=12)
+    np.testing.assert_allclose(res.eigenvalues, want, rtol=EV_RTOL)
+    assert np.all(res.residuals <= RES_TOL)
+    for k in range(3):
+        check_pair(oop, res.eigenvalues[k], res.eigenvectors[:, k])
