@@ -56,6 +56,8 @@ def workload_model(name: str, hamming_weight: int | None = None):
         return lattices.heisenberg_square(4)
     if name == "chain32":
         return lattices.heisenberg_chain(32)
+    if name == "chain40":
+        return lattices.heisenberg_chain(40)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -231,6 +233,126 @@ def gpu_arm(args, rank, world, dist):
     }
 
 
+# --------------------------------------------------- spec forms --
+
+def forms_arm(stream):
+    """Time to the 6x6 ground state of the Lanczos phase alone (the basis and
+    the stream form are shared by every form and built beforehand): plain
+    FP64 from the seed-1234 start, FP32-stored Krylov vectors with FP64
+    anchoring, a warm start from the neighbouring coupling J2 = 0.05, and the
+    learned start (MLP 36-512-512-2 trained on 2^20 configurations sampled from
+    the J2 = 0.05 and 0.10 ground states; its training is reported apart, its
+    tensor-core inference is inside the timed solve)."""
+    import torch
+    from spined import internal as I, lattices, _lib as L
+    from spined.learned import Mlp, Samples, sample
+    from spined.model import build_model
+    b = build_model(lattices.heisenberg_square(6))
+    D = I.get_number_states(b.basis)
+    op0 = b.hamiltonian
+    op0.prepare(L.SED_FORM_STREAM)
+    out = {}
+    v = torch.empty(D, dtype=torch.float64, device="cuda")
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    def solve(op, **kw):
+        return timed(lambda: I.eigh(op, tol=1e-8, out=v, **kw))
+
+    def rec(name, t, r, extra=None):
+        out[name] = {"seconds": t, "lanczos_steps": r.iterations, "fp32_steps": r.fp32_iterations,
+                     "E0": float(r.eigenvalues[0]), "residual": float(r.residuals[0])}
+        if extra:
+            out[name].update(extra)
+
+    for _ in range(2):  # second pass is the measured one (warm caches, tuned launch shapes)
+        t, r = solve(op0, seed=1234)
+        rec("plain_fp64", t, r)
+        e_ref = float(r.eigenvalues[0])
+        psi0 = v.clone()
+        t, r = solve(op0, seed=1234, precision=L.SED_PRECISION_MIXED)
+        rec("mixed_random", t, r)
+    # neighbouring couplings on the same basis
+    psis = {}
+    for j2 in (0.05, 0.10):
+        mm = lattices.heisenberg_square(6, j2=j2)
+        terms = [I.mk_interaction(mat, sites) for mat, sites in mm.terms]
+        op = I.mk_operator(b.basis, terms)
+        op.prepare(L.SED_FORM_STREAM)
+        I.eigh(op, tol=1e-8, out=v, seed=1234)
+        psis[j2] = v.clone()
+        del op
+    warm = psis[0.05] / torch.linalg.norm(psis[0.05])
+    t, r = solve(op0, start=warm)
+    rec("warm_fp64", t, r, {"overlap": abs(torch.dot(warm, psi0).item())})
+    t, r = solve(op0, start=warm, precision=L.SED_PRECISION_MIXED)
+    rec("warm_mixed", t, r)
+    # learned start
+    mask = lattices.square_sublattice_mask(6)
+    t_s, data = timed(lambda: Samples.concat([sample(b.basis, psis[0.05], 1 << 19, seed=1, sign_mask=mask),
+                                              sample(b.basis, psis[0.10], 1 << 19, seed=2, sign_mask=mask)]))
+    net = Mlp(36, 512, sign_mask=mask, seed=5)
+    t_tr, loss = timed(lambda: net.train(data, epochs=8, batch=4096, lr=3e-3, seed=3))
+    start = torch.empty(D, dtype=torch.float64, device="cuda")
+    net.start_vector(b.basis, out=start)
+    for prec, name in ((L.SED_PRECISION_FP64, "learned_fp64"), (L.SED_PRECISION_MIXED, "learned_mixed")):
+        def run():
+            net.start_vector(b.basis, out=start)
+            start.div_(torch.linalg.norm(start))
+            return I.eigh(op0, tol=1e-8, out=v, start=start, precision=prec)
+        t, r = timed(run)
+        t_inf, _ = timed(lambda: net.start_vector(b.basis, out=start))
+        rec(name, t, r, {"inference_s": t_inf})
+    out["learned_mixed"]["overlap"] = abs(torch.dot(start / torch.linalg.norm(start), psi0).item())
+    out["training"] = {"sample_s": t_s, "train_s": t_tr, "samples": len(data), "epochs": 8, "final_loss": loss,
+                       "tensor_cores": net.uses_tensor_cores}
+    base = out["plain_fp64"]["seconds"]
+    for k in ("mixed_random", "warm_fp64", "warm_mixed", "learned_fp64", "learned_mixed"):
+        out[k]["vs_plain_fp64"] = out[k]["seconds"] / base
+        out[k]["eigenvalue_rel_err"] = abs(out[k]["E0"] - e_ref) / abs(e_ref)
+    return out
+
+
+def batched_arm():
+    """The 128 J1-J2 chains (N uniform over 16..28, J2/J1 uniform in [0, 0.6],
+    seed 2024): lowest 4 eigenpairs each by block Lanczos (block 4, FP64), all
+    in one persistent launch, against the same problems solved one after the
+    other by sed_eigh (nev = 4)."""
+    import torch
+    from spined import internal as I, lattices, _lib as L
+    from spined.model import build_model
+    models = lattices.j1j2_chains(128, seed=2024)
+    t0 = time.perf_counter()
+    built = [build_model(m) for m in models]
+    for x in built:
+        x.hamiltonian.prepare(L.SED_FORM_STREAM)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    ops = [x.hamiltonian for x in built]
+    I.eigh_batched(ops, nev=4, vectors=False)  # first call: launch-shape trial runs
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = I.eigh_batched(ops, nev=4, vectors=False)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for op in ops:
+        I.eigh(op, nev=4)
+    torch.cuda.synchronize()
+    t_serial = time.perf_counter() - t0
+    dims = [I.get_number_states(x.basis) for x in built]
+    return {"workload": "128 J1-J2 chains, N in 16..28, lowest 4 eigenpairs, block Lanczos (block 4, FP64)",
+            "sum_D": int(sum(dims)), "max_D": int(max(dims)), "setup_s": t_setup, "batched_s": t_batch,
+            "kernel_ms": res.kernel_ms, "ctas_per_sm": res.ctas_per_sm, "grid": res.grid,
+            "block_steps_max": res.block_steps_max, "max_residual": float(res.residuals.max()),
+            "serial_sed_eigh_s": t_serial, "speedup_vs_serial": t_serial / t_batch}
+
+
 # ------------------------------------------------------------------ CPU --
 
 def cpu_sample(workload: str, budget_s: float = 8.0):
@@ -315,8 +437,10 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-budget", type=float, default=6.0, help="seconds of CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the forms and batched measurements")
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
     ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
+    ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
     args = ap.parse_args()
     args.precision_code = 0 if args.precision == "fp64" else 1
     rank = int(os.environ.get("RANK", "0"))
@@ -336,13 +460,25 @@ def main():
     if args.once:
         from spined import internal as I
         from spined.model import build_model
+        t0 = time.perf_counter()
         b = build_model(workload_model(args.workload, args.hamming_weight))
-        r = I.eigh(b.hamiltonian, tol=1e-8, seed=1234, precision=args.precision_code)
+        D = I.get_number_states(b.basis)
+        out = torch.empty(D, dtype=torch.float64, device="cuda")
+        r = I.eigh(b.hamiltonian, tol=1e-8, seed=1234, precision=args.precision_code, max_basis=args.max_basis,
+                   out=out)
         torch.cuda.synchronize()
-        print(json.dumps({"D": I.get_number_states(b.basis), "E0": float(r.eigenvalues[0]),
-                          "residual": float(r.residuals[0]), "steps": r.iterations}))
+        print(json.dumps({"workload": args.workload, "D": D, "E0": float(r.eigenvalues[0]),
+                          "residual": float(r.residuals[0]), "steps": r.iterations,
+                          "fp32_steps": r.fp32_iterations, "restarts": r.restarts, "max_basis": args.max_basis,
+                          "precision": args.precision, "solve_s": r.seconds_total,
+                          "wall_s": time.perf_counter() - t0}))
         return
     r = gpu_arm(args, rank, world, dist)
+    extras = {}
+    if rank == 0 and not args.no_extras and world == 1:
+        import torch
+        extras["forms"] = forms_arm(torch.cuda.current_stream())
+        extras["batched"] = batched_arm()
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and world == 1:
@@ -371,6 +507,7 @@ def main():
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

@@ -47,8 +47,9 @@ constexpr int kMaxBlocks = 16;      // stored Krylov blocks per cycle (n <= 64)
 constexpr int kMaxN = kB * kMaxBlocks;
 constexpr int kPart = 16 * (kMaxBlocks + 1);  // partial sums per CTA and slot
 constexpr uint64_t kBarrierNs = 20000000000ull;  // 20 s per barrier: far beyond any phase
-constexpr size_t kStatsOff = 12 * 8;                // per-problem output record: out[12], stats[4], flag[4]
-constexpr size_t kOutBytes = kStatsOff + 32;
+constexpr size_t kStatsOff = 12 * 8;                // per-problem output record: out[12], stats[4], flag[4], prof[8]
+constexpr size_t kProfOff = kStatsOff + 32;
+constexpr size_t kOutBytes = kProfOff + 64;
 
 struct ChainDesc {
   StreamView S;       // real operator, FP64 stream form
@@ -63,6 +64,7 @@ struct ChainDesc {
   double* out;        // theta[8], residual[4]
   uint32_t* stats;    // block steps, restarts, matvecs, status (0 running, 1 done, 2 not converged, 3 breakdown)
   uint32_t* flag;     // [4]: decision words written by the leader CTA
+  uint64_t* prof;     // [8] nanoseconds per phase on the leader CTA: spmv, cgs2, qr, rayleigh-ritz, ritz+restart, residual
   uint32_t m_blocks;
   uint32_t nev;
   uint32_t packed;    // stream entries hold col | code << col_bits
@@ -623,6 +625,12 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
   __shared__ double Rb[16], norms2[4];
   uint32_t steps = 0, restarts = 0, matvecs = 0, status = 2;
   double const tol = a.tol;
+  uint64_t tmark = tc::global_ns(), acc[6] = {};
+  auto lap = [&](int phase) {  // leader thread 0 only; others ignore
+    uint64_t const now = tc::global_ns();
+    acc[phase] += now - tmark;
+    tmark = now;
+  };
   random_block(x);
   bool qr_ok;
   if (!block_qr(x, c.V, Rb, qr_ok)) {
@@ -636,10 +644,13 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
     for (;; ++j) {
       double* Vj = c.V + (uint64_t)j * c.D * 4;
       if (!group_barrier(bar, ncta, a.error)) return;  // V_j complete on every CTA before the gathers
+      lap(4);
       block_spmv(x, Vj, c.W);
       ++matvecs;
       __syncthreads();
+      lap(0);
       if (!cgs2(x, c.W, j + 1, C, norms2)) return;
+      lap(1);
       if (leader)
         for (int k = threadIdx.x; k < 16 * (int)(j + 1); k += blockDim.x) c.Tc[j * kStride + k] = C[k];
       ++steps;
@@ -650,6 +661,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
       if (*(volatile int*)a.error) return;
       if (leader)
         for (int k = threadIdx.x; k < 16; k += blockDim.x) c.Bblk[j * 16 + k] = broke ? 0.0 : Rb[k];
+      lap(2);
       bool const full = j + 1 >= c.m_blocks || steps >= a.max_steps || broke;
       if (full || (j + 1) % a.rr_every == 0) {
         __threadfence();
@@ -662,6 +674,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
           }
         }
         if (!group_barrier(bar, ncta, a.error)) return;
+        lap(3);
         if (ldcg(c.flag) != 0u || full) break;
       }
     }
@@ -672,6 +685,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
     copy_block(x, c.V, c.W);
     if (thick) copy_block(x, c.V + c.D * 4, c.W2);
     if (!group_barrier(bar, ncta, a.error)) return;  // Psi rows visible to every CTA's SpMV gathers
+    lap(4);
     // true residuals of the lowest four Ritz pairs
     block_spmv(x, c.V, c.W);
     ++matvecs;
@@ -690,6 +704,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
       cta_sum<4>(p, red, tmp);
       if (!group_sum(x, tmp, 4, tmp + 16)) return;
     }
+    lap(5);
     bool all = true;
     for (uint32_t i = 0; i < c.nev; ++i) all = all && sqrt(tmp[16 + i]) <= tol;
     __syncthreads();
@@ -727,6 +742,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
     c.stats[1] = restarts;
     c.stats[2] = matvecs;
     c.stats[3] = status;
+    for (int q = 0; q < 6; ++q) c.prof[q] = acc[q];
   }
 }
 
@@ -883,12 +899,15 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     L.group_of_chain.assign(count, 0);
     if (count <= grid) {
       // one group per problem, CTAs in proportion to work (largest remainders)
+      // every problem has one CTA; the other grid - count CTAs go out in
+      // proportion to work (floors first, then the largest remainders)
       double const W = std::accumulate(work.begin(), work.end(), 0.0);
       std::vector<uint32_t> n(count, 1);
-      unsigned left = grid - count;
+      unsigned const extra = grid - count;
+      unsigned left = extra;
       std::vector<std::pair<double, uint32_t>> rem;
-      for (unsigned i = 0; i < count; ++i) {
-        double const want = std::max(0.0, work[i] / W * grid - 1.0);
+      for (uint32_t i : idx) {
+        double const want = work[i] / W * extra;
         uint32_t const add = std::min<uint32_t>((uint32_t)want, left);
         n[i] += add;
         left -= add;
@@ -960,6 +979,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     c.out = reinterpret_cast<double*>(base + off_out[i]);
     c.stats = reinterpret_cast<uint32_t*>(base + off_out[i] + kStatsOff);
     c.flag = reinterpret_cast<uint32_t*>(base + off_out[i] + kStatsOff + 16);
+    c.prof = reinterpret_cast<uint64_t*>(base + off_out[i] + kProfOff);
     c.m_blocks = m_blocks[i];
     c.nev = nev;
     c.packed = op.stream.packed ? 1u : 0u;
@@ -1062,6 +1082,31 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
       SED_TRY_CUDA(cudaMemcpyAsync(eigenvectors[i], tmpv.ptr, ((size_t)ld * (nev - 1) + D) * 8, cudaMemcpyDefault, stream));
       SED_TRY_CUDA(cudaStreamSynchronize(stream));
     }
+  }
+  if (logging_enabled()) {
+    unsigned worst = 0;
+    uint64_t worst_t = 0;
+    std::vector<uint64_t> prof(8);
+    for (unsigned i = 0; i < count; ++i) {
+      SED_TRY_CUDA(cudaMemcpy(prof.data(), base + off_out[i] + kProfOff, 64, cudaMemcpyDeviceToHost));
+      uint64_t t = 0;
+      for (int q = 0; q < 6; ++q) t += prof[q];
+      if (t > worst_t) {
+        worst_t = t;
+        worst = i;
+      }
+    }
+    SED_TRY_CUDA(cudaMemcpy(prof.data(), base + off_out[worst] + kProfOff, 64, cudaMemcpyDeviceToHost));
+    SED_TRY_CUDA(cudaMemcpy(stats.data(), base + off_out[worst] + kStatsOff, 16, cudaMemcpyDeviceToHost));
+    unsigned ncta = 0;
+    {
+      Layout L = make_layout((unsigned)sms * plan.ctas_per_sm);
+      ncta = L.groups[L.group_of_chain[worst]].ncta;
+    }
+    log_line("sed_eigh_batched: slowest problem %u (D = %llu, %u CTAs, %u block steps, %u restarts): spmv %.2f ms, "
+             "cgs2 %.2f ms, qr %.2f ms, rayleigh-ritz %.2f ms, ritz/restart %.2f ms, residual %.2f ms",
+             worst, (unsigned long long)od[worst]->basis->D, ncta, stats[0], stats[1], prof[0] * 1e-6,
+             prof[1] * 1e-6, prof[2] * 1e-6, prof[3] * 1e-6, prof[4] * 1e-6, prof[5] * 1e-6);
   }
   auto t_end = std::chrono::steady_clock::now();
   if (info) {

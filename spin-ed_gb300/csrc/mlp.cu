@@ -314,24 +314,24 @@ struct MlpTcArgs {
 };
 
 // dynamic shared memory: A tiles, two B stages, b1, b2, W3 (FP32), partials
+constexpr int kTcStages = 4;  // ring of weight stages, 128 rows x 128 B (16 KB) each
+
 size_t tc_smem_bytes(int hidden) {
-  int const nm = hidden < 256 ? hidden : 256;
-  return (size_t)kTcRows * hidden * 2 + 2 * (size_t)nm * 128 + 4 * (size_t)hidden * 4 +
+  return (size_t)kTcRows * hidden * 2 + (size_t)kTcStages * 128 * 128 + 4 * (size_t)hidden * 4 +
          (size_t)kTcThreads * 2 * 4 + 1024;
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full1[2], full[2], empty[2], done;
+  __shared__ uint64_t full[kTcStages], empty[kTcStages], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   uint8_t* const smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  int const H = p.hidden, NM = H < 256 ? H : 256, halves = H / NM;
+  int const H = p.hidden, NM = 128, quarters = H / NM;  // N = 128 per MMA, H / 128 column blocks
   uint32_t const stage_bytes = (uint32_t)NM * 128;
   uint8_t* const A = smem;  // H/64 tiles of 128 rows x 128 B
   uint8_t* const B0 = smem + (size_t)kTcRows * H * 2;
-  uint8_t* const Bs[2] = {B0, B0 + stage_bytes};
-  float* const sb1 = reinterpret_cast<float*>(B0 + 2 * (size_t)stage_bytes);
+  float* const sb1 = reinterpret_cast<float*>(B0 + (size_t)kTcStages * stage_bytes);
   float* const sb2 = sb1 + H;
   float* const sw3 = sb2 + H;  // [2][H]
   float* const spart = sw3 + 2 * H;  // [4 column quarters][128 rows][2]
@@ -340,10 +340,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   int const r = quarter * 32 + lane;             // row of this thread in the epilogues
   int const cols = H / 4, c_begin = cq * cols;
   uint32_t const idesc = tc::idesc_bf16_f32(128, (uint32_t)NM);
+  // The weight stream is one ring of jobs: jobs 0 .. quarters-1 are the
+  // column blocks of W1 (K = 64), then job quarters + kb * quarters + q is
+  // (K tile kb, column block q) of W2. Job j lives in stage j % kTcStages.
+  int const jobs1 = quarters, jobs = quarters + (H / 64) * quarters;
+  auto job_src = [&](int j) -> uint8_t const* {
+    if (j < jobs1) return p.w1img + (size_t)j * stage_bytes;
+    int const u = j - jobs1, kb = u / quarters, q = u % quarters;
+    return p.w2img + ((size_t)kb * H + (size_t)q * NM) * 128;
+  };
+  auto stage = [&](int j) { return B0 + (size_t)(j % kTcStages) * stage_bytes; };
 
   if (t == 0) {
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&full1[i], 1);
+    for (int i = 0; i < kTcStages; ++i) {
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&empty[i], 1);
     }
@@ -385,39 +394,57 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   tc::fence_after_sync();
   uint32_t const tmem = tmem_slot;
 
-  // ---- layer 1: both N halves of W1 at once, 4 MMAs (K = 16 each) per half
+  // Issues the MMAs of ring job j (waiting for its stage), commits them to
+  // empty[stage], and refills the stage of job j - 1 with job j - 1 + stages
+  // once job j - 1's MMAs are done (thread 0 only).
+  auto run_job = [&](int j) -> bool {
+    if (!tc::mbar_wait(&full[j % kTcStages], (uint32_t)(j / kTcStages) & 1, kTcWaitNs)) return false;
+    tc::fence_after_sync();
+    bool const l1 = j < jobs1;
+    int const u = l1 ? 0 : j - jobs1;
+    int const kb = l1 ? 0 : u / quarters, q = l1 ? j : u % quarters;
+    uint32_t const at = tc::smem_u32(A) + (uint32_t)(kb * kTcRows * 128), b0 = tc::smem_u32(stage(j));
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      tc::mma_bf16(tmem + (uint32_t)(q * NM), tc::desc_sw128(at + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
+                   (kb > 0 || k > 0) ? 1u : 0u);
+    tc::mma_commit(&empty[j % kTcStages]);
+    int const jp = j - 1, jn = j - 1 + kTcStages;
+    // layer-1 stages are refilled after the layer-1 MMAs (see below)
+    if (jp >= jobs1 && jn < jobs) {
+      if (!tc::mbar_wait(&empty[jp % kTcStages], (uint32_t)(jp / kTcStages) & 1, kTcWaitNs)) return false;
+      tc::mbar_expect_tx(&full[jn % kTcStages], stage_bytes);
+      tc::bulk_g2s(stage(jn), job_src(jn), stage_bytes, &full[jn % kTcStages]);
+    }
+    return true;
+  };
+
+  // ---- layer 1: the W1 column blocks fill the ring, one MMA group each
   if (t == 0) {
-    for (int h = 0; h < halves; ++h) {
-      tc::mbar_expect_tx(&full1[h], stage_bytes);
-      tc::bulk_g2s(Bs[h], p.w1img + (size_t)h * stage_bytes, stage_bytes, &full1[h]);
+    for (int j = 0; j < kTcStages && j < jobs; ++j) {
+      tc::mbar_expect_tx(&full[j], stage_bytes);
+      tc::bulk_g2s(stage(j), job_src(j), stage_bytes, &full[j]);
     }
     bool ok = true;
-    for (int h = 0; h < halves && ok; ++h) {
-      ok = tc::mbar_wait(&full1[h], 0, kTcWaitNs);
-      if (!ok) break;
-      tc::fence_after_sync();
-      uint32_t const a0 = tc::smem_u32(A), b0 = tc::smem_u32(Bs[h]);
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        tc::mma_bf16(tmem + (uint32_t)(h * NM), tc::desc_sw128(a0 + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
-                     k > 0);
-    }
+    for (int j = 0; j < jobs1 && ok; ++j) ok = run_job(j);
     if (ok) tc::mma_commit(&done);
-    else abort_flag = 1;
+    // refill the stages of the layer-1 jobs with the first W2 jobs as their
+    // MMAs complete (overlaps epilogue 1)
+    for (int j = 0; j < jobs1 && ok; ++j) {
+      int const jn = j + kTcStages;
+      if (jn >= jobs || jn < kTcStages) continue;
+      ok = tc::mbar_wait(&empty[j % kTcStages], (uint32_t)(j / kTcStages) & 1, kTcWaitNs);
+      if (!ok) break;
+      tc::mbar_expect_tx(&full[jn % kTcStages], stage_bytes);
+      tc::bulk_g2s(stage(jn), job_src(jn), stage_bytes, &full[jn % kTcStages]);
+    }
+    if (!ok) abort_flag = 1;
   }
   __syncwarp();
   __syncthreads();
   bool ok = abort_flag == 0;
   if (ok) ok = tc::mbar_wait(&done, 0, kTcWaitNs);
   tc::fence_after_sync();
-  int const tiles2 = H / 64, jobs = tiles2 * halves;
-  // stages are free again: start streaming W2 (jobs (tile, half), two ahead)
-  if (t == 0 && ok)
-    for (int j = 0; j < 2 && j < jobs; ++j) {
-      int const kb = j / halves, h = j % halves;
-      tc::mbar_expect_tx(&full[j], stage_bytes);
-      tc::bulk_g2s(Bs[j], p.w2img + ((size_t)kb * H + (size_t)h * NM) * 128, stage_bytes, &full[j]);
-    }
   __syncwarp();
   uint32_t const lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
   // ---- epilogue 1: h1 = tanh(acc + b1) -> BF16 -> A tiles (row r, this
@@ -447,30 +474,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   __syncthreads();
   ok = abort_flag == 0;
 
-  // ---- layer 2: job j = (K tile j / halves, N half j % halves) in stage j & 1
+  // ---- layer 2: ring jobs jobs1 .. jobs-1
   if (t == 0 && ok) {
-    uint32_t const a0 = tc::smem_u32(A);
-    for (int j = 0; j < jobs && ok; ++j) {
-      int const s = j & 1, kb = j / halves, h = j % halves;
-      ok = tc::mbar_wait(&full[s], (uint32_t)(j >> 1) & 1, kTcWaitNs);
-      if (!ok) break;
-      tc::fence_after_sync();
-      uint32_t const b0 = tc::smem_u32(Bs[s]), at = a0 + (uint32_t)(kb * kTcRows * 128);
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        tc::mma_bf16(tmem + (uint32_t)(h * NM), tc::desc_sw128(at + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
-                     (kb > 0 || k > 0) ? 1u : 0u);
-      tc::mma_commit(&empty[s]);
-      // refill the stage of job j - 1 with job j + 1 once its MMAs are done
-      if (j >= 1 && j + 1 < jobs) {
-        int const sp = (j - 1) & 1;
-        ok = tc::mbar_wait(&empty[sp], (uint32_t)((j - 1) >> 1) & 1, kTcWaitNs);
-        if (!ok) break;
-        int const kn = (j + 1) / halves, hn = (j + 1) % halves;
-        tc::mbar_expect_tx(&full[sp], stage_bytes);
-        tc::bulk_g2s(Bs[sp], p.w2img + ((size_t)kn * H + (size_t)hn * NM) * 128, stage_bytes, &full[sp]);
-      }
-    }
+    for (int j = jobs1; j < jobs && ok; ++j) ok = run_job(j);
     if (ok) tc::mma_commit(&done);
     else abort_flag = 1;
   }

@@ -348,7 +348,8 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
     double const target =
         rel_floor > 0.0 ? std::max(0.5 * tol_true, rel_floor * std::max(1.0, std::fabs(theta[0]))) : 0.5 * tol_true;
     bool const est_ok = worst <= target;
-    if (est_ok || full) {
+    bool const last = out.steps >= max_steps;
+    if (est_ok || last) {
       // Ritz vectors and true residuals (FP64)
       bool all = true;
       out.theta.assign(want, 0.0);
@@ -373,14 +374,12 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
         out.resid[i] = std::sqrt(rr / pp);
         if (!(out.resid[i] <= tol_true)) all = false;
       }
-      if (all || (rel_floor > 0.0 && est_ok) || out.steps >= max_steps) {
+      if (all || (rel_floor > 0.0 && est_ok) || last) {
         out.converged = all || (rel_floor > 0.0 && est_ok);
         return LS_SUCCESS;
       }
-      if (!full) {
-        k = n;
-        continue;
-      }
+    }
+    if (full) {
       // ---- thick restart: keep the lowest `keep` Ritz vectors, then v_n
       uint32_t const keep = std::min<uint32_t>(n - 1, std::max<uint32_t>(nev + 1, m / 2));
       std::vector<double> Y((size_t)n * keep);
