@@ -41,6 +41,10 @@ METRIC = "time-to-ground-state (resid<=1e-8) vs plain FP64 GPU Lanczos; matvec H
 # seed-1234 Philox start vector (the CPU restatement runs the same algorithm
 # from the same start vector and needs the same number of matvecs).
 SQUARE6_STEPS = 57  # 56 Lanczos steps + the final residual check
+# DRAM bytes (read + write) of one k_spmv launch on the 6x6 workload, from one
+# ncu capture (profiles/k_spmv_square6_traffic.md): 4 935 736 320 read +
+# 124 209 920 written.
+SPMV_TRAFFIC_BYTES = 4935736320 + 124209920
 
 
 def workload_model(name: str, hamming_weight: int | None = None):
@@ -441,6 +445,9 @@ def main():
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
     ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
     ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
+    ap.add_argument("--profile-case", default=None, choices=["mlp", "batch16"],
+                    help="one small run of a single kernel family, for profilers: the tensor-core MLP "
+                         "inference over 2^20 random 36-spin states, or a 16-chain batched solve")
     args = ap.parse_args()
     args.precision_code = 0 if args.precision == "fp64" else 1
     rank = int(os.environ.get("RANK", "0"))
@@ -457,6 +464,22 @@ def main():
         dist = tdist
     import __graft_entry__ as g
     g.build()
+    if args.profile_case == "mlp":
+        import numpy as np
+        from spined.learned import Mlp
+        net = Mlp(36, 512, seed=1)
+        st = np.random.default_rng(0).integers(0, 2 ** 36, size=1 << 20, dtype=np.uint64)
+        out = net.forward(st)
+        print(json.dumps({"case": "mlp", "states": len(st), "tensor_cores": net.uses_tensor_cores,
+                          "max_abs": float(np.abs(out).max())}))
+        return
+    if args.profile_case == "batch16":
+        from spined import internal as I, lattices
+        from spined.model import build_model
+        built = [build_model(lattices.heisenberg_chain(16 + 2 * (k % 4), j2=0.05 * k)) for k in range(16)]
+        r = I.eigh_batched([b.hamiltonian for b in built], nev=4, vectors=False)
+        print(json.dumps({"case": "batch16", "kernel_ms": r.kernel_ms, "max_residual": float(r.residuals.max())}))
+        return
     if args.once:
         from spined import internal as I
         from spined.model import build_model
@@ -497,7 +520,8 @@ def main():
             "gpu_launches": r["launches"],
             "e2e": {"value": r["e2e_s"], "unit": "s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
             "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
-                         "frac": r["achieved"] / r["peak"], "traffic": None,
+                         "frac": r["achieved"] / r["peak"],
+                         "traffic": SPMV_TRAFFIC_BYTES if args.workload == "square6" else None,
                          "kernel": "k_spmv (streamed SELL-32 SpMV, FP64)", "spmv_ms": r["spmv_ms"],
                          "alg_bytes": r["alg_bytes"], "compulsory_bytes": r["compulsory_bytes"],
                          "peak_kind": r["peak_kind"]},

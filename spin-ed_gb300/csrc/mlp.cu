@@ -296,8 +296,10 @@ unsigned blocks_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<
 // columns; one thread issues the copies and the MMAs, four warps run the
 // epilogues (warp w owns TMEM lanes / rows 32 w .. 32 w + 31).
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 512;  // 16 warps: 4 per TMEM lane quarter
-constexpr uint64_t kTcWaitNs = 1000000000ull;  // 1 s per wait: far beyond any MMA or copy
+constexpr int kTcEpiWarps = 16;                    // 4 per TMEM lane quarter
+constexpr int kTcThreads = (kTcEpiWarps + 2) * 32;  // + one copy warp + one MMA warp
+constexpr int kTcStages = 5;                        // ring of weight stages, 128 rows x 128 B (16 KB) each
+constexpr uint64_t kTcWaitNs = 1000000000ull;       // 1 s per wait: far beyond any MMA or copy
 
 struct MlpTcArgs {
   uint64_t const* states;
@@ -313,21 +315,30 @@ struct MlpTcArgs {
   int* error;
 };
 
-// dynamic shared memory: A tiles, two B stages, b1, b2, W3 (FP32), partials
-constexpr int kTcStages = 4;  // ring of weight stages, 128 rows x 128 B (16 KB) each
-
+// dynamic shared memory: A tiles, the weight ring, b1, b2, W3 (FP32), partials
 size_t tc_smem_bytes(int hidden) {
   return (size_t)kTcRows * hidden * 2 + (size_t)kTcStages * 128 * 128 + 4 * (size_t)hidden * 4 +
-         (size_t)kTcThreads * 2 * 4 + 1024;
+         (size_t)kTcEpiWarps * 32 * 2 * 4 + 1024;
 }
 
+__device__ __forceinline__ void epi_sync() {  // the 512 epilogue threads only
+  asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32) : "memory");
+}
+
+// Warp-specialised: warp 16 streams the weights through the ring (waiting
+// only for a stage's previous MMAs to finish), warp 17 issues the MMAs as
+// soon as a stage lands (never waiting for MMA completion), warps 0-15 run
+// the epilogues. The weight stream is one sequence of jobs: jobs
+// 0 .. H/128-1 are the 128-row blocks of W1 (K = 64), then job
+// H/128 + kb * H/128 + q is (K tile kb, row block q) of W2; job j lives in
+// stage j % kTcStages.
 __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full[kTcStages], empty[kTcStages], done;
+  __shared__ uint64_t full[kTcStages], empty[kTcStages], done, h1_ready;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   uint8_t* const smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  int const H = p.hidden, NM = 128, quarters = H / NM;  // N = 128 per MMA, H / 128 column blocks
+  int const H = p.hidden, NM = 128, blocks = H / NM;
   uint32_t const stage_bytes = (uint32_t)NM * 128;
   uint8_t* const A = smem;  // H/64 tiles of 128 rows x 128 B
   uint8_t* const B0 = smem + (size_t)kTcRows * H * 2;
@@ -336,17 +347,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   float* const sw3 = sb2 + H;  // [2][H]
   float* const spart = sw3 + 2 * H;  // [4 column quarters][128 rows][2]
   int const t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  int const quarter = warp & 3, cq = warp >> 2;  // TMEM lane quarter, column quarter
-  int const r = quarter * 32 + lane;             // row of this thread in the epilogues
-  int const cols = H / 4, c_begin = cq * cols;
-  uint32_t const idesc = tc::idesc_bf16_f32(128, (uint32_t)NM);
-  // The weight stream is one ring of jobs: jobs 0 .. quarters-1 are the
-  // column blocks of W1 (K = 64), then job quarters + kb * quarters + q is
-  // (K tile kb, column block q) of W2. Job j lives in stage j % kTcStages.
-  int const jobs1 = quarters, jobs = quarters + (H / 64) * quarters;
+  int const jobs1 = blocks, jobs = blocks + (H / 64) * blocks;
   auto job_src = [&](int j) -> uint8_t const* {
     if (j < jobs1) return p.w1img + (size_t)j * stage_bytes;
-    int const u = j - jobs1, kb = u / quarters, q = u % quarters;
+    int const u = j - jobs1, kb = u / blocks, q = u % blocks;
     return p.w2img + ((size_t)kb * H + (size_t)q * NM) * 128;
   };
   auto stage = [&](int j) { return B0 + (size_t)(j % kTcStages) * stage_bytes; };
@@ -357,6 +361,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
       tc::mbar_init(&empty[i], 1);
     }
     tc::mbar_init(&done, 1);
+    tc::mbar_init(&h1_ready, 1);
     abort_flag = 0;
     tc::fence_mbar_init();
   }
@@ -368,9 +373,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
     sw3[c] = __bfloat162float(p.W3[c]);
     sw3[H + c] = __bfloat162float(p.W3[H + c]);
   }
-  // X tile: row xr, input j -> BF16 +1 / -1, zero for j >= n_in; four threads
-  // per row, two 16-byte chunks each
-  {
+  if (t < kTcEpiWarps * 32) {
+    // X tile: row xr, input j -> BF16 +1 / -1, zero for j >= n_in; four
+    // threads per row, two 16-byte chunks each
     int const xr = t & 127, part = t >> 7;
     int64_t const xrow = (int64_t)blockIdx.x * kTcRows + xr;
     uint64_t const s = xrow < p.n ? p.states[xrow] : 0;
@@ -394,128 +399,122 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   tc::fence_after_sync();
   uint32_t const tmem = tmem_slot;
 
-  // Issues the MMAs of ring job j (waiting for its stage), commits them to
-  // empty[stage], and refills the stage of job j - 1 with job j - 1 + stages
-  // once job j - 1's MMAs are done (thread 0 only).
-  auto run_job = [&](int j) -> bool {
-    if (!tc::mbar_wait(&full[j % kTcStages], (uint32_t)(j / kTcStages) & 1, kTcWaitNs)) return false;
+  if (warp == kTcEpiWarps) {
+    // ---- copy warp: keep the ring full
+    if (lane == 0) {
+      for (int j = 0; j < jobs; ++j) {
+        int const st = j % kTcStages, use = j / kTcStages;
+        if (use > 0 && !tc::mbar_wait(&empty[st], (uint32_t)(use - 1) & 1, kTcWaitNs)) {
+          abort_flag = 1;
+          break;
+        }
+        tc::mbar_expect_tx(&full[st], stage_bytes);
+        tc::bulk_g2s(stage(j), job_src(j), stage_bytes, &full[st]);
+      }
+    }
+    __syncwarp();
+  } else if (warp == kTcEpiWarps + 1) {
+    // ---- MMA warp
+    if (lane == 0) {
+      uint32_t const idesc = tc::idesc_bf16_f32(128, (uint32_t)NM);
+      bool ok = true;
+      for (int j = 0; j < jobs && ok; ++j) {
+        if (j == jobs1) {
+          tc::mma_commit(&done);  // layer 1 complete -> epilogue 1
+          ok = tc::mbar_wait(&h1_ready, 0, kTcWaitNs);
+          if (!ok) break;
+          tc::fence_after_sync();
+        }
+        int const st = j % kTcStages;
+        ok = tc::mbar_wait(&full[st], (uint32_t)(j / kTcStages) & 1, kTcWaitNs);
+        if (!ok) break;
+        tc::fence_after_sync();
+        bool const l1 = j < jobs1;
+        int const u = l1 ? 0 : j - jobs1;
+        int const kb = l1 ? 0 : u / blocks, q = l1 ? j : u % blocks;
+        uint32_t const at = tc::smem_u32(A) + (uint32_t)(kb * kTcRows * 128), b0 = tc::smem_u32(stage(j));
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          tc::mma_bf16(tmem + (uint32_t)(q * NM), tc::desc_sw128(at + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
+                       (kb > 0 || k > 0) ? 1u : 0u);
+        tc::mma_commit(&empty[st]);
+      }
+      if (ok) tc::mma_commit(&done);  // layer 2 complete -> epilogue 2
+      else abort_flag = 1;
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
+    // rows) and the column quarter w / 4
+    int const quarter = warp & 3, cq = warp >> 2;
+    int const r = quarter * 32 + lane;
+    int const cols = H / 4, c_begin = cq * cols;
+    uint32_t const lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+    bool ok = tc::mbar_wait(&done, 0, kTcWaitNs);
     tc::fence_after_sync();
-    bool const l1 = j < jobs1;
-    int const u = l1 ? 0 : j - jobs1;
-    int const kb = l1 ? 0 : u / quarters, q = l1 ? j : u % quarters;
-    uint32_t const at = tc::smem_u32(A) + (uint32_t)(kb * kTcRows * 128), b0 = tc::smem_u32(stage(j));
+    __syncwarp();
+    // epilogue 1: h1 = tanh(acc + b1) -> BF16 -> A tiles
+    if (ok) {
+      for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
+        float v[32];
+        tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
+        uint32_t pk[16];
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-      tc::mma_bf16(tmem + (uint32_t)(q * NM), tc::desc_sw128(at + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
-                   (kb > 0 || k > 0) ? 1u : 0u);
-    tc::mma_commit(&empty[j % kTcStages]);
-    int const jp = j - 1, jn = j - 1 + kTcStages;
-    // layer-1 stages are refilled after the layer-1 MMAs (see below)
-    if (jp >= jobs1 && jn < jobs) {
-      if (!tc::mbar_wait(&empty[jp % kTcStages], (uint32_t)(jp / kTcStages) & 1, kTcWaitNs)) return false;
-      tc::mbar_expect_tx(&full[jn % kTcStages], stage_bytes);
-      tc::bulk_g2s(stage(jn), job_src(jn), stage_bytes, &full[jn % kTcStages]);
-    }
-    return true;
-  };
-
-  // ---- layer 1: the W1 column blocks fill the ring, one MMA group each
-  if (t == 0) {
-    for (int j = 0; j < kTcStages && j < jobs; ++j) {
-      tc::mbar_expect_tx(&full[j], stage_bytes);
-      tc::bulk_g2s(stage(j), job_src(j), stage_bytes, &full[j]);
-    }
-    bool ok = true;
-    for (int j = 0; j < jobs1 && ok; ++j) ok = run_job(j);
-    if (ok) tc::mma_commit(&done);
-    // refill the stages of the layer-1 jobs with the first W2 jobs as their
-    // MMAs complete (overlaps epilogue 1)
-    for (int j = 0; j < jobs1 && ok; ++j) {
-      int const jn = j + kTcStages;
-      if (jn >= jobs || jn < kTcStages) continue;
-      ok = tc::mbar_wait(&empty[j % kTcStages], (uint32_t)(j / kTcStages) & 1, kTcWaitNs);
-      if (!ok) break;
-      tc::mbar_expect_tx(&full[jn % kTcStages], stage_bytes);
-      tc::bulk_g2s(stage(jn), job_src(jn), stage_bytes, &full[jn % kTcStages]);
-    }
-    if (!ok) abort_flag = 1;
-  }
-  __syncwarp();
-  __syncthreads();
-  bool ok = abort_flag == 0;
-  if (ok) ok = tc::mbar_wait(&done, 0, kTcWaitNs);
-  tc::fence_after_sync();
-  __syncwarp();
-  uint32_t const lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-  // ---- epilogue 1: h1 = tanh(acc + b1) -> BF16 -> A tiles (row r, this
-  // warp's column quarter, 32 columns = four 16-byte chunks per load)
-  if (ok) {
-    for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
-      float v[32];
-      tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
-      uint32_t pk[16];
+        for (int q = 0; q < 16; ++q)
+          pk[q] = tc::pack_bf16x2(tc::tanh_fast(v[2 * q] + sb1[c0 + 2 * q]),
+                                  tc::tanh_fast(v[2 * q + 1] + sb1[c0 + 2 * q + 1]));
+        uint8_t* const tile = A + (size_t)(c0 >> 6) * (kTcRows * 128) + r * 128;
 #pragma unroll
-      for (int q = 0; q < 16; ++q)
-        pk[q] = tc::pack_bf16x2(tc::tanh_fast(v[2 * q] + sb1[c0 + 2 * q]), tc::tanh_fast(v[2 * q + 1] + sb1[c0 + 2 * q + 1]));
-      uint8_t* const tile = A + (size_t)(c0 >> 6) * (kTcRows * 128) + r * 128;
-#pragma unroll
-      for (int q4 = 0; q4 < 4; ++q4) {
-        int const chunk = (((c0 & 63) >> 3) + q4) ^ (r & 7);
-        *reinterpret_cast<uint4*>(tile + (chunk << 4)) =
-            make_uint4(pk[4 * q4], pk[4 * q4 + 1], pk[4 * q4 + 2], pk[4 * q4 + 3]);
+        for (int q4 = 0; q4 < 4; ++q4) {
+          int const chunk = (((c0 & 63) >> 3) + q4) ^ (r & 7);
+          *reinterpret_cast<uint4*>(tile + (chunk << 4)) =
+              make_uint4(pk[4 * q4], pk[4 * q4 + 1], pk[4 * q4 + 2], pk[4 * q4 + 3]);
+        }
       }
     }
-  }
-  tc::fence_proxy_async_smem();
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  if (!ok) abort_flag = 1;
-  __syncthreads();
-  ok = abort_flag == 0;
-
-  // ---- layer 2: ring jobs jobs1 .. jobs-1
-  if (t == 0 && ok) {
-    for (int j = jobs1; j < jobs && ok; ++j) ok = run_job(j);
-    if (ok) tc::mma_commit(&done);
-    else abort_flag = 1;
-  }
-  __syncwarp();
-  __syncthreads();
-  ok = abort_flag == 0;
-  if (ok) ok = tc::mbar_wait(&done, 1, kTcWaitNs);
-  tc::fence_after_sync();
-  __syncwarp();
-  // ---- epilogue 2: h2 = tanh(acc + b2); partial (a, s) = W3 h2 over this
-  // warp's column quarter, summed over the quarters through shared memory
-  float a = 0.0f, sg = 0.0f;
-  if (ok) {
-    for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
-      float v[32];
-      tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    epi_sync();
+    if (t == 0) {
+      if (!ok) abort_flag = 1;
+      tc::mbar_arrive(&h1_ready);
+    }
+    if (ok) ok = tc::mbar_wait(&done, 1, kTcWaitNs);
+    tc::fence_after_sync();
+    __syncwarp();
+    // epilogue 2: h2 = tanh(acc + b2); partial (a, s) over this column quarter
+    float a = 0.0f, sg = 0.0f;
+    if (ok) {
+      for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
+        float v[32];
+        tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
 #pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        float const hq = tc::tanh_fast(v[q] + sb2[c0 + q]);
-        a = fmaf(sw3[c0 + q], hq, a);
-        sg = fmaf(sw3[H + c0 + q], hq, sg);
+        for (int q = 0; q < 32; ++q) {
+          float const hq = tc::tanh_fast(v[q] + sb2[c0 + q]);
+          a = fmaf(sw3[c0 + q], hq, a);
+          sg = fmaf(sw3[H + c0 + q], hq, sg);
+        }
       }
     }
+    spart[(cq * kTcRows + r) * 2] = a;
+    spart[(cq * kTcRows + r) * 2 + 1] = sg;
+    tc::fence_before_sync();
+    epi_sync();
+    if (t < kTcRows) {
+      int64_t const row = (int64_t)blockIdx.x * kTcRows + t;
+      float sa = __ldg(p.b3), ss = __ldg(p.b3 + 1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        sa += spart[(q * kTcRows + t) * 2];
+        ss += spart[(q * kTcRows + t) * 2 + 1];
+      }
+      if (ok && row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
+    }
+    if (!ok && lane == 0) atomicExch(p.error, 1);
   }
-  spart[(cq * kTcRows + r) * 2] = a;
-  spart[(cq * kTcRows + r) * 2 + 1] = sg;
   tc::fence_before_sync();
   __syncthreads();
-  if (ok && t < kTcRows) {
-    int64_t const row = (int64_t)blockIdx.x * kTcRows + t;
-    float sa = __ldg(p.b3), ss = __ldg(p.b3 + 1);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      sa += spart[(q * kTcRows + t) * 2];
-      ss += spart[(q * kTcRows + t) * 2 + 1];
-    }
-    if (row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
-  }
-  if (!ok && (t & 31) == 0) atomicExch(p.error, 1);
+  if (abort_flag && t == 0) atomicExch(p.error, 1);
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, (uint32_t)H);

@@ -13,12 +13,14 @@
 // Converged pairs (estimate beta |y_{last,i}| <= tol / 2) are checked with
 // their true residual ||H psi - theta psi|| computed in FP64.
 //
-// Storage S = double (SED_PRECISION_FP64) or float (SED_PRECISION_MIXED):
-// with float the Krylov vectors and w are stored in FP32 while the matvec
-// arithmetic, the dot products, norms, updates, T and its eigensolve are
-// FP64. The FP32 phase stops at the FP32 floor (a residual of about 1e-6
-// of |theta|); its FP64 Ritz vector then starts an FP64 thick-restart phase
-// with at most 10 stored vectors that refines it to the tolerance.
+// Storage S = double (SED_PRECISION_FP64) or float (SED_PRECISION_MIXED).
+// With float the Krylov vectors and w are stored in FP32 and the phase
+// computes in FP32 (the streamed FP32 SpMV; FP32 products in the
+// projections with per-block partial sums in FP64), while T, its
+// eigensolve, the Ritz vectors and their residuals are FP64. The FP32 phase
+// stops at the FP32 floor (a residual of about 1e-6 of |theta|); its FP64
+// Ritz vector then starts an FP64 thick-restart phase with at most 10 stored
+// vectors that refines it to the tolerance.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -36,24 +38,38 @@ constexpr int kDotCols = 8;
 template <class S>
 __device__ __forceinline__ double ldv(S const* p, uint64_t i) { return (double)p[i]; }
 
+// Arithmetic type of the projections: FP64 for FP64 storage; for FP32
+// storage FP32 products and per-thread sums (GB300's FP64 pipe is slower
+// than HBM for these streams, and converting every FP32 element to FP64
+// would occupy it too), with the per-thread partials summed in FP64.
+template <class S>
+struct Arith {
+  using T = double;
+};
+template <>
+struct Arith<float> {
+  using T = float;
+};
+
 // partial[(g * gridDim.x + b) * 8 + c] = sum over this block's rows of
 // V[:, 8 g + c] . w  (columns >= ncols give 0); blockIdx.y = g.
 template <class S>
 __global__ void __launch_bounds__(256) k_tdots(S const* __restrict__ V, uint64_t ld, uint32_t ncols,
                                                S const* __restrict__ w, uint64_t D, double* __restrict__ partial) {
+  using T = typename Arith<S>::T;
   __shared__ double red[8][kDotCols];
   uint32_t const c0 = blockIdx.y * kDotCols;
-  double acc[kDotCols] = {};
+  T acc[kDotCols] = {};
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x) {
-    double const wr = ldv(w, r);
+    T const wr = (T)w[r];
 #pragma unroll
     for (int c = 0; c < kDotCols; ++c)
-      if (c0 + c < ncols) acc[c] = fma(ldv(V, (uint64_t)(c0 + c) * ld + r), wr, acc[c]);
+      if (c0 + c < ncols) acc[c] = fma((T)V[(uint64_t)(c0 + c) * ld + r], wr, acc[c]);
   }
   int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int c = 0; c < kDotCols; ++c) {
-    double x = acc[c];
+    double x = (double)acc[c];
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     if (lane == 0) red[warp][c] = x;
   }
@@ -69,12 +85,13 @@ __global__ void __launch_bounds__(256) k_tdots(S const* __restrict__ V, uint64_t
 template <class S>
 __global__ void k_tupdate(S const* __restrict__ V, uint64_t ld, uint32_t ncols, double const* __restrict__ coef,
                           S* __restrict__ w, uint64_t D) {
-  __shared__ double cf[kMaxThick + 1];
-  for (uint32_t c = threadIdx.x; c < ncols; c += blockDim.x) cf[c] = coef[c];
+  using T = typename Arith<S>::T;
+  __shared__ T cf[kMaxThick + 1];
+  for (uint32_t c = threadIdx.x; c < ncols; c += blockDim.x) cf[c] = (T)coef[c];
   __syncthreads();
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x) {
-    double x = ldv(w, r);
-    for (uint32_t c = 0; c < ncols; ++c) x = fma(-ldv(V, (uint64_t)c * ld + r), cf[c], x);
+    T x = (T)w[r];
+    for (uint32_t c = 0; c < ncols; ++c) x = fma(-(T)V[(uint64_t)c * ld + r], cf[c], x);
     w[r] = (S)x;
   }
 }
@@ -308,7 +325,15 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
   out = ThickResult{};
   while (true) {
     // ---- one Lanczos step from v_k
-    if (int st = operator_apply_device(op, dtype, 1, V + (uint64_t)k * D, D, w, D, stream, SED_FORM_AUTO)) return st;
+    if constexpr (std::is_same<S, float>::value) {
+      if (op.stream.ready && op.stream.diag_f.ptr) {
+        if (int st = operator_apply32(op, V + (uint64_t)k * D, w, stream)) return st;
+      } else if (int st = operator_apply_device(op, dtype, 1, V + (uint64_t)k * D, D, w, D, stream, SED_FORM_AUTO)) {
+        return st;
+      }
+    } else if (int st = operator_apply_device(op, dtype, 1, V + (uint64_t)k * D, D, w, D, stream, SED_FORM_AUTO)) {
+      return st;
+    }
     ++out.matvecs;
     ++out.steps;
     if (int st = dots(k + 1, w, c)) return st;
@@ -451,6 +476,8 @@ int solve_thick(OperatorData& op, int out_dtype, sed_eigh_options const& o, doub
   ThickResult r32, r64;
   uint64_t fp32_steps = 0;
   if (o.precision == SED_PRECISION_MIXED) {
+    if (op.stream.ready)
+      if (int st = operator_prepare_fp32(op, stream)) return st;
     // FP32-stored phase down to the FP32 floor, then FP64 refinement of its
     // Ritz vector with at most 10 stored FP64 vectors
     if (int st = thick_run<float>(op, stream, m, nev, tol, 1e-6, start_ptr, o.seed, max_iter, psi.as<double>(), r32))
