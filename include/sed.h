@@ -359,6 +359,12 @@ SED_API int sed_mlp_set_path(sed_mlp* mlp, int path);
 /* 1 if inference runs on the tensor cores, else 0. */
 SED_API int sed_mlp_uses_tensor_cores(sed_mlp const* mlp);
 
+/* sed_eigh keeps its largest Krylov workspace (the stored basis vectors)
+ * allocated on each device between calls, because freeing tens of GB costs
+ * about 20 ms per call; it is released automatically when another libsed
+ * allocation runs out of memory. This frees it now (all devices). */
+SED_API void sed_release_workspace(void);
+
 /* Number of libsed kernels launched by this process so far (graph replays
  * count their kernel nodes). */
 SED_API uint64_t sed_kernel_launches(void);

@@ -77,11 +77,54 @@ void log_line(char const* fmt, ...) {
   va_end(ap);
 }
 
+// One cached Krylov workspace per device (see krylov_take / krylov_give).
+namespace {
+constexpr int kCacheDevices = 64;
+std::mutex g_cache_mu;
+DeviceBuffer g_krylov_cache[kCacheDevices];
+
+// Frees the cached workspace of `device` (all devices for -1).
+void release_cache(int device) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  for (int d = 0; d < kCacheDevices; ++d)
+    if (device < 0 || d == device) g_krylov_cache[d].reset();
+}
+}  // namespace
+
+int krylov_take(size_t bytes, DeviceBuffer& out) {
+  int dev = -1;
+  if (int st = current_device(&dev)) return st;
+  if (dev >= 0 && dev < kCacheDevices) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    if (g_krylov_cache[dev].ptr && g_krylov_cache[dev].bytes >= bytes) {
+      out = std::move(g_krylov_cache[dev]);
+      return LS_SUCCESS;
+    }
+  }
+  return out.allocate(bytes);
+}
+
+void krylov_give(DeviceBuffer& b) {
+  if (!b.ptr) return;
+  int const dev = b.device;
+  if (dev >= 0 && dev < kCacheDevices) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    if (b.bytes > g_krylov_cache[dev].bytes) std::swap(g_krylov_cache[dev], b);
+  }
+  b.reset();
+}
+
 int DeviceBuffer::allocate(size_t n) {
   reset();
   if (int st = current_device(&device)) return st;
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, n ? n : 1);
+  if (e == cudaErrorMemoryAllocation) {
+    // the cached Krylov workspace may hold the memory: free it and retry once
+    cudaGetLastError();
+    release_cache(device);
+    e = cudaMalloc(&p, n ? n : 1);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     return fail(e == cudaErrorMemoryAllocation ? LS_OUT_OF_MEMORY : LS_CUDA_ERROR,
@@ -132,6 +175,9 @@ int current_device(int* device) {
 using namespace sed;
 
 extern "C" {
+
+void sed_release_workspace(void) { release_cache(-1); }
+
 
 char const* ls_error_to_string(int status) {
   std::string s = describe(status);

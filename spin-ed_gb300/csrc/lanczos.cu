@@ -588,6 +588,7 @@ struct Solver {
   ~Solver() {
     if (graph) cudaGraphExecDestroy(graph);
     if (hh) cudaFreeHost(hh);
+    krylov_give(ws.V);
   }
 
   X* V() const { return ws.V.as<X>(); }
@@ -597,7 +598,7 @@ struct Solver {
     m_max = m;
     int dev = op.basis->device;
     vblocks = grid_size(D, dev, 8);
-    if (int st = ws.V.allocate((size_t)m_max * D * sizeof(X))) return st;
+    if (int st = krylov_take((size_t)m_max * D * sizeof(X), ws.V)) return st;
     if (int st = ws.header.allocate(sizeof(LzHeader))) return st;
     if (int st = ws.alpha.allocate((size_t)m_max * 8)) return st;
     if (int st = ws.beta.allocate((size_t)m_max * 8)) return st;
@@ -984,7 +985,11 @@ int solve_mixed(OperatorData& op, int out_dtype, sed_eigh_options const& o, doub
   DeviceBuffer psi, y, V, hdr_b, alpha, beta, sbuf, work, partial;
   if (int st = psi.allocate(D * 8)) return st;
   if (int st = y.allocate(D * 8)) return st;
-  if (int st = V.allocate((size_t)m * D * 4)) return st;
+  struct KrylovGuard {
+    DeviceBuffer& b;
+    ~KrylovGuard() { krylov_give(b); }
+  } krylov_guard{V};
+  if (int st = krylov_take((size_t)m * D * 4, V)) return st;
   if (int st = hdr_b.allocate(sizeof(LzHeader))) return st;
   if (int st = alpha.allocate((size_t)m * 8)) return st;
   if (int st = beta.allocate((size_t)m * 8)) return st;

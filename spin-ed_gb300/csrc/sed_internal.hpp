@@ -65,6 +65,14 @@ struct DeviceBuffer {
   }
 };
 
+// A device buffer of at least `bytes` for a Krylov basis on the current
+// device: the cached one when it is big enough, else a new allocation.
+int krylov_take(size_t bytes, DeviceBuffer& out);
+// Returns a Krylov basis buffer: the larger of it and the cached one stays
+// cached (sed_eigh keeps its workspace between calls: freeing tens of GB
+// costs about 20 ms per call), the other is freed.
+void krylov_give(DeviceBuffer& b);
+
 struct ScopedDevice {
   int previous = -1;
   explicit ScopedDevice(int device);

@@ -147,6 +147,7 @@ SIGNATURES = [
     ("sed_mlp_sample", _I, [_P, _P, _U64, _U64, _U64, _P, _P, _P]),
     ("sed_mlp_start_vector", _I, [_P, _P, _P]),
     ("sed_mlp_set_path", _I, [_P, _I]),
+    ("sed_release_workspace", None, []),
     ("sed_mlp_uses_tensor_cores", _I, [_P]),
     ("sed_kernel_launches", _U64, []),
     ("sed_version", C.c_char_p, []),
