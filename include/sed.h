@@ -234,6 +234,19 @@ SED_API int sed_eigh(ls_operator const* op, int dtype, sed_eigh_options const* o
  * sed_eigh with SED_FORM_AUTO); SED_FORM_STREAM and SED_FORM_AUTO record the
  * stream form now (AUTO silently keeps on-the-fly if it does not fit). */
 SED_API int sed_operator_prepare(ls_operator* op, int form);
+/* How the stream form is recorded. AUTO uses the orbit table when the
+ * characters are real and the table fits in 40 % of the free device memory:
+ * a map from every word of the basis's weight class (C(n, w) words, or 2^n
+ * without a Hamming weight; 4 bytes each) to its representative's index and
+ * character sign, filled by enumerating the orbits of the representatives,
+ * after which each generated element costs one rank and one table load.
+ * CANONICALISE always searches the group for each element. Both record
+ * bit-identical stream forms. The setting is process-wide. */
+enum { SED_RECORD_AUTO = 0, SED_RECORD_CANONICALISE = 1 };
+SED_API void sed_set_record_mode(int mode);
+/* 1 if the operator's stream form was recorded through the orbit table. */
+SED_API int sed_operator_recorded_with_table(ls_operator const* op);
+
 /* Bytes the stream form occupies on the device (0 if not recorded). */
 SED_API uint64_t sed_operator_stream_bytes(ls_operator const* op);
 /* Stored elements of the stream form (off-diagonal, per matvec). */

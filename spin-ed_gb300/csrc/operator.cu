@@ -363,6 +363,137 @@ void root_of_unity(uint32_t q, uint32_t L, double& re, double& im) {
   }
 }
 
+// ------------------------------------------------------------ orbit table --
+// An alternative to canonicalising every generated element: a table over the
+// whole weight class of the basis (C(n, w) words, or 2^n without a Hamming
+// weight) that maps each word to the index of its orbit's representative and
+// the sign of the character of the element taking it there (real characters
+// only), filled by enumerating the orbit of every representative once. The
+// stream form then costs one rank computation and one table load per element
+// instead of a search over the group. Words of orbits outside the basis keep
+// the fill value kNull.
+
+constexpr uint32_t kTabSign = 0x80000000u;
+
+// Colex rank of x among the words of weight hw (hw >= 0), or x itself.
+__device__ __forceinline__ uint64_t word_rank(uint64_t x, int hw, uint64_t const* __restrict__ bin /* [64][33] */) {
+  if (hw < 0) return x;
+  uint64_t rk = 0;
+  uint32_t i = 0;
+  while (x) {
+    uint32_t const p = (uint32_t)(__ffsll((long long)x) - 1);
+    x &= x - 1;
+    ++i;
+    rk += bin[p * 33 + i];
+  }
+  return rk;
+}
+
+__device__ __forceinline__ void stage_binom(uint64_t const* __restrict__ binom, uint64_t* bin) {
+  for (uint32_t q = threadIdx.x; q < 64 * 33; q += blockDim.x) {
+    uint32_t const p = q / 33, i = q % 33;
+    bin[q] = binom[p * 65 + i];
+  }
+}
+
+// One thread per (representative, coset): every image h(p_c(r)) (and its
+// spin-inverted word) gets table entry j | sign(character of the element).
+// With spin inversion in the group only words whose top bit (n - 1) is clear
+// are stored (their colex ranks are the first C(n - 1, w)): of each pair
+// {z, ~z} the one with the clear top bit is written, once, and a lookup of a
+// word with the top bit set looks up its inverse and flips the sign by the
+// inversion character.
+template <class W>
+__global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const PlanView P, uint64_t const* __restrict__ reps,
+                                                       uint64_t D, int hw, uint64_t const* __restrict__ binom,
+                                                       uint32_t* __restrict__ table, uint64_t space,
+                                                       int* __restrict__ error) {
+  __shared__ uint64_t bin[64 * 33];
+  stage_binom(binom, bin);
+  __syncthreads();
+  uint64_t const t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const j = t / P.n_cosets;
+  uint32_t const c = (uint32_t)(t % P.n_cosets);
+  if (j >= D) return;
+  W const mask = (W)P.mask;
+  W const y = coset_apply<W>((W)reps[j], P, c);
+  uint32_t const pc = P.coset_phase[c];
+  for (uint32_t h = 0; h < P.n_h; ++h) {
+    W const z = shift_apply<W>(y, P.h_mask + (uint64_t)h * P.n_terms, P.h_rot + (uint64_t)h * P.n_terms, P.n_terms);
+    uint32_t const ph = add_phase(pc, P.h_phase[h], P.L);
+    W w = z;
+    uint32_t pw = ph;
+    if (P.inv && ((uint64_t)z >> (P.n_bits - 1)) & 1u) {
+      w = (W)(~z & mask);
+      pw = add_phase(ph, P.inv_phase, P.L);
+    }
+    uint64_t const k0 = word_rank((uint64_t)w, hw, bin);
+    if (k0 < space) table[k0] = (uint32_t)j | (pw ? kTabSign : 0u);
+    else *error = 1;
+  }
+}
+
+// The stream form from the orbit table: one warp per SELL-32 slice, one row
+// per lane, elements in the canonical order of walk_row; same entries, codes,
+// diagonal and row classes as k_record.
+template <bool Real>
+__global__ void __launch_bounds__(256) k_record_table(IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
+                                                      uint64_t n_slices, uint64_t const* __restrict__ slice_ptr,
+                                                      uint32_t col_bits, bool packed, uint32_t* __restrict__ entries,
+                                                      uint16_t* __restrict__ codes, void* __restrict__ diag,
+                                                      uint8_t* __restrict__ row_class, uint32_t const* __restrict__ table,
+                                                      int hw, uint64_t const* __restrict__ binom, uint64_t space,
+                                                      int* __restrict__ error, bool inv_half, bool inv_sign,
+                                                      uint32_t n_bits, uint64_t word_mask) {
+  __shared__ uint64_t bin[64 * 33];
+  stage_binom(binom, bin);
+  __syncthreads();
+  uint32_t const lane = threadIdx.x & 31;
+  uint64_t const s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= n_slices) return;  // warp-uniform
+  uint64_t const i = s * 32 + lane;
+  uint64_t const base = slice_ptr[s];
+  uint32_t const width = (uint32_t)((slice_ptr[s + 1] - base) >> 5);
+  uint32_t count = 0;
+  if (i < I.D) {
+    uint64_t const r = I.reps[i];
+    walk_row(r, T, [&](uint32_t e, uint64_t st, uint32_t vid) {
+      // terms that change the Hamming weight leave the sector: dropped, as
+      // the canonicalising path drops them (their orbit is not in the basis)
+      uint32_t v = kNull;
+      if (hw < 0 || __popcll(st) == hw) {
+        uint64_t w = st;
+        bool const flip = inv_half && ((st >> (n_bits - 1)) & 1u);
+        if (flip) w = ~st & word_mask;
+        uint64_t const k = word_rank(w, hw, bin);
+        if (k < space) v = __ldg(table + k);
+        else *error = 1;
+        if (flip && v != kNull && inv_sign) v ^= kTabSign;
+      }
+      uint32_t ent = kNull, code = 0;
+      if (v != kNull) {
+        uint32_t const jj = v & ~kTabSign;
+        code = element_code(vid, (v & kTabSign) ? 1u : 0u, weights[jj], C);
+        ent = packed ? (jj | (code << col_bits)) : jj;
+      }
+      entries[base + (uint64_t)e * 32 + lane] = ent;
+      if (!packed) codes[base + (uint64_t)e * 32 + lane] = (uint16_t)code;
+      count = e + 1;
+    });
+    if (Real) {
+      static_cast<double*>(diag)[i] = row_diag<double>(r, T);
+    } else {
+      cplx const d = row_diag<cplx>(r, T);
+      static_cast<double2*>(diag)[i] = make_double2(d.re, d.im);
+    }
+    row_class[i] = (uint8_t)divisor_class(weights[i], C);
+  }
+  for (uint32_t e = count; e < width; ++e) {
+    entries[base + (uint64_t)e * 32 + lane] = kNull;
+    if (!packed) codes[base + (uint64_t)e * 32 + lane] = 0;
+  }
+}
+
 }  // namespace
 
 
@@ -542,6 +673,15 @@ int operator_ensure_ready(OperatorData& op) {
   return LS_SUCCESS;
 }
 
+int g_record_mode = SED_RECORD_AUTO;
+
+uint64_t host_binom(unsigned n, unsigned k) {
+  if (k > n) return 0;
+  uint64_t c = 1;
+  for (unsigned i = 1; i <= k; ++i) c = c * (n - k + i) / i;  // exact: c * (n-k+i) is divisible by i
+  return c;
+}
+
 StreamView stream_view(OperatorData const& op) {
   StreamForm const& sf = op.stream;
   OperatorTables const& tb = *op.tables;
@@ -603,10 +743,48 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     if (int st = sf.values.allocate(std::max<uint64_t>(1, n_entries) * 2)) return st;
   if (int st = sf.diag.allocate(std::max<uint64_t>(1, D) * (op.is_real ? 8 : 16))) return st;
   if (int st = sf.row_class.allocate(std::max<uint64_t>(1, D))) return st;
-  if (n_slices) {
+  // orbit-table path: real characters, a weight class small enough to tabulate
+  uint64_t space = 0;
+  bool use_table = false;
+  if (n_slices && g_record_mode != SED_RECORD_CANONICALISE && characters_real(b) && D < kTabSign) {
+    bool const half = b.plan.inv != 0;
+    if (b.hw >= 0 && b.hw <= 32 && b.n <= 64) space = host_binom(half ? b.n - 1 : b.n, (unsigned)b.hw);
+    else if (b.hw < 0 && b.n <= 34) space = (uint64_t)1 << (half ? b.n - 1 : b.n);
+    size_t fr = 0, tt = 0;
+    SED_TRY_CUDA(cudaMemGetInfo(&fr, &tt));
+    use_table = space > 0 && space * 4 <= fr / 5 * 2;
+  }
+  if (use_table) {
+    DeviceBuffer table;
+    struct TableGuard {
+      DeviceBuffer& b;
+      ~TableGuard() { krylov_give(b); }
+    } table_guard{table};
+    DeviceBuffer err;
+    if (int st = err.allocate(16)) return st;
+    if (int st = krylov_take(space * 4, table)) return st;
+    SED_TRY_CUDA(cudaMemsetAsync(table.ptr, 0xFF, space * 4, stream));
+    SED_TRY_CUDA(cudaMemsetAsync(err.ptr, 0, 16, stream));
+    bool const wide = b.plan.n_bits > 32;
+    uint64_t const threads = D * b.plan.n_cosets;
+    unsigned const sgrid = (unsigned)((threads + 255) / 256);
+    if (wide) { k_orbit_scatter<uint64_t><<<sgrid, 256, 0, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>()); note_launches(1); }
+    else { k_orbit_scatter<uint32_t><<<sgrid, 256, 0, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>()); note_launches(1); }
+    SED_TRY_CUDA(cudaGetLastError());
+    IndexView const I = b.index_view();
+    unsigned const rgrid = (unsigned)((n_slices * 32 + 255) / 256);
+    if (op.is_real) { k_record_table<true><<<rgrid, 256, 0, stream>>>(I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask); note_launches(1); }
+    else { k_record_table<false><<<rgrid, 256, 0, stream>>>(I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask); note_launches(1); }
+    SED_TRY_CUDA(cudaGetLastError());
+    int herr = 0;
+    SED_TRY_CUDA(cudaMemcpyAsync(&herr, err.ptr, 4, cudaMemcpyDeviceToHost, stream));
+    SED_TRY_CUDA(cudaStreamSynchronize(stream));
+    if (herr) return fail(LS_SYSTEM_ERROR, "orbit table: a word outside the weight class (internal error)");
+  } else if (n_slices) {
     bool const wide = b.plan.n_bits > 32;
     IndexView const I = b.index_view();
     auto launch = [&](auto w_tag, auto real_tag) {
+
       using W = decltype(w_tag);
       constexpr bool R = decltype(real_tag)::value;
       size_t const smem = record_smem_bytes();
@@ -633,11 +811,13 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
   sf.n_elements = n_elements;
   sf.n_codes = tb.n_codes;
   sf.ready = true;
+  sf.orbit_table = use_table;
   sf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (logging_enabled())
-    log_line("stream form: %llu elements, %llu slots (%s), %.1f MB, %.3f s",
+    log_line("stream form: %llu elements, %llu slots (%s), %.1f MB, %.3f s (%s)",
              (unsigned long long)n_elements, (unsigned long long)n_entries,
-             packed ? "packed" : "split", sf.bytes() / 1e6, sf.seconds);
+             packed ? "packed" : "split", sf.bytes() / 1e6, sf.seconds,
+             use_table ? "orbit table" : "canonicalisation");
   return LS_SUCCESS;
 }
 
@@ -1141,6 +1321,14 @@ int ls_operator_expectation(ls_operator const* op, int dtype, uint64_t size, uin
   } catch (std::exception const& e) {
     return fail(LS_SYSTEM_ERROR, e.what());
   }
+}
+
+void sed_set_record_mode(int mode) {
+  g_record_mode = mode == SED_RECORD_CANONICALISE ? SED_RECORD_CANONICALISE : SED_RECORD_AUTO;
+}
+
+int sed_operator_recorded_with_table(ls_operator const* op) {
+  return op && op->d->stream.ready && op->d->stream.orbit_table ? 1 : 0;
 }
 
 int sed_operator_prepare(ls_operator* op, int form) {

@@ -181,6 +181,7 @@ struct StreamForm {
   DeviceBuffer inv_sqrt_s;      // double[n classes]
   unsigned n_codes = 0;
   double seconds = 0;
+  bool orbit_table = false;     // recorded through the orbit table
   // FP32 companions for the mixed-precision Krylov phase (real operators)
   DeviceBuffer diag_f;   // float[D]
   DeviceBuffer table_f;  // float[n_codes]
@@ -217,6 +218,9 @@ int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void cons
 int operator_prepare_fp32(OperatorData& op, cudaStream_t stream);
 
 bool characters_real(BasisData const& b);
+uint64_t host_binom(unsigned n, unsigned k);
+// How the stream form is recorded (sed_set_record_mode).
+extern int g_record_mode;
 
 // sed_eigh's thick-restart solver (real operators, 0 < max_basis <= 32).
 int solve_thick(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* evals, void* evecs, uint64_t ldv,

@@ -38,6 +38,7 @@ SED_FORM_AUTO, SED_FORM_STREAM, SED_FORM_ON_THE_FLY = 0, 1, 2
 SED_PRECISION_FP64, SED_PRECISION_MIXED = 0, 1
 SED_START_RANDOM, SED_START_GIVEN = 0, 1
 SED_MLP_PATH_AUTO, SED_MLP_PATH_SIMT = 0, 1
+SED_RECORD_AUTO, SED_RECORD_CANONICALISE = 0, 1
 
 PROGRESS_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_uint64, C.POINTER(C.c_double),
                           C.POINTER(C.c_double), C.c_uint)
@@ -148,6 +149,8 @@ SIGNATURES = [
     ("sed_mlp_start_vector", _I, [_P, _P, _P]),
     ("sed_mlp_set_path", _I, [_P, _I]),
     ("sed_release_workspace", None, []),
+    ("sed_set_record_mode", None, [_I]),
+    ("sed_operator_recorded_with_table", _I, [_P]),
     ("sed_mlp_uses_tensor_cores", _I, [_P]),
     ("sed_kernel_launches", _U64, []),
     ("sed_version", C.c_char_p, []),

@@ -177,3 +177,51 @@ def test_block_matvec_bit_identical_to_columns(sed, oracle, block):
         torch.cuda.synchronize()
         assert torch.equal(y[:, c], yc)
     np.testing.assert_allclose(y[:, 0].cpu().numpy(), oop.matvec(x[:, 0].cpu().numpy()).real, atol=1e-11)
+
+
+TABLE_MODELS = {
+    "chain24": lattices.heisenberg_chain(24),
+    "chain16_k8": lattices.heisenberg_chain(16, momentum=8, parity=None),   # k = pi: characters +-1
+    "chain18_k9_odd": lattices.heisenberg_chain(18, momentum=9, parity=1),
+    "chain14_w5": lattices.heisenberg_chain(14, hamming_weight=5),          # no spin inversion
+    "square4_inv-": lattices.heisenberg_square(4, spin_inversion=-1),
+    "square4_j2": lattices.heisenberg_square(4, j2=0.3),
+    "ring10_nohw": lattices.Model("ring10", 10, None, 1, [(lattices.chain_translation(10), 0)],
+                                  [(lattices.HEISENBERG, lattices.chain_bonds(10))]),
+    "chain12_3site_weight_changing": MODELS["chain12_3site"],
+    "chain12_field": lattices.Model("chain12f", 12, 6, None, [(lattices.chain_translation(12), 0)],
+                                    [(lattices.HEISENBERG, lattices.chain_bonds(12)),
+                                     ([[0.3, 0.0], [0.0, -0.3]], [[i] for i in range(12)])]),
+}
+
+
+@pytest.mark.parametrize("name", list(TABLE_MODELS))
+def test_orbit_table_record_bit_identical(sed, oracle, name):
+    """The stream form recorded through the orbit table (a map from every word
+    of the weight class to its representative) equals the one recorded by
+    canonicalising every element: the same entries, so bit-identical
+    matvecs; and both match the oracle."""
+    import torch
+    from spined.model import build_model
+    m = TABLE_MODELS[name]
+    lib = L.load()
+    built, ob, oop = both(sed, oracle, m)
+    try:
+        lib.sed_set_record_mode(L.SED_RECORD_CANONICALISE)
+        canon = build_model(m)
+        canon.hamiltonian.prepare(L.SED_FORM_STREAM)
+    finally:
+        lib.sed_set_record_mode(L.SED_RECORD_AUTO)
+    built.hamiltonian.prepare(L.SED_FORM_STREAM)
+    assert lib.sed_operator_recorded_with_table(built.hamiltonian.ptr) == 1
+    assert lib.sed_operator_recorded_with_table(canon.hamiltonian.ptr) == 0
+    assert built.hamiltonian.stream_elements == canon.hamiltonian.stream_elements
+    D = len(ob.reps)
+    x = torch.randn(D, dtype=torch.float64, device="cuda")
+    y1, y2 = torch.zeros_like(x), torch.zeros_like(x)
+    sed.inplace_apply(built.hamiltonian, x, y1)
+    sed.inplace_apply(canon.hamiltonian, x, y2)
+    torch.cuda.synchronize()
+    assert torch.equal(y1, y2)
+    np.testing.assert_allclose(y1.cpu().numpy(), oop.matvec(x.cpu().numpy()).real, rtol=0,
+                               atol=1e-12 * max(1.0, float(y1.abs().max())))
