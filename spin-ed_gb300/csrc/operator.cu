@@ -396,6 +396,45 @@ __device__ __forceinline__ void stage_binom(uint64_t const* __restrict__ binom, 
   }
 }
 
+// On a row-structured group (a torus: one generator rotates every row, the
+// other shifts rows) the table stores, of each set {row rotations of z and of
+// ~z}, only the smallest word: it has the smallest rotation of z's (or ~z's)
+// top row on top, so only the rotations listed in the group's row tables are
+// built. Returns the smallest word and the phase of the element (rotation,
+// inversion) taking z to it.
+template <class W>
+__device__ __forceinline__ W rows_rot_min(W z, PlanView const& P, RowTab const& R, uint32_t* kphase) {
+  W const mask = (W)P.mask;
+  uint32_t const rm = (uint32_t)P.row_mask, top = P.n_rows - 1;
+  uint32_t const tv = (uint32_t)(z >> (top * P.row_bits)) & rm;
+  uint32_t M = R.min[tv];
+  if (P.inv) {
+    uint32_t const b = R.min[tv ^ rm];
+    M = b < M ? b : M;
+  }
+  W best = mask;
+  uint32_t br = 0, binv = 0;
+  for (uint32_t inv = 0; inv <= (P.inv ? 1u : 0u); ++inv) {
+    uint32_t const v = inv ? (tv ^ rm) : tv;
+    if (R.min[v] != M) continue;
+    uint32_t set = R.set[v];
+    while (set) {
+      uint32_t const r = (uint32_t)__builtin_ctz_sed(set);
+      set &= set - 1;
+      W const c = cand_image<W>(z, mask, P, top, r, inv);
+      if (c < best) {
+        best = c;
+        br = r;
+        binv = inv;
+      }
+    }
+  }
+  uint64_t ph = (uint64_t)P.rot_exp[br] * P.rot_phase;
+  if (binv) ph += P.inv_phase;
+  *kphase = (uint32_t)(ph % P.L);
+  return best;
+}
+
 // One thread per (representative, coset): every image h(p_c(r)) (and its
 // spin-inverted word) gets table entry j | sign(character of the element).
 // With spin inversion in the group only words whose top bit (n - 1) is clear
@@ -409,7 +448,9 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
                                                        uint32_t* __restrict__ table, uint64_t space,
                                                        int* __restrict__ error) {
   __shared__ uint64_t bin[64 * 33];
+  __shared__ uint16_t rows_s[2048];
   stage_binom(binom, bin);
+  RowTab const RT = stage_rows(P, rows_s);  // synchronises the block
   __syncthreads();
   uint64_t const t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t const j = t / P.n_cosets;
@@ -418,6 +459,45 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
   W const mask = (W)P.mask;
   W const y = coset_apply<W>((W)reps[j], P, c);
   uint32_t const pc = P.coset_phase[c];
+  if (P.rows == 1) {
+    // The images with source row k at the top form one class under row
+    // rotations and inversion; its smallest member has the smallest rotation
+    // of row k (or of its inverse) on top, so only the rotations in the row
+    // tables are built, and the class writes one entry.
+    uint32_t const rm = (uint32_t)P.row_mask;
+    for (uint32_t k = 0; k < P.n_rows; ++k) {
+      uint32_t const rv = (uint32_t)(y >> (k * P.row_bits)) & rm;
+      uint32_t M = RT.min[rv];
+      if (P.inv) {
+        uint32_t const b = RT.min[rv ^ rm];
+        M = b < M ? b : M;
+      }
+      W best = mask;
+      uint32_t br = 0, binv = 0;
+      for (uint32_t inv = 0; inv <= (P.inv ? 1u : 0u); ++inv) {
+        uint32_t const v = inv ? (rv ^ rm) : rv;
+        if (RT.min[v] != M) continue;
+        uint32_t set = RT.set[v];
+        while (set) {
+          uint32_t const r = (uint32_t)__builtin_ctz_sed(set);
+          set &= set - 1;
+          W const z = cand_image<W>(y, mask, P, k, r, inv);
+          if (z < best) {
+            best = z;
+            br = r;
+            binv = inv;
+          }
+        }
+      }
+      uint32_t const tt = k + 1 == P.n_rows ? 0u : k + 1;
+      uint64_t ph = (uint64_t)pc + (uint64_t)P.rot_exp[br] * P.rot_phase + (uint64_t)P.sh_exp[tt] * P.shift_phase;
+      if (binv) ph += P.inv_phase;
+      uint64_t const k0 = word_rank((uint64_t)best, hw, bin);
+      if (k0 < space) table[k0] = (uint32_t)j | ((ph % P.L) ? kTabSign : 0u);
+      else *error = 1;
+    }
+    return;
+  }
   for (uint32_t h = 0; h < P.n_h; ++h) {
     W const z = shift_apply<W>(y, P.h_mask + (uint64_t)h * P.n_terms, P.h_rot + (uint64_t)h * P.n_terms, P.n_terms);
     uint32_t const ph = add_phase(pc, P.h_phase[h], P.L);
@@ -436,8 +516,8 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
 // The stream form from the orbit table: one warp per SELL-32 slice, one row
 // per lane, elements in the canonical order of walk_row; same entries, codes,
 // diagonal and row classes as k_record.
-template <bool Real>
-__global__ void __launch_bounds__(256) k_record_table(IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
+template <class W, bool Real>
+__global__ void __launch_bounds__(256) k_record_table(__grid_constant__ const PlanView P, IndexView I, TermsView T, CodeView C, uint32_t const* __restrict__ weights,
                                                       uint64_t n_slices, uint64_t const* __restrict__ slice_ptr,
                                                       uint32_t col_bits, bool packed, uint32_t* __restrict__ entries,
                                                       uint16_t* __restrict__ codes, void* __restrict__ diag,
@@ -446,7 +526,9 @@ __global__ void __launch_bounds__(256) k_record_table(IndexView I, TermsView T, 
                                                       int* __restrict__ error, bool inv_half, bool inv_sign,
                                                       uint32_t n_bits, uint64_t word_mask) {
   __shared__ uint64_t bin[64 * 33];
+  __shared__ uint16_t rows_s[2048];
   stage_binom(binom, bin);
+  RowTab const RT = stage_rows(P, rows_s);
   __syncthreads();
   uint32_t const lane = threadIdx.x & 31;
   uint64_t const s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -463,12 +545,19 @@ __global__ void __launch_bounds__(256) k_record_table(IndexView I, TermsView T, 
       uint32_t v = kNull;
       if (hw < 0 || __popcll(st) == hw) {
         uint64_t w = st;
-        bool const flip = inv_half && ((st >> (n_bits - 1)) & 1u);
-        if (flip) w = ~st & word_mask;
+        bool flip = false;
+        if (P.rows == 1) {
+          uint32_t kp;
+          w = (uint64_t)rows_rot_min<W>((W)st, P, RT, &kp);
+          flip = kp != 0;
+        } else if (inv_half && ((st >> (n_bits - 1)) & 1u)) {
+          w = ~st & word_mask;
+          flip = inv_sign;
+        }
         uint64_t const k = word_rank(w, hw, bin);
         if (k < space) v = __ldg(table + k);
         else *error = 1;
-        if (flip && v != kNull && inv_sign) v ^= kTabSign;
+        if (flip && v != kNull) v ^= kTabSign;
       }
       uint32_t ent = kNull, code = 0;
       if (v != kNull) {
@@ -773,8 +862,18 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     SED_TRY_CUDA(cudaGetLastError());
     IndexView const I = b.index_view();
     unsigned const rgrid = (unsigned)((n_slices * 32 + 255) / 256);
-    if (op.is_real) { k_record_table<true><<<rgrid, 256, 0, stream>>>(I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask); note_launches(1); }
-    else { k_record_table<false><<<rgrid, 256, 0, stream>>>(I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask); note_launches(1); }
+    auto rec = [&](auto w_tag, auto real_tag) {
+      using W = decltype(w_tag);
+      constexpr bool R = decltype(real_tag)::value;
+      { k_record_table<W, R><<<rgrid, 256, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask); note_launches(1); }
+    };
+    if (wide) {
+      if (op.is_real) rec(uint64_t{}, std::true_type{});
+      else rec(uint64_t{}, std::false_type{});
+    } else {
+      if (op.is_real) rec(uint32_t{}, std::true_type{});
+      else rec(uint32_t{}, std::false_type{});
+    }
     SED_TRY_CUDA(cudaGetLastError());
     int herr = 0;
     SED_TRY_CUDA(cudaMemcpyAsync(&herr, err.ptr, 4, cudaMemcpyDeviceToHost, stream));
