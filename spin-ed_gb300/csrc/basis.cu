@@ -14,6 +14,7 @@
 // A prefix table over the top bits of the representatives then serves the
 // index lookups of the matvec.
 #include <algorithm>
+#include <vector>
 #include <cstring>
 
 #include "sed_internal.hpp"
@@ -24,13 +25,39 @@ namespace {
 constexpr unsigned kThreads = 256;
 constexpr unsigned kTileWords = kThreads * 8;  // bitmap words per tile
 
+constexpr unsigned kMaxSegs = 1024;  // top-row segments of the rank space (2^row_bits <= 1024)
+
+// Marks representatives: bitmap word t holds ranks 32 t .. 32 t + 31. With
+// segments (n_seg > 0), only the bitmap words listed in them are examined
+// (the others were zeroed): on a torus a representative's top row must be
+// the smallest rotation of itself and of its inverse, and the words with a
+// given top row form one contiguous rank range, so whole ranges are skipped.
 template <class W>
 __global__ void k_mark(__grid_constant__ const PlanView P, uint64_t const* __restrict__ binom, unsigned n, int hw,
-                       uint64_t space, uint64_t n_words, uint32_t* __restrict__ bitmap) {
+                       uint64_t space, uint64_t n_words, uint32_t* __restrict__ bitmap,
+                       uint64_t const* __restrict__ seg_begin, uint64_t const* __restrict__ seg_prefix, uint32_t n_seg) {
   __shared__ uint16_t srow[2048];
+  __shared__ uint64_t sb[kMaxSegs], sp[kMaxSegs + 1];
   RowTab const RT = stage_rows(P, srow);
-  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_words;
-       t += (uint64_t)gridDim.x * blockDim.x) {
+  for (uint32_t q = threadIdx.x; q < n_seg; q += blockDim.x) {
+    sb[q] = seg_begin[q];
+    sp[q] = seg_prefix[q];
+  }
+  if (threadIdx.x == 0 && n_seg) sp[n_seg] = seg_prefix[n_seg];
+  __syncthreads();
+  uint64_t const total = n_seg ? sp[n_seg] : n_words;
+  for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
+       u += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t t = u;
+    if (n_seg) {  // segment holding u: the last with prefix <= u
+      uint32_t lo = 0, hi = n_seg - 1;
+      while (lo < hi) {
+        uint32_t const mid = (lo + hi + 1) >> 1;
+        if (sp[mid] <= u) lo = mid;
+        else hi = mid - 1;
+      }
+      t = sb[lo] + (u - sp[lo]);
+    }
     uint64_t const r0 = t * 32;
     unsigned const count = (unsigned)min((uint64_t)32, space - r0);
     uint64_t x = unrank_word(r0, n, hw, binom);
@@ -329,16 +356,57 @@ int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
     }
     uint64_t const n_words = (space + 31) / 32;
     uint64_t const n_tiles = (n_words + kTileWords - 1) / kTileWords;
-    DeviceBuffer bitmap, tiles;
+    DeviceBuffer bitmap, tiles, segs;
     if (int st = bitmap.allocate(std::max<uint64_t>(1, n_words) * 4)) return st;
     if (int st = tiles.allocate((n_tiles + 1) * 8)) return st;
-    unsigned const grid = grid_for(n_words, b.device) * 4;
+    // Top-row segments (tori): the rank range of the words with top row T is
+    // [lo_T, lo_T + cnt_T) in increasing T; keep the T whose value is its own
+    // smallest rotation and no larger than its inverse's smallest rotation.
+    std::vector<uint64_t> seg_b, seg_p;
+    if (b.plan.rows == 1 && b.plan.row_bits <= 10 && b.n >= b.plan.row_bits) {
+      unsigned const B = b.plan.row_bits, low = b.n - B;
+      uint32_t const rm = (1u << B) - 1;
+      uint64_t lo = 0, kept = 0;
+      for (uint32_t T = 0; T <= rm; ++T) {
+        int const need = b.hw - __builtin_popcount(T);
+        uint64_t const cnt = b.hw < 0 ? ((uint64_t)1 << low)
+                                      : (need < 0 || (unsigned)need > low ? 0 : host_binom(low, (unsigned)need));
+        bool ok = b.plan.row_min[T] == T;
+        if (b.plan.inv) ok = ok && b.plan.row_min[T ^ rm] >= T;
+        if (ok && cnt) {
+          // a bitmap word shared with the neighbouring range is examined by
+          // both segments: same word, same result
+          uint64_t const wb = lo / 32, we = (lo + cnt + 31) / 32;
+          seg_b.push_back(wb);
+          seg_p.push_back(kept);
+          kept += we - wb;
+        }
+        lo += cnt;
+      }
+      seg_p.push_back(kept);
+      if (seg_b.size() > kMaxSegs || lo != space) {
+        seg_b.clear();
+        seg_p.clear();
+      }
+    }
+    uint32_t const n_seg = (uint32_t)seg_b.size();
+    if (n_seg) {
+      if (int st = segs.allocate((2 * (size_t)n_seg + 1) * 8)) return st;
+      SED_TRY_CUDA(cudaMemcpyAsync(segs.ptr, seg_b.data(), n_seg * 8, cudaMemcpyHostToDevice, stream));
+      SED_TRY_CUDA(cudaMemcpyAsync(segs.as<uint64_t>() + n_seg, seg_p.data(), (n_seg + 1) * 8, cudaMemcpyHostToDevice,
+                                   stream));
+      SED_TRY_CUDA(cudaMemsetAsync(bitmap.ptr, 0, std::max<uint64_t>(1, n_words) * 4, stream));
+    }
+    uint64_t const work = n_seg ? seg_p.back() : n_words;
+    unsigned const grid = grid_for(std::max<uint64_t>(1, work), b.device) * 4;
+    uint64_t const* sbeg = n_seg ? segs.as<uint64_t>() : nullptr;
+    uint64_t const* spre = n_seg ? segs.as<uint64_t>() + n_seg : nullptr;
     if (wide)
       { k_mark<uint64_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
-                                                       n_words, bitmap.as<uint32_t>()); note_launches(1); }
+                                                       n_words, bitmap.as<uint32_t>(), sbeg, spre, n_seg); note_launches(1); }
     else
       { k_mark<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
-                                                       n_words, bitmap.as<uint32_t>()); note_launches(1); }
+                                                       n_words, bitmap.as<uint32_t>(), sbeg, spre, n_seg); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
     if (n_tiles) {
       { k_tile_counts<<<(unsigned)n_tiles, kThreads, 0, stream>>>(bitmap.as<uint32_t>(), n_words,
