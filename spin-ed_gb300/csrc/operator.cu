@@ -396,6 +396,39 @@ __device__ __forceinline__ void stage_binom(uint64_t const* __restrict__ binom, 
   }
 }
 
+// Colex rank by 6-bit chunks: R[(c * (w + 1) + m) * 64 + v] is the sum of
+// C(6 c + q, m + i) over the set bits q of v (the i-th of them, from 1), for
+// m set bits below chunk c; the rank is the sum over the chunks.
+struct RankTab {
+  uint64_t const* R;  // shared memory, or null for the bit-by-bit loop
+  uint32_t n_chunks, wp1;
+};
+
+__device__ __forceinline__ uint64_t word_rank_tab(uint64_t x, int hw, RankTab const& T, uint64_t const* bin) {
+  if (hw < 0) return x;
+  if (!T.R) return word_rank(x, hw, bin);
+  uint64_t rk = 0;
+  uint32_t m = 0;
+  for (uint32_t c = 0; c < T.n_chunks; ++c) {
+    uint32_t const v = (uint32_t)(x >> (6 * c)) & 63u;
+    rk += T.R[(c * T.wp1 + m) * 64 + v];
+    m += __popc(v);
+  }
+  return rk;
+}
+
+// Stages the chunked rank table (rank_bytes > 0) or the binomial table into
+// the dynamic shared memory `dyn`; returns the rank view.
+__device__ __forceinline__ RankTab stage_rank(uint64_t const* __restrict__ binom, uint64_t const* __restrict__ rank_tab,
+                                              uint32_t rank_words, uint32_t n_chunks, uint32_t wp1, uint64_t* dyn) {
+  if (rank_words) {
+    for (uint32_t q = threadIdx.x; q < rank_words; q += blockDim.x) dyn[q] = rank_tab[q];
+    return RankTab{dyn, n_chunks, wp1};
+  }
+  stage_binom(binom, dyn);
+  return RankTab{nullptr, 0, 0};
+}
+
 // On a row-structured group (a torus: one generator rotates every row, the
 // other shifts rows) the table stores, of each set {row rotations of z and of
 // ~z}, only the smallest word: it has the smallest rotation of z's (or ~z's)
@@ -446,10 +479,12 @@ template <class W>
 __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const PlanView P, uint64_t const* __restrict__ reps,
                                                        uint64_t D, int hw, uint64_t const* __restrict__ binom,
                                                        uint32_t* __restrict__ table, uint64_t space,
-                                                       int* __restrict__ error) {
-  __shared__ uint64_t bin[64 * 33];
+                                                       int* __restrict__ error, uint64_t const* __restrict__ rank_tab,
+                                                       uint32_t rank_words, uint32_t n_chunks, uint32_t wp1) {
+  extern __shared__ uint64_t dyn_rank[];
   __shared__ uint16_t rows_s[2048];
-  stage_binom(binom, bin);
+  uint64_t const* const bin = dyn_rank;
+  RankTab const RK = stage_rank(binom, rank_tab, rank_words, n_chunks, wp1, dyn_rank);
   RowTab const RT = stage_rows(P, rows_s);  // synchronises the block
   __syncthreads();
   uint64_t const t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -492,7 +527,7 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
       uint32_t const tt = k + 1 == P.n_rows ? 0u : k + 1;
       uint64_t ph = (uint64_t)pc + (uint64_t)P.rot_exp[br] * P.rot_phase + (uint64_t)P.sh_exp[tt] * P.shift_phase;
       if (binv) ph += P.inv_phase;
-      uint64_t const k0 = word_rank((uint64_t)best, hw, bin);
+      uint64_t const k0 = word_rank_tab((uint64_t)best, hw, RK, bin);
       if (k0 < space) table[k0] = (uint32_t)j | ((ph % P.L) ? kTabSign : 0u);
       else *error = 1;
     }
@@ -507,7 +542,7 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
       w = (W)(~z & mask);
       pw = add_phase(ph, P.inv_phase, P.L);
     }
-    uint64_t const k0 = word_rank((uint64_t)w, hw, bin);
+    uint64_t const k0 = word_rank_tab((uint64_t)w, hw, RK, bin);
     if (k0 < space) table[k0] = (uint32_t)j | (pw ? kTabSign : 0u);
     else *error = 1;
   }
@@ -524,10 +559,13 @@ __global__ void __launch_bounds__(256) k_record_table(__grid_constant__ const Pl
                                                       uint8_t* __restrict__ row_class, uint32_t const* __restrict__ table,
                                                       int hw, uint64_t const* __restrict__ binom, uint64_t space,
                                                       int* __restrict__ error, bool inv_half, bool inv_sign,
-                                                      uint32_t n_bits, uint64_t word_mask) {
-  __shared__ uint64_t bin[64 * 33];
+                                                      uint32_t n_bits, uint64_t word_mask,
+                                                      uint64_t const* __restrict__ rank_tab, uint32_t rank_words,
+                                                      uint32_t n_chunks, uint32_t wp1) {
+  extern __shared__ uint64_t dyn_rank[];
   __shared__ uint16_t rows_s[2048];
-  stage_binom(binom, bin);
+  uint64_t const* const bin = dyn_rank;
+  RankTab const RK = stage_rank(binom, rank_tab, rank_words, n_chunks, wp1, dyn_rank);
   RowTab const RT = stage_rows(P, rows_s);
   __syncthreads();
   uint32_t const lane = threadIdx.x & 31;
@@ -554,7 +592,7 @@ __global__ void __launch_bounds__(256) k_record_table(__grid_constant__ const Pl
           w = ~st & word_mask;
           flip = inv_sign;
         }
-        uint64_t const k = word_rank(w, hw, bin);
+        uint64_t const k = word_rank_tab(w, hw, RK, bin);
         if (k < space) v = __ldg(table + k);
         else *error = 1;
         if (flip && v != kNull) v ^= kTabSign;
@@ -854,18 +892,54 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     if (int st = krylov_take(space * 4, table)) return st;
     SED_TRY_CUDA(cudaMemsetAsync(table.ptr, 0xFF, space * 4, stream));
     SED_TRY_CUDA(cudaMemsetAsync(err.ptr, 0, 16, stream));
+    // chunked rank table (6-bit chunks) when it fits in 96 KB of shared memory
+    uint32_t n_chunks = 0, wp1 = 0, rank_words = 0;
+    DeviceBuffer rank_buf;
+    if (b.hw >= 0) {
+      n_chunks = (b.n + 5) / 6;
+      wp1 = (uint32_t)b.hw + 1;
+      uint64_t const words = (uint64_t)n_chunks * wp1 * 64;
+      if (words * 8 <= 96 * 1024) {
+        std::vector<uint64_t> R(words, 0);
+        for (uint32_t c = 0; c < n_chunks; ++c)
+          for (uint32_t m = 0; m < wp1; ++m)
+            for (uint32_t v = 0; v < 64; ++v) {
+              uint64_t acc = 0;
+              uint32_t i = 0;
+              for (uint32_t q = 0; q < 6; ++q)
+                if ((v >> q) & 1u) {
+                  ++i;
+                  uint32_t const p = 6 * c + q;
+                  if (p < 64) acc += host_binom(p, m + i);
+                }
+              R[((size_t)c * wp1 + m) * 64 + v] = acc;
+            }
+        if (int st = rank_buf.allocate(words * 8)) return st;
+        SED_TRY_CUDA(cudaMemcpyAsync(rank_buf.ptr, R.data(), words * 8, cudaMemcpyHostToDevice, stream));
+        SED_TRY_CUDA(cudaStreamSynchronize(stream));
+        rank_words = (uint32_t)words;
+      }
+    }
+    size_t const dsmem = rank_words ? (size_t)rank_words * 8 : (size_t)64 * 33 * 8;
     bool const wide = b.plan.n_bits > 32;
     uint64_t const threads = D * b.plan.n_cosets;
     unsigned const sgrid = (unsigned)((threads + 255) / 256);
-    if (wide) { k_orbit_scatter<uint64_t><<<sgrid, 256, 0, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>()); note_launches(1); }
-    else { k_orbit_scatter<uint32_t><<<sgrid, 256, 0, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>()); note_launches(1); }
+    uint64_t const* rtab = rank_words ? rank_buf.as<uint64_t>() : nullptr;
+    if (wide) {
+      cudaFuncSetAttribute(k_orbit_scatter<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
+      { k_orbit_scatter<uint64_t><<<sgrid, 256, dsmem, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>(), rtab, rank_words, n_chunks, wp1); note_launches(1); }
+    } else {
+      cudaFuncSetAttribute(k_orbit_scatter<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
+      { k_orbit_scatter<uint32_t><<<sgrid, 256, dsmem, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>(), rtab, rank_words, n_chunks, wp1); note_launches(1); }
+    }
     SED_TRY_CUDA(cudaGetLastError());
     IndexView const I = b.index_view();
     unsigned const rgrid = (unsigned)((n_slices * 32 + 255) / 256);
     auto rec = [&](auto w_tag, auto real_tag) {
       using W = decltype(w_tag);
       constexpr bool R = decltype(real_tag)::value;
-      { k_record_table<W, R><<<rgrid, 256, 0, stream>>>(b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask); note_launches(1); }
+      cudaFuncSetAttribute(k_record_table<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
+      { k_record_table<W, R><<<rgrid, 256, dsmem, stream>>>(b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask, rtab, rank_words, n_chunks, wp1); note_launches(1); }
     };
     if (wide) {
       if (op.is_real) rec(uint64_t{}, std::true_type{});
