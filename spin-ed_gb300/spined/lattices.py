@@ -66,6 +66,21 @@ def square_symmetries(L: int) -> list[list[int]]:
     return [tx, ty, rx, ry, rot]
 
 
+def rect_translations(Lx: int, Ly: int) -> list[list[int]]:
+    """Tx, Ty on an Lx x Ly torus (site = y * Lx + x)."""
+    idx = lambda x, y: (y % Ly) * Lx + (x % Lx)
+    tx = [idx(x + 1, y) for y in range(Ly) for x in range(Lx)]
+    ty = [idx(x, y + 1) for y in range(Ly) for x in range(Lx)]
+    return [tx, ty]
+
+
+def rect_bonds(Lx: int, Ly: int) -> list[list[int]]:
+    """Nearest-neighbour bonds of an Lx x Ly torus."""
+    idx = lambda x, y: (y % Ly) * Lx + (x % Lx)
+    return [[idx(x, y), idx(x + 1, y)] for y in range(Ly) for x in range(Lx)] + \
+           [[idx(x, y), idx(x, y + 1)] for y in range(Ly) for x in range(Lx)]
+
+
 def square_bonds(L: int) -> list[list[int]]:
     """Nearest-neighbour bonds in the order of the reference's 6x6 example."""
     idx = lambda x, y: (y % L) * L + (x % L)

@@ -19,6 +19,14 @@ CASES = {
     "ring10_nohw_inv": lattices.Model("r10", 10, None, 1, [(lattices.chain_translation(10), 0)],
                                       [(lattices.HEISENBERG, lattices.chain_bonds(10))]),
     "chain34_k0": lattices.heisenberg_chain(34),  # 64-bit words, D ~ 1.7e6? (large)
+    # tori: the top-row pruning of the scan with momentum (pi, pi), without a
+    # Hamming weight, and on a 6x4 torus (rows of 6 sites, 4 rows)
+    "square4_kpi": lattices.Model("sq4kpi", 16, 8, 1, [(g, 2) for g in lattices.square_symmetries(4)[:2]],
+                                  [(lattices.HEISENBERG, lattices.square_bonds(4))]),
+    "square4_nohw": lattices.Model("sq4nohw", 16, None, 1, [(g, 0) for g in lattices.square_symmetries(4)],
+                                   [(lattices.HEISENBERG, lattices.square_bonds(4))]),
+    "torus6x4_w11": lattices.Model("t6x4", 24, 11, None, [(g, 0) for g in lattices.rect_translations(6, 4)],
+                                   [(lattices.HEISENBERG, lattices.rect_bonds(6, 4))]),
 }
 
 

@@ -189,6 +189,14 @@ TABLE_MODELS = {
     "ring10_nohw": lattices.Model("ring10", 10, None, 1, [(lattices.chain_translation(10), 0)],
                                   [(lattices.HEISENBERG, lattices.chain_bonds(10))]),
     "chain12_3site_weight_changing": MODELS["chain12_3site"],
+    "square4_kpi": lattices.Model("sq4kpi", 16, 8, 1, [(g, 2) for g in lattices.square_symmetries(4)[:2]],
+                                  [(lattices.HEISENBERG, lattices.square_bonds(4))]),
+    "square4_nohw": lattices.Model("sq4nohw", 16, None, 1, [(g, 0) for g in lattices.square_symmetries(4)],
+                                   [(lattices.HEISENBERG, lattices.square_bonds(4))]),
+    "torus6x4_w11_j2": lattices.Model("t6x4", 24, 11, None, [(g, 0) for g in lattices.rect_translations(6, 4)],
+                                      [(lattices.HEISENBERG, lattices.rect_bonds(6, 4)),
+                                       ([[0.4 * v for v in r] for r in lattices.HEISENBERG],
+                                        [[y * 6 + x, ((y + 1) % 4) * 6 + (x + 1) % 6] for y in range(4) for x in range(6)])]),
     "chain12_field": lattices.Model("chain12f", 12, 6, None, [(lattices.chain_translation(12), 0)],
                                     [(lattices.HEISENBERG, lattices.chain_bonds(12)),
                                      ([[0.3, 0.0], [0.0, -0.3]], [[i] for i in range(12)])]),
