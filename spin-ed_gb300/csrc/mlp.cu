@@ -286,25 +286,36 @@ __global__ void k_draw(double const* __restrict__ prefix, uint64_t D, double tot
 unsigned blocks_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
 // ------------------------------------------------ tensor-core inference ---
-// The whole network for 128 states per CTA on the 5th-generation tensor
-// cores, for n <= 64 inputs and hidden = 128, 256 or 512:
+// The whole network for tiles of 128 states on the 5th-generation tensor
+// cores, for n <= 64 inputs and hidden H = 128, 256 or 512:
 //   X [128 x 64] (spins built in shared memory from the state bits, zero
-//   padded), h1 = tanh(X W1^T + b1) -> TMEM (FP32) -> BF16 in shared memory,
+//   padded), h1 = tanh(X W1^T + b1) -> TMEM (FP32) -> BF16 back into TMEM,
 //   h2 = tanh(h1 W2^T + b2) -> TMEM, (a, s) = W3 h2 + b3 in registers.
-// Weights come from pre-swizzled images in global memory (L2-resident, a
-// few hundred KB) through bulk asynchronous copies, two stages of N x 64
-// columns; one thread issues the copies and the MMAs, four warps run the
-// epilogues (warp w owns TMEM lanes / rows 32 w .. 32 w + 31).
+// Persistent: one CTA per SM walks the tiles blockIdx.x, + gridDim.x, ...
+// TMEM (512 columns): two accumulator slots of 128 columns (0-127, 128-255)
+// and h1 as the A operand of layer 2 (columns 256 .. 256 + H/2, two BF16 per
+// column). Both layers produce their output 128 columns at a time, cycling
+// through the two slots, so the epilogue of one block overlaps the MMAs of
+// the next. Keeping h1 out of shared memory leaves room for a deep ring of
+// weight stages: the weights (pre-swizzled images in global memory, a few
+// hundred KB, L2-resident) are re-read for every tile, and the copies in
+// flight must cover the L2 latency.
 constexpr int kTcRows = 128;
 constexpr int kTcEpiWarps = 16;                    // 4 per TMEM lane quarter
 constexpr int kTcThreads = (kTcEpiWarps + 2) * 32;  // + one copy warp + one MMA warp
-constexpr int kTcStages = 5;                        // ring of weight stages, 128 rows x 128 B (16 KB) each
+constexpr int kTcTileBytes = 128 * 128;             // one weight K tile: 128 rows x 64 BF16, swizzled
+constexpr int kTcJobTiles = 4;                      // K tiles per layer-2 job (one ring stage)
+constexpr int kTcMaxStages = 8;                     // ring of weight stages of kTcJobTiles K tiles each
+constexpr int kTcMaxBlocks = 4;                     // H / 128
+constexpr uint32_t kTcCols = 512;                   // TMEM columns per CTA
+constexpr uint32_t kTcH1Col = 256;                  // first TMEM column of h1
 constexpr uint64_t kTcWaitNs = 1000000000ull;       // 1 s per wait: far beyond any MMA or copy
+constexpr size_t kTcSmemLimit = 232448 - 1024;      // opt-in shared memory per CTA, less the static part
 
 struct MlpTcArgs {
   uint64_t const* states;
   int64_t n;
-  int n_in, hidden;
+  int n_in, hidden, stages;
   uint8_t const* w1img;  // hidden rows x 128 B (K = 64, zero padded), swizzled
   uint8_t const* w2img;  // hidden/64 tiles of hidden rows x 128 B, swizzled
   float const* b1;
@@ -315,209 +326,318 @@ struct MlpTcArgs {
   int* error;
 };
 
-// dynamic shared memory: A tiles, the weight ring, b1, b2, W3 (FP32), partials
+// dynamic shared memory: the X tile, b1, b2, W3 (FP32), two buffers of
+// per-warp partial sums, then the weight ring with as many stages as fit
+size_t tc_fixed_bytes(int hidden) {
+  return (size_t)kTcRows * 128 + 4 * (size_t)hidden * 4 + 2 * (size_t)4 * kTcRows * 2 * 4 + 1024;
+}
+int tc_job_tiles(int hidden) { return std::min(kTcJobTiles, hidden / 64); }
+int tc_stages(int hidden) {
+  return (int)std::min<size_t>(kTcMaxStages, (kTcSmemLimit - tc_fixed_bytes(hidden)) /
+                                                  ((size_t)tc_job_tiles(hidden) * kTcTileBytes));
+}
 size_t tc_smem_bytes(int hidden) {
-  return (size_t)kTcRows * hidden * 2 + (size_t)kTcStages * 128 * 128 + 4 * (size_t)hidden * 4 +
-         (size_t)kTcEpiWarps * 32 * 2 * 4 + 1024;
+  return tc_fixed_bytes(hidden) + (size_t)tc_stages(hidden) * tc_job_tiles(hidden) * kTcTileBytes;
 }
 
 __device__ __forceinline__ void epi_sync() {  // the 512 epilogue threads only
   asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32) : "memory");
 }
 
+// X tile of `tile` (rows past n get state 0): row xr, input j -> BF16 +1 / -1,
+// zero for j >= n_in; four threads per row, two 16-byte chunks each. Called
+// by the 512 epilogue threads.
+__device__ __forceinline__ void tc_build_x(MlpTcArgs const& p, int64_t tile, uint8_t* X, int t) {
+  int const xr = t & 127, part = t >> 7;
+  int64_t const xrow = tile * kTcRows + xr;
+  uint64_t const s = xrow < p.n ? p.states[xrow] : 0;
+#pragma unroll
+  for (int cc = 0; cc < 2; ++cc) {
+    int const c = 2 * part + cc;
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int const j = 8 * c + 2 * q;
+      uint32_t const lo = j < p.n_in ? (((s >> j) & 1) ? 0x3F80u : 0xBF80u) : 0u;
+      uint32_t const hi = j + 1 < p.n_in ? (((s >> (j + 1)) & 1) ? 0x3F80u : 0xBF80u) : 0u;
+      w[q] = lo | (hi << 16);
+    }
+    *reinterpret_cast<uint4*>(X + xr * 128 + ((c ^ (xr & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
 // Warp-specialised: warp 16 streams the weights through the ring (waiting
-// only for a stage's previous MMAs to finish), warp 17 issues the MMAs as
-// soon as a stage lands (never waiting for MMA completion), warps 0-15 run
-// the epilogues. The weight stream is one sequence of jobs: jobs
-// 0 .. H/128-1 are the 128-row blocks of W1 (K = 64), then job
-// H/128 + kb * H/128 + q is (K tile kb, row block q) of W2; job j lives in
-// stage j % kTcStages.
+// only for a stage's previous MMAs to finish), warp 17 issues the MMAs,
+// warps 0-15 run the epilogues and build the X tiles. Per tile the weight
+// stream is H/128 jobs of W1 (row block q, K = 64) followed by the W2 jobs
+// (row block q, K tile kb) in q-major order; global job g lives in stage
+// g % stages. Accumulator uses are numbered u = 0, 1, ... over the layer-1
+// and layer-2 blocks of all tiles in order; use u takes slot u % 2.
+// Barriers: acc_full (MMAs of a use done; committed by the MMA warp),
+// acc_empty (the epilogue has read the slot), h1_ready (block q of h1 is in
+// TMEM), x_ready (the X tile is in shared memory); the last three get one
+// arrival per epilogue warp.
 __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full[kTcStages], empty[kTcStages], done, h1_ready;
+  __shared__ uint64_t full[kTcMaxStages], empty[kTcMaxStages];
+  __shared__ uint64_t acc_full[2], acc_empty[2], h1_ready[kTcMaxBlocks];
+  __shared__ uint64_t x_ready, drain;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   uint8_t* const smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  int const H = p.hidden, NM = 128, blocks = H / NM;
-  uint32_t const stage_bytes = (uint32_t)NM * 128;
-  uint8_t* const A = smem;  // H/64 tiles of 128 rows x 128 B
-  uint8_t* const B0 = smem + (size_t)kTcRows * H * 2;
-  float* const sb1 = reinterpret_cast<float*>(B0 + (size_t)kTcStages * stage_bytes);
+  int const H = p.hidden, NM = 128, blocks = H / NM, ktiles = H / 64, S = p.stages;
+  int const JT = min(kTcJobTiles, ktiles), kjobs = ktiles / JT;  // K tiles per layer-2 job, jobs per block
+  uint32_t const stage_bytes = (uint32_t)(JT * kTcTileBytes);
+  uint8_t* const X = smem;  // 128 rows x 128 B
+  uint8_t* const B0 = X + (size_t)kTcRows * 128;
+  float* const sb1 = reinterpret_cast<float*>(B0 + (size_t)S * stage_bytes);
   float* const sb2 = sb1 + H;
-  float* const sw3 = sb2 + H;  // [2][H]
-  float* const spart = sw3 + 2 * H;  // [4 column quarters][128 rows][2]
+  float* const sw3 = sb2 + H;        // [2][H]
+  float* const spart = sw3 + 2 * H;  // [2 buffers][4 column slices][128 rows][2]
   int const t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  int const jobs1 = blocks, jobs = blocks + (H / 64) * blocks;
-  auto job_src = [&](int j) -> uint8_t const* {
-    if (j < jobs1) return p.w1img + (size_t)j * stage_bytes;
-    int const u = j - jobs1, kb = u / blocks, q = u % blocks;
-    return p.w2img + ((size_t)kb * H + (size_t)q * NM) * 128;
-  };
-  auto stage = [&](int j) { return B0 + (size_t)(j % kTcStages) * stage_bytes; };
+  int64_t const n_tiles = (p.n + kTcRows - 1) / kTcRows;
+  int const my_tiles = blockIdx.x < n_tiles ? (int)((n_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  int const jobs_per_tile = blocks + kjobs * blocks;
 
   if (t == 0) {
-    for (int i = 0; i < kTcStages; ++i) {
+    for (int i = 0; i < S; ++i) {
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&empty[i], 1);
     }
-    tc::mbar_init(&done, 1);
-    tc::mbar_init(&h1_ready, 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&acc_full[i], 1);
+      tc::mbar_init(&acc_empty[i], kTcEpiWarps);
+    }
+    for (int q = 0; q < kTcMaxBlocks; ++q) tc::mbar_init(&h1_ready[q], kTcEpiWarps);
+    tc::mbar_init(&x_ready, kTcEpiWarps);
+    tc::mbar_init(&drain, 1);
     abort_flag = 0;
     tc::fence_mbar_init();
   }
   __syncwarp();
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)H);
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, kTcCols);
   for (int c = t; c < H; c += kTcThreads) {
     sb1[c] = __ldg(p.b1 + c);
     sb2[c] = __ldg(p.b2 + c);
     sw3[c] = __bfloat162float(p.W3[c]);
     sw3[H + c] = __bfloat162float(p.W3[H + c]);
   }
-  if (t < kTcEpiWarps * 32) {
-    // X tile: row xr, input j -> BF16 +1 / -1, zero for j >= n_in; four
-    // threads per row, two 16-byte chunks each
-    int const xr = t & 127, part = t >> 7;
-    int64_t const xrow = (int64_t)blockIdx.x * kTcRows + xr;
-    uint64_t const s = xrow < p.n ? p.states[xrow] : 0;
-#pragma unroll
-    for (int cc = 0; cc < 2; ++cc) {
-      int const c = 2 * part + cc;
-      uint32_t w[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        int const j = 8 * c + 2 * q;
-        uint32_t const lo = j < p.n_in ? (((s >> j) & 1) ? 0x3F80u : 0xBF80u) : 0u;
-        uint32_t const hi = j + 1 < p.n_in ? (((s >> (j + 1)) & 1) ? 0x3F80u : 0xBF80u) : 0u;
-        w[q] = lo | (hi << 16);
-      }
-      *reinterpret_cast<uint4*>(A + xr * 128 + ((c ^ (xr & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
-    }
-  }
-  tc::fence_proxy_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   uint32_t const tmem = tmem_slot;
 
   if (warp == kTcEpiWarps) {
-    // ---- copy warp: keep the ring full
+    // ---- copy warp: keep the ring full (stage st, its use count `use`)
     if (lane == 0) {
-      for (int j = 0; j < jobs; ++j) {
-        int const st = j % kTcStages, use = j / kTcStages;
-        if (use > 0 && !tc::mbar_wait(&empty[st], (uint32_t)(use - 1) & 1, kTcWaitNs)) {
+      int64_t const total = (int64_t)my_tiles * jobs_per_tile;
+      int64_t g = 0;
+      int st = 0, u = 0;
+      uint32_t use = 0;
+      for (; g < total; ++g) {
+        if (use > 0 && !tc::mbar_wait(&empty[st], (use - 1) & 1, kTcWaitNs)) {
           abort_flag = 1;
           break;
         }
-        tc::mbar_expect_tx(&full[st], stage_bytes);
-        tc::bulk_g2s(stage(j), job_src(j), stage_bytes, &full[st]);
+        uint8_t* const dst = B0 + (size_t)st * stage_bytes;
+        if (u < blocks) {  // W1 row block u (K = 64)
+          tc::mbar_expect_tx(&full[st], kTcTileBytes);
+          tc::bulk_g2s(dst, p.w1img + (size_t)u * kTcTileBytes, kTcTileBytes, &full[st]);
+        } else {  // W2 row block q, K tiles kg JT .. kg JT + JT - 1
+          int const v = u - blocks, q = v / kjobs, kg = v % kjobs;
+          tc::mbar_expect_tx(&full[st], stage_bytes);
+          for (int i = 0; i < JT; ++i)
+            tc::bulk_g2s(dst + (size_t)i * kTcTileBytes, p.w2img + ((size_t)(kg * JT + i) * H + (size_t)q * NM) * 128,
+                         kTcTileBytes, &full[st]);
+        }
+        if (++u == jobs_per_tile) u = 0;
+        if (++st == S) {
+          st = 0;
+          ++use;
+        }
       }
+      // never leave with copies in flight: wait for the last stages to land
+      for (int64_t h = g > S ? g - S : 0; h < g; ++h)
+        if (!tc::mbar_wait(&full[h % S], (uint32_t)(h / S) & 1, kTcWaitNs)) abort_flag = 1;
     }
     __syncwarp();
   } else if (warp == kTcEpiWarps + 1) {
-    // ---- MMA warp
-    if (lane == 0) {
-      uint32_t const idesc = tc::idesc_bf16_f32(128, (uint32_t)NM);
-      bool ok = true;
-      for (int j = 0; j < jobs && ok; ++j) {
-        if (j == jobs1) {
-          tc::mma_commit(&done);  // layer 1 complete -> epilogue 1
-          ok = tc::mbar_wait(&h1_ready, 0, kTcWaitNs);
-          if (!ok) break;
-          tc::fence_after_sync();
-        }
-        int const st = j % kTcStages;
-        ok = tc::mbar_wait(&full[st], (uint32_t)(j / kTcStages) & 1, kTcWaitNs);
-        if (!ok) break;
-        tc::fence_after_sync();
-        bool const l1 = j < jobs1;
-        int const u = l1 ? 0 : j - jobs1;
-        int const kb = l1 ? 0 : u / blocks, q = l1 ? j : u % blocks;
-        uint32_t const at = tc::smem_u32(A) + (uint32_t)(kb * kTcRows * 128), b0 = tc::smem_u32(stage(j));
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          tc::mma_bf16(tmem + (uint32_t)(q * NM), tc::desc_sw128(at + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc,
-                       (kb > 0 || k > 0) ? 1u : 0u);
-        tc::mma_commit(&empty[st]);
+    // ---- MMA warp: the whole warp runs the loop, so that stage addresses
+    // and descriptors are warp-uniform; one elected lane issues the MMAs
+    // and commits.
+    uint32_t const idesc = tc::idesc_bf16_f32(128, (uint32_t)NM);
+    bool ok = true;
+    int st = 0;          // ring stage of the next job
+    uint32_t sph = 0;    // parity of that stage's current use
+    int64_t u = 0;       // accumulator use
+    auto take = [&]() {  // wait for the next job's stage to land
+      bool const r = tc::mbar_wait(&full[st], sph, kTcWaitNs);
+      tc::fence_after_sync();
+      return __all_sync(0xffffffffu, r);
+    };
+    auto release = [&](bool leader) {  // the stage is free once the MMAs issued so far have read it
+      if (leader) tc::mma_commit(&empty[st]);
+      if (++st == S) {
+        st = 0;
+        sph ^= 1u;
       }
-      if (ok) tc::mma_commit(&done);  // layer 2 complete -> epilogue 2
-      else abort_flag = 1;
+    };
+    auto slot_free = [&](int64_t uu) {  // the epilogue has drained use uu - 2 of the slot
+      bool const r = uu < 2 || tc::mbar_wait(&acc_empty[uu & 1], (uint32_t)((uu >> 1) - 1) & 1, kTcWaitNs);
+      tc::fence_after_sync();
+      return __all_sync(0xffffffffu, r);
+    };
+    for (int it = 0; it < my_tiles && ok; ++it) {
+      uint32_t const par = (uint32_t)it & 1;
+      ok = __all_sync(0xffffffffu, tc::mbar_wait(&x_ready, par, kTcWaitNs) && !abort_flag);
+      tc::fence_after_sync();
+      // layer 1: block q of X W1^T
+      for (int q = 0; q < blocks && ok; ++q, ++u) {
+        ok = slot_free(u) && take();
+        if (!ok) break;
+        uint32_t const d = tmem + (uint32_t)((u & 1) * NM);
+        uint32_t const at = tc::smem_u32(X), b0 = tc::smem_u32(B0 + (size_t)st * stage_bytes);
+        bool const leader = tc::elect_one();
+        if (leader) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            tc::mma_bf16(d, tc::desc_sw128(at + 32 * k), tc::desc_sw128(b0 + 32 * k), idesc, k > 0 ? 1u : 0u);
+        }
+        release(leader);
+        if (leader) tc::mma_commit(&acc_full[u & 1]);
+        __syncwarp();
+      }
+      // layer 2: block q of h1 W2^T over all K tiles, h1 read from TMEM
+      for (int q = 0; q < blocks && ok; ++q, ++u) {
+        ok = slot_free(u);
+        uint32_t const d = tmem + (uint32_t)((u & 1) * NM);
+        for (int kg = 0; kg < kjobs && ok; ++kg) {
+          // K tiles kb = kg JT .. + JT - 1; h1 block b holds K tiles 2 b, 2 b + 1
+          for (int b = (kg * JT) >> 1; q == 0 && ok && b <= (kg * JT + JT - 1) >> 1; ++b) {
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(&h1_ready[b], par, kTcWaitNs) && !abort_flag);
+            tc::fence_after_sync();
+          }
+          if (ok) ok = take();
+          if (!ok) break;
+          uint32_t const b0 = tc::smem_u32(B0 + (size_t)st * stage_bytes);
+          bool const leader = tc::elect_one();
+          if (leader) {
+            for (int i = 0; i < JT; ++i) {
+              int const kb = kg * JT + i;
+#pragma unroll
+              for (int k = 0; k < 4; ++k)
+                tc::mma_bf16_ts(d, tmem + kTcH1Col + (uint32_t)(kb * 32 + k * 8),
+                                tc::desc_sw128(b0 + (uint32_t)(i * kTcTileBytes) + 32 * k), idesc,
+                                (kb > 0 || k > 0) ? 1u : 0u);
+            }
+          }
+          release(leader);
+          __syncwarp();
+        }
+        if (ok && tc::elect_one()) tc::mma_commit(&acc_full[u & 1]);
+        __syncwarp();
+      }
+    }
+    // every MMA issued has completed before TMEM is released
+    if (tc::elect_one()) {
+      if (!ok) abort_flag = 1;
+      tc::mma_commit(&drain);
+      if (!tc::mbar_wait(&drain, 0, kTcWaitNs)) abort_flag = 1;
     }
     __syncwarp();
   } else {
     // ---- epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
-    // rows) and the column quarter w / 4
+    // rows) and columns 32 (w / 4) .. + 31 of each 128-column block
     int const quarter = warp & 3, cq = warp >> 2;
     int const r = quarter * 32 + lane;
-    int const cols = H / 4, c_begin = cq * cols;
     uint32_t const lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-    bool ok = tc::mbar_wait(&done, 0, kTcWaitNs);
-    tc::fence_after_sync();
-    __syncwarp();
-    // epilogue 1: h1 = tanh(acc + b1) -> BF16 -> A tiles
-    if (ok) {
-      for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
+    bool ok = true;
+    int64_t u = 0;
+    if (my_tiles > 0) {
+      tc_build_x(p, blockIdx.x, X, t);
+      tc::fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&x_ready);
+    }
+    float const b3a = __ldg(p.b3), b3s = __ldg(p.b3 + 1);
+    // wait for accumulator use uu and load this warp's 32 columns of it;
+    // the slot is handed back as soon as the load has completed
+    auto load_acc = [&](int64_t uu, float (&v)[32]) {
+      if (ok) ok = tc::mbar_wait(&acc_full[uu & 1], (uint32_t)(uu >> 1) & 1, kTcWaitNs) && !abort_flag;
+      tc::fence_after_sync();
+      __syncwarp();
+      if (!ok) return false;
+      tc::tmem_ld32(lane_addr + (uint32_t)((uu & 1) * NM + cq * 32), v);
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_empty[uu & 1]);
+      return true;
+    };
+    // After a failed wait a warp skips the remaining work but still passes
+    // every epi_sync, so that the named barrier never waits for it.
+    for (int it = 0; it < my_tiles; ++it) {
+      int64_t const tile = (int64_t)blockIdx.x + (int64_t)it * gridDim.x;
+      uint32_t const par = (uint32_t)it & 1;
+      // epilogue 1: h1 = tanh(acc + b1) -> BF16 pairs -> TMEM, block by block
+      for (int q = 0; q < blocks; ++q, ++u) {
         float v[32];
-        tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
+        if (!load_acc(u, v)) break;
+        int const c0 = q * NM + cq * 32;
         uint32_t pk[16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q)
-          pk[q] = tc::pack_bf16x2(tc::tanh_fast(v[2 * q] + sb1[c0 + 2 * q]),
-                                  tc::tanh_fast(v[2 * q + 1] + sb1[c0 + 2 * q + 1]));
-        uint8_t* const tile = A + (size_t)(c0 >> 6) * (kTcRows * 128) + r * 128;
-#pragma unroll
-        for (int q4 = 0; q4 < 4; ++q4) {
-          int const chunk = (((c0 & 63) >> 3) + q4) ^ (r & 7);
-          *reinterpret_cast<uint4*>(tile + (chunk << 4)) =
-              make_uint4(pk[4 * q4], pk[4 * q4 + 1], pk[4 * q4 + 2], pk[4 * q4 + 3]);
-        }
+        for (int i = 0; i < 16; ++i)
+          pk[i] = tc::pack_bf16x2(tc::tanh_fast(v[2 * i] + sb1[c0 + 2 * i]),
+                                  tc::tanh_fast(v[2 * i + 1] + sb1[c0 + 2 * i + 1]));
+        tc::tmem_st16(lane_addr + kTcH1Col + (uint32_t)(c0 >> 1), pk);
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&h1_ready[q]);
       }
-    }
-    tc::fence_proxy_async_smem();
-    tc::fence_before_sync();
-    epi_sync();
-    if (t == 0) {
-      if (!ok) abort_flag = 1;
-      tc::mbar_arrive(&h1_ready);
-    }
-    if (ok) ok = tc::mbar_wait(&done, 1, kTcWaitNs);
-    tc::fence_after_sync();
-    __syncwarp();
-    // epilogue 2: h2 = tanh(acc + b2); partial (a, s) over this column quarter
-    float a = 0.0f, sg = 0.0f;
-    if (ok) {
-      for (int c0 = c_begin; c0 < c_begin + cols; c0 += 32) {
+      // the next tile's X (layer 1 of this tile has finished reading X)
+      if (ok && it + 1 < my_tiles) {
+        tc_build_x(p, tile + gridDim.x, X, t);
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&x_ready);
+      }
+      // epilogue 2: h2 = tanh(acc + b2); partial (a, s) over this warp's columns
+      float a = 0.0f, sg = 0.0f;
+      for (int q = 0; q < blocks; ++q, ++u) {
         float v[32];
-        tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
+        if (!load_acc(u, v)) break;
+        int const c0 = q * NM + cq * 32;
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
-          float const hq = tc::tanh_fast(v[q] + sb2[c0 + q]);
-          a = fmaf(sw3[c0 + q], hq, a);
-          sg = fmaf(sw3[H + c0 + q], hq, sg);
+        for (int i = 0; i < 32; ++i) {
+          float const hq = tc::tanh_fast(v[i] + sb2[c0 + i]);
+          a = fmaf(sw3[c0 + i], hq, a);
+          sg = fmaf(sw3[H + c0 + i], hq, sg);
         }
       }
-    }
-    spart[(cq * kTcRows + r) * 2] = a;
-    spart[(cq * kTcRows + r) * 2 + 1] = sg;
-    tc::fence_before_sync();
-    epi_sync();
-    if (t < kTcRows) {
-      int64_t const row = (int64_t)blockIdx.x * kTcRows + t;
-      float sa = __ldg(p.b3), ss = __ldg(p.b3 + 1);
+      // two buffers of partials: a buffer is rewritten two tiles later, after
+      // every reader of it has passed the next tile's epi_sync
+      float* const sp = spart + (size_t)par * (4 * kTcRows * 2);
+      sp[(cq * kTcRows + r) * 2] = a;
+      sp[(cq * kTcRows + r) * 2 + 1] = sg;
+      epi_sync();
+      if (t < kTcRows) {
+        int64_t const row = tile * kTcRows + t;
+        float sa = b3a, ss = b3s;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        sa += spart[(q * kTcRows + t) * 2];
-        ss += spart[(q * kTcRows + t) * 2 + 1];
+        for (int i = 0; i < 4; ++i) {
+          sa += sp[(i * kTcRows + t) * 2];
+          ss += sp[(i * kTcRows + t) * 2 + 1];
+        }
+        if (ok && row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
       }
-      if (ok && row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
     }
-    if (!ok && lane == 0) atomicExch(p.error, 1);
+    if (!ok) abort_flag = 1;
   }
   tc::fence_before_sync();
   __syncthreads();
   if (abort_flag && t == 0) atomicExch(p.error, 1);
   if (warp == 0) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tmem, (uint32_t)H);
+    tc::tmem_dealloc(tmem, kTcCols);
   }
 }
 
@@ -573,6 +693,7 @@ struct MlpData {
   DeviceBuffer wimg, tc_error;
   bool img_valid = false;
   int path = 0;  // SED_MLP_PATH_*
+  int n_sm = 0;  // multiprocessors of the device (grid of the persistent kernel)
   ~MlpData() {
     if (stream) cudaStreamDestroy(stream);
   }
@@ -690,6 +811,7 @@ int forward_tc(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
   a.n = (int64_t)n;
   a.n_in = (int)d.n_in;
   a.hidden = H;
+  a.stages = tc_stages(H);
   a.w1img = d.wimg.as<uint8_t>();
   a.w2img = d.wimg.as<uint8_t>() + img1;
   a.b1 = d.p.as<float>() + d.ob1;
@@ -698,7 +820,9 @@ int forward_tc(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
   a.b3 = d.p.as<float>() + d.ob3;
   a.out = out;
   a.error = d.tc_error.as<int>();
-  unsigned const grid = (unsigned)((n + kTcRows - 1) / kTcRows);
+  if (d.n_sm == 0) SED_TRY_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, d.device));
+  uint64_t const tiles = (n + kTcRows - 1) / kTcRows;
+  unsigned const grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)d.n_sm);  // persistent: one CTA per SM
   { k_mlp_forward_tc<<<grid, kTcThreads, smem, s>>>(a); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   int err = 0;
