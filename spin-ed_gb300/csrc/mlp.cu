@@ -344,13 +344,17 @@ __device__ __forceinline__ void epi_sync() {  // the 512 epilogue threads only
   asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32) : "memory");
 }
 
-// X tile of `tile` (rows past n get state 0): row xr, input j -> BF16 +1 / -1,
-// zero for j >= n_in; four threads per row, two 16-byte chunks each. Called
-// by the 512 epilogue threads.
-__device__ __forceinline__ void tc_build_x(MlpTcArgs const& p, int64_t tile, uint8_t* X, int t) {
+// State of row t % 128 of `tile` (0 past n), read by epilogue thread t.
+__device__ __forceinline__ uint64_t tc_state(MlpTcArgs const& p, int64_t tile, int t) {
+  int64_t const xrow = tile * kTcRows + (t & 127);
+  return xrow < p.n ? p.states[xrow] : 0;
+}
+
+// X tile row t % 128 from its state s: input j -> BF16 +1 / -1, zero for
+// j >= n_in; four threads per row, two 16-byte chunks each. Called by the
+// 512 epilogue threads.
+__device__ __forceinline__ void tc_build_x(MlpTcArgs const& p, uint64_t s, uint8_t* X, int t) {
   int const xr = t & 127, part = t >> 7;
-  int64_t const xrow = tile * kTcRows + xr;
-  uint64_t const s = xrow < p.n ? p.states[xrow] : 0;
 #pragma unroll
   for (int cc = 0; cc < 2; ++cc) {
     int const c = 2 * part + cc;
@@ -554,7 +558,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
     bool ok = true;
     int64_t u = 0;
     if (my_tiles > 0) {
-      tc_build_x(p, blockIdx.x, X, t);
+      tc_build_x(p, tc_state(p, blockIdx.x, t), X, t);
       tc::fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&x_ready);
@@ -573,52 +577,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
       if (lane == 0) tc::mbar_arrive(&acc_empty[uu & 1]);
       return true;
     };
-    // After a failed wait a warp skips the remaining work but still passes
-    // every epi_sync, so that the named barrier never waits for it.
-    for (int it = 0; it < my_tiles; ++it) {
-      int64_t const tile = (int64_t)blockIdx.x + (int64_t)it * gridDim.x;
-      uint32_t const par = (uint32_t)it & 1;
-      // epilogue 1: h1 = tanh(acc + b1) -> BF16 pairs -> TMEM, block by block
-      for (int q = 0; q < blocks; ++q, ++u) {
-        float v[32];
-        if (!load_acc(u, v)) break;
-        int const c0 = q * NM + cq * 32;
-        uint32_t pk[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
-          pk[i] = tc::pack_bf16x2(tc::tanh_fast(v[2 * i] + sb1[c0 + 2 * i]),
-                                  tc::tanh_fast(v[2 * i + 1] + sb1[c0 + 2 * i + 1]));
-        tc::tmem_st16(lane_addr + kTcH1Col + (uint32_t)(c0 >> 1), pk);
-        tc::fence_before_sync();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&h1_ready[q]);
-      }
-      // the next tile's X (layer 1 of this tile has finished reading X)
-      if (ok && it + 1 < my_tiles) {
-        tc_build_x(p, tile + gridDim.x, X, t);
-        tc::fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&x_ready);
-      }
-      // epilogue 2: h2 = tanh(acc + b2); partial (a, s) over this warp's columns
-      float a = 0.0f, sg = 0.0f;
-      for (int q = 0; q < blocks; ++q, ++u) {
-        float v[32];
-        if (!load_acc(u, v)) break;
-        int const c0 = q * NM + cq * 32;
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          float const hq = tc::tanh_fast(v[i] + sb2[c0 + i]);
-          a = fmaf(sw3[c0 + i], hq, a);
-          sg = fmaf(sw3[H + c0 + i], hq, sg);
-        }
-      }
-      // two buffers of partials: a buffer is rewritten two tiles later, after
-      // every reader of it has passed the next tile's epi_sync
-      float* const sp = spart + (size_t)par * (4 * kTcRows * 2);
-      sp[(cq * kTcRows + r) * 2] = a;
-      sp[(cq * kTcRows + r) * 2 + 1] = sg;
-      epi_sync();
+    // (a, s) of a finished tile: the four column slices' partials plus b3;
+    // run by threads 0-127 one tile later, off the epilogue's critical path
+    auto write_out = [&](int64_t tile, float const* sp) {
       if (t < kTcRows) {
         int64_t const row = tile * kTcRows + t;
         float sa = b3a, ss = b3s;
@@ -629,7 +590,67 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
         }
         if (ok && row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
       }
+    };
+    // After a failed wait a warp skips the remaining work but still passes
+    // every epi_sync, so that the named barrier never waits for it.
+    for (int it = 0; it < my_tiles; ++it) {
+      int64_t const tile = (int64_t)blockIdx.x + (int64_t)it * gridDim.x;
+      uint32_t const par = (uint32_t)it & 1;
+      // the next tile's states, loaded early: X is built after epilogue 1
+      uint64_t const s_next = it + 1 < my_tiles ? tc_state(p, tile + gridDim.x, t) : 0;
+      // epilogue 1: h1 = tanh(acc + b1) -> BF16 pairs -> TMEM, block by block
+      for (int q = 0; q < blocks; ++q, ++u) {
+        float v[32];
+        if (!load_acc(u, v)) break;
+        int const c0 = q * NM + cq * 32;
+        uint32_t pk[16];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {  // 16-byte broadcast loads of the biases
+          float4 const b = *reinterpret_cast<float4 const*>(sb1 + c0 + 4 * i);
+          pk[2 * i] = tc::pack_bf16x2(tc::tanh_fast(v[4 * i] + b.x), tc::tanh_fast(v[4 * i + 1] + b.y));
+          pk[2 * i + 1] = tc::pack_bf16x2(tc::tanh_fast(v[4 * i + 2] + b.z), tc::tanh_fast(v[4 * i + 3] + b.w));
+        }
+        tc::tmem_st16(lane_addr + kTcH1Col + (uint32_t)(c0 >> 1), pk);
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&h1_ready[q]);
+      }
+      // the next tile's X (layer 1 of this tile has finished reading X)
+      if (ok && it + 1 < my_tiles) {
+        tc_build_x(p, s_next, X, t);
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&x_ready);
+      }
+      // the previous tile's output (its partials are complete since its epi_sync)
+      if (it > 0) write_out(tile - gridDim.x, spart + (size_t)(par ^ 1u) * (4 * kTcRows * 2));
+      // epilogue 2: h2 = tanh(acc + b2); partial (a, s) over this warp's columns
+      float a = 0.0f, sg = 0.0f;
+      for (int q = 0; q < blocks; ++q, ++u) {
+        float v[32];
+        if (!load_acc(u, v)) break;
+        int const c0 = q * NM + cq * 32;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {  // 16-byte broadcast loads of b2 and W3
+          float4 const b = *reinterpret_cast<float4 const*>(sb2 + c0 + 4 * i);
+          float4 const wa = *reinterpret_cast<float4 const*>(sw3 + c0 + 4 * i);
+          float4 const ws = *reinterpret_cast<float4 const*>(sw3 + H + c0 + 4 * i);
+          float const h0 = tc::tanh_fast(v[4 * i] + b.x), h1 = tc::tanh_fast(v[4 * i + 1] + b.y);
+          float const h2 = tc::tanh_fast(v[4 * i + 2] + b.z), h3 = tc::tanh_fast(v[4 * i + 3] + b.w);
+          a = fmaf(wa.x, h0, fmaf(wa.y, h1, fmaf(wa.z, h2, fmaf(wa.w, h3, a))));
+          sg = fmaf(ws.x, h0, fmaf(ws.y, h1, fmaf(ws.z, h2, fmaf(ws.w, h3, sg))));
+        }
+      }
+      // two buffers of partials: a buffer is rewritten two tiles later, after
+      // its reader (write_out in the next tile) has passed the next epi_sync
+      float* const sp = spart + (size_t)par * (4 * kTcRows * 2);
+      sp[(cq * kTcRows + r) * 2] = a;
+      sp[(cq * kTcRows + r) * 2 + 1] = sg;
+      epi_sync();
     }
+    if (my_tiles > 0)
+      write_out((int64_t)blockIdx.x + (int64_t)(my_tiles - 1) * gridDim.x,
+                spart + (size_t)((my_tiles - 1) & 1) * (4 * kTcRows * 2));
     if (!ok) abort_flag = 1;
   }
   tc::fence_before_sync();
