@@ -51,34 +51,64 @@ struct Arith<float> {
   using T = float;
 };
 
-// partial[(g * gridDim.x + b) * 8 + c] = sum over this block's rows of
-// V[:, 8 g + c] . w  (columns >= ncols give 0); blockIdx.y = g.
-template <class S>
+// partial[(g * gridDim.x + b) * kDotCols + c] = sum over this block's rows
+// of V[:, NC g + c] . w for c < NC (columns >= ncols give 0); blockIdx.y = g.
+// NC is a template parameter: on GB300 a predicated-off FP64 FMA still takes
+// its issue slot on the slow FP64 pipe, so the column count of a launch is
+// matched exactly instead of padding to a fixed width.
+template <class S, int NC>
 __global__ void __launch_bounds__(256) k_tdots(S const* __restrict__ V, uint64_t ld, uint32_t ncols,
                                                S const* __restrict__ w, uint64_t D, double* __restrict__ partial) {
   using T = typename Arith<S>::T;
-  __shared__ double red[8][kDotCols];
-  uint32_t const c0 = blockIdx.y * kDotCols;
-  T acc[kDotCols] = {};
-  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x) {
-    T const wr = (T)w[r];
+  __shared__ double red[8][NC];
+  uint32_t const c0 = blockIdx.y * NC;
+  uint32_t const nc = ncols - c0 < (uint32_t)NC ? ncols - c0 : (uint32_t)NC;
+  S const* const Vc = V + (uint64_t)c0 * ld;
+  T acc[NC] = {};
+  if (nc == (uint32_t)NC) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x) {
+      T const wr = (T)w[r];
 #pragma unroll
-    for (int c = 0; c < kDotCols; ++c)
-      if (c0 + c < ncols) acc[c] = fma((T)V[(uint64_t)(c0 + c) * ld + r], wr, acc[c]);
+      for (int c = 0; c < NC; ++c) acc[c] = fma((T)Vc[(uint64_t)c * ld + r], wr, acc[c]);
+    }
+  } else {  // short last group (at most NC - 1 predicated-off columns)
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x) {
+      T const wr = (T)w[r];
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c < (int)nc) acc[c] = fma((T)Vc[(uint64_t)c * ld + r], wr, acc[c]);
+    }
   }
   int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int c = 0; c < kDotCols; ++c) {
+  for (int c = 0; c < NC; ++c) {
     double x = (double)acc[c];
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     if (lane == 0) red[warp][c] = x;
   }
   __syncthreads();
-  if (threadIdx.x < kDotCols) {
+  if (threadIdx.x < NC) {
     double s = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q][threadIdx.x];
     partial[((uint64_t)blockIdx.y * gridDim.x + blockIdx.x) * kDotCols + threadIdx.x] = s;
   }
+}
+
+// Launch of k_tdots over ncols columns in g = ceil(ncols / 8) groups of
+// NC = ceil(ncols / g) columns; returns NC.
+template <class S>
+int launch_tdots(S const* V, uint64_t ld, uint32_t ncols, S const* w, uint64_t D, double* partial, unsigned vb,
+                 cudaStream_t stream) {
+  uint32_t const g = (ncols + kDotCols - 1) / kDotCols;
+  int const nc = (int)((ncols + g - 1) / g);
+  dim3 const grid(vb, g);
+  switch (nc) {
+#define SED_TDOTS(N) \
+  case N: { k_tdots<S, N><<<grid, 256, 0, stream>>>(V, ld, ncols, w, D, partial); note_launches(1); } break;
+    SED_TDOTS(1) SED_TDOTS(2) SED_TDOTS(3) SED_TDOTS(4) SED_TDOTS(5) SED_TDOTS(6) SED_TDOTS(7) SED_TDOTS(8)
+#undef SED_TDOTS
+  }
+  return nc;
 }
 
 // w -= sum_{c < ncols} V[:, c] coef[c]  (FP64 arithmetic)
@@ -102,25 +132,43 @@ __global__ void k_tscale(S const* __restrict__ w, uint64_t D, double f, S* __res
     out[r] = (S)(ldv(w, r) * f);
 }
 
-// In place, row by row: V[:, c] <- sum_{i < m} V[:, i] Y[i * kk + c] for c < kk.
-template <class S>
+// In place, row by row: V[:, c] <- sum_{i < m} V[:, i] Y[i * kk + c] for
+// c < kk <= 4 KB. The kk sums of a row are independent chains, one FMA of
+// each per V value; KB is a template parameter so that at most three
+// predicated-off FMAs per V value take FP64 issue slots.
+template <class S, int KB>
 __global__ void k_trotate(S* __restrict__ V, uint64_t ld, uint32_t m, double const* __restrict__ Y, uint32_t kk,
                           uint64_t D) {
-  __shared__ double y[kMaxThick * kMaxThick];
-  for (uint32_t e = threadIdx.x; e < m * kk; e += blockDim.x) y[e] = Y[e];
+  constexpr int KC = 4 * KB;
+  __shared__ double y[kMaxThick * KC];
+  for (uint32_t e = threadIdx.x; e < m * KC; e += blockDim.x) {
+    uint32_t const i = e / KC, c = e % KC;
+    y[e] = c < kk ? Y[i * kk + c] : 0.0;
+  }
   __syncthreads();
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x) {
-    double v[kMaxThick];
+    double acc[KC];
 #pragma unroll
-    for (int i = 0; i < kMaxThick; ++i)
-      if (i < (int)m) v[i] = ldv(V, (uint64_t)i * ld + r);
-    for (uint32_t c = 0; c < kk; ++c) {
-      double s = 0.0;
+    for (int c = 0; c < KC; ++c) acc[c] = 0.0;
+    for (uint32_t i = 0; i < m; ++i) {
+      double const vi = ldv(V, (uint64_t)i * ld + r);
 #pragma unroll
-      for (int i = 0; i < kMaxThick; ++i)
-        if (i < (int)m) s = fma(v[i], y[i * kk + c], s);
-      V[(uint64_t)c * ld + r] = (S)s;
+      for (int c = 0; c < KC; ++c) acc[c] = fma(vi, y[i * KC + c], acc[c]);
     }
+#pragma unroll
+    for (int c = 0; c < KC; ++c)
+      if (c < (int)kk) V[(uint64_t)c * ld + r] = (S)acc[c];
+  }
+}
+
+template <class S>
+void launch_trotate(S* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk, uint64_t D, unsigned vb,
+                    cudaStream_t stream) {
+  switch ((kk + 3) / 4) {
+#define SED_TROT(N) \
+  case N: { k_trotate<S, N><<<vb, 256, 0, stream>>>(V, ld, m, Y, kk, D); note_launches(1); } break;
+    SED_TROT(1) SED_TROT(2) SED_TROT(3) SED_TROT(4) SED_TROT(5) SED_TROT(6) SED_TROT(7) SED_TROT(8)
+#undef SED_TROT
   }
 }
 
@@ -283,23 +331,24 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
   S* V = Vb.as<S>();
   S* w = wb.as<S>();
   std::vector<double> hp((size_t)groups * vb * kDotCols);
-  auto dots = [&](uint32_t ncols, S const* x, std::vector<double>& res) -> int {
+  // res[c] = V[:, first + c] . x for c < ncols
+  auto dots_at = [&](uint32_t first, uint32_t ncols, S const* x, std::vector<double>& res) -> int {
     uint32_t const g = (ncols + kDotCols - 1) / kDotCols;
-    { k_tdots<S><<<dim3(vb, g), 256, 0, stream>>>(V, D, ncols, x, D, part.as<double>()); note_launches(1); }
+    int const nc = launch_tdots<S>(V + (uint64_t)first * D, D, ncols, x, D, part.as<double>(), vb, stream);
     SED_TRY_CUDA(cudaGetLastError());
     SED_TRY_CUDA(cudaMemcpyAsync(hp.data(), part.ptr, (size_t)g * vb * kDotCols * 8, cudaMemcpyDeviceToHost, stream));
     SED_TRY_CUDA(cudaStreamSynchronize(stream));
     res.assign(ncols, 0.0);
     for (uint32_t gg = 0; gg < g; ++gg)
       for (unsigned b = 0; b < vb; ++b)
-        for (int c = 0; c < kDotCols; ++c)
-          if (gg * kDotCols + c < ncols) res[gg * kDotCols + c] += hp[((size_t)gg * vb + b) * kDotCols + c];
+        for (int c = 0; c < nc; ++c)
+          if (gg * nc + c < ncols) res[gg * nc + c] += hp[((size_t)gg * vb + b) * kDotCols + c];
     return LS_SUCCESS;
   };
+  auto dots = [&](uint32_t ncols, S const* x, std::vector<double>& res) -> int { return dots_at(0, ncols, x, res); };
   auto norm = [&](S const* x, double& nrm) -> int {
     // ||x||: dots of column 0 of a one-column "V" = x itself
-    uint32_t const g = 1;
-    { k_tdots<S><<<dim3(vb, g), 256, 0, stream>>>(x, D, 1, x, D, part.as<double>()); note_launches(1); }
+    launch_tdots<S>(x, D, 1, x, D, part.as<double>(), vb, stream);
     SED_TRY_CUDA(cudaMemcpyAsync(hp.data(), part.ptr, (size_t)vb * kDotCols * 8, cudaMemcpyDeviceToHost, stream));
     SED_TRY_CUDA(cudaStreamSynchronize(stream));
     double s = 0.0;
@@ -320,7 +369,8 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
 
   std::vector<double> T((size_t)(m + 1) * (m + 1), 0.0);
   auto Tij = [&](uint32_t i, uint32_t j) -> double& { return T[(size_t)i * (m + 1) + j]; };
-  uint32_t k = 0;  // index of the newest basis vector
+  uint32_t k = 0;      // index of the newest basis vector
+  uint32_t arrow = 0;  // index of the continuation vector after the last restart (0: none)
   std::vector<double> c, c2, theta, Z;
   out = ThickResult{};
   while (true) {
@@ -336,9 +386,18 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
     }
     ++out.matvecs;
     ++out.steps;
-    if (int st = dots(k + 1, w, c)) return st;
-    SED_TRY_CUDA(cudaMemcpyAsync(coef.ptr, c.data(), (k + 1) * 8, cudaMemcpyHostToDevice, stream));
-    { k_tupdate<S><<<vb, 256, 0, stream>>>(V, D, k + 1, coef.as<double>(), w, D); note_launches(1); }
+    // Orthogonalisation, two passes. Away from the continuation vector of a
+    // restart, H v_k has (in exact arithmetic) components along v_{k-1} and
+    // v_k only, so the first pass projects out those two; the second pass
+    // runs against the whole basis and removes what rounding left along any
+    // stored vector. On the step from the continuation vector (whose column
+    // of the projected matrix is an arrowhead over the kept Ritz vectors)
+    // both passes are full.
+    uint32_t const first = k > arrow ? k - 1 : 0;
+    if (int st = dots_at(first, k + 1 - first, w, c)) return st;
+    SED_TRY_CUDA(cudaMemcpyAsync(coef.ptr, c.data(), (k + 1 - first) * 8, cudaMemcpyHostToDevice, stream));
+    { k_tupdate<S><<<vb, 256, 0, stream>>>(V + (uint64_t)first * D, D, k + 1 - first, coef.as<double>(), w, D); note_launches(1); }
+    c.insert(c.begin(), first, 0.0);
     if (int st = dots(k + 1, w, c2)) return st;
     SED_TRY_CUDA(cudaMemcpyAsync(coef.ptr, c2.data(), (k + 1) * 8, cudaMemcpyHostToDevice, stream));
     { k_tupdate<S><<<vb, 256, 0, stream>>>(V, D, k + 1, coef.as<double>(), w, D); note_launches(1); }
@@ -411,7 +470,7 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
       for (uint32_t q = 0; q < n; ++q)
         for (uint32_t cidx = 0; cidx < keep; ++cidx) Y[(size_t)q * keep + cidx] = Z[(size_t)q * n + cidx];
       SED_TRY_CUDA(cudaMemcpyAsync(Yb.ptr, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, stream));
-      { k_trotate<S><<<vb, 256, 0, stream>>>(V, D, n, Yb.as<double>(), keep, D); note_launches(1); }
+      launch_trotate<S>(V, D, n, Yb.as<double>(), keep, D, vb, stream);
       if (breakdown) {
         // no continuation vector: a fresh random direction, orthogonalised
         { k_trandom<S><<<vb, 256, 0, stream>>>(V + (uint64_t)keep * D, D, seed + 7919 * (out.restarts + 1)); note_launches(1); }
@@ -430,6 +489,7 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
       std::fill(T.begin(), T.end(), 0.0);
       for (uint32_t i = 0; i < keep; ++i) Tij(i, i) = theta[i];
       k = keep;
+      arrow = keep;
       ++out.restarts;
       continue;
     }
