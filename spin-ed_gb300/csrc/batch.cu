@@ -316,8 +316,10 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
 // X -= sum_{i<nb} V_i C_i (two passes of classical Gram-Schmidt). C (shared,
 // nb * 16, row-major a*4+c per block, may be null) receives the summed
 // coefficients; norms2 (shared, may be null) the squared column norms of X
-// before the projection.
-__device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2) {
+// before the projection. The first pass runs against blocks first .. nb-1
+// only (first > 0 where X = H V_{nb-1} is, in exact arithmetic, orthogonal
+// to the older blocks); the second pass always runs against all nb blocks.
+__device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, uint32_t first = 0) {
   double const* V = x.c.V;
   uint64_t const D = x.c.D;
   int const K = (int)nb * 16;
@@ -325,7 +327,8 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2) 
     for (int k = threadIdx.x; k < K; k += blockDim.x) C[k] = 0.0;
   __syncthreads();
   for (int pass = 0; pass < 2; ++pass) {
-    for (uint32_t i = 0; i < nb; ++i) {
+    uint32_t const i0 = pass == 0 ? first : 0u;
+    for (uint32_t i = i0; i < nb; ++i) {
       double p[16] = {};
       double const* Vi = V + (uint64_t)i * D * 4;
       for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
@@ -353,14 +356,15 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2) 
       Kp = K + 4;
     }
     double* tot = x.tmp + kPart;
-    if (!group_sum(x, x.tmp, Kp, tot)) return false;
+    int const k0 = 16 * (int)i0;
+    if (!group_sum(x, x.tmp + k0, Kp - k0, tot + k0)) return false;
     if (C)
-      for (int k = threadIdx.x; k < K; k += blockDim.x) C[k] += tot[k];
+      for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) C[k] += tot[k];
     if (Kp > K && threadIdx.x < 4) norms2[threadIdx.x] = tot[K + threadIdx.x];
     // X -= sum_i V_i tot_i
     for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
       Row4 w = *reinterpret_cast<Row4 const*>(X + r * 4);
-      for (uint32_t i = 0; i < nb; ++i) {
+      for (uint32_t i = i0; i < nb; ++i) {
         Row4 const a = *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4);
         double const* c = tot + 16 * i;
         w.x -= a.x * c[0] + a.y * c[4] + a.z * c[8] + a.w * c[12];
@@ -383,7 +387,8 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2) 
 // projected against the basis, and the block is factored by CholQR2. Rb gets
 // R with the replaced columns zeroed (their coupling to H V_j is below the
 // threshold). Returns false on barrier failure or if the replacement fails.
-__device__ bool lanczos_qr(Ctx& x, double* X, uint32_t nb, double* norms2, double* Rb, uint32_t step) {
+__device__ bool lanczos_qr(Ctx& x, double* X, uint32_t nb, double* norms2, double* Rb, uint32_t step,
+                           bool& replaced) {
   __shared__ double R[16];
   __shared__ int mask_s, total_mask_s;
   if (threadIdx.x == 0) total_mask_s = 0;
@@ -429,6 +434,7 @@ __device__ bool lanczos_qr(Ctx& x, double* X, uint32_t nb, double* norms2, doubl
     Rb[threadIdx.x] = (total_mask_s & (1 << col)) ? 0.0 : R[threadIdx.x];
   }
   __syncthreads();
+  replaced = total_mask_s != 0;
   return true;
 }
 
@@ -640,6 +646,10 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
   uint32_t j0 = 0;
   while (status != 3) {
     uint32_t j = j0;
+    // block whose H-image needs full projections in both passes: the
+    // continuation block of a restart (arrowhead couplings) or a block with
+    // replaced (random) columns
+    uint32_t full_from = j0;
     bool broke = false;
     for (;; ++j) {
       double* Vj = c.V + (uint64_t)j * c.D * 4;
@@ -649,7 +659,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
       ++matvecs;
       __syncthreads();
       lap(0);
-      if (!cgs2(x, c.W, j + 1, C, norms2)) return;
+      if (!cgs2(x, c.W, j + 1, C, norms2, j > full_from ? j - 1 : 0u)) return;
       lap(1);
       if (leader)
         for (int k = threadIdx.x; k < 16 * (int)(j + 1); k += blockDim.x) c.Tc[j * kStride + k] = C[k];
@@ -657,7 +667,9 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
       // QR of W -> V_{j+1}, B_j (with deflation of lost directions)
       double* Vn = c.V + (uint64_t)(j + 1) * c.D * 4;
       copy_block(x, Vn, c.W);
-      broke = !lanczos_qr(x, Vn, j + 1, norms2, Rb, steps);
+      bool replaced = false;
+      broke = !lanczos_qr(x, Vn, j + 1, norms2, Rb, steps, replaced);
+      if (replaced) full_from = j + 1;
       if (*(volatile int*)a.error) return;
       if (leader)
         for (int k = threadIdx.x; k < 16; k += blockDim.x) c.Bblk[j * 16 + k] = broke ? 0.0 : Rb[k];
@@ -746,7 +758,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
   }
 }
 
-__global__ void __launch_bounds__(256) k_batch_lanczos(BatchArgs a) {
+__global__ void __launch_bounds__(256, 2) k_batch_lanczos(BatchArgs a) {
   __shared__ double red[8 * 16];
   __shared__ double tmp[2 * kPart];
   __shared__ double C[kPart];
