@@ -124,7 +124,29 @@ __global__ void k_update(X* __restrict__ V, uint64_t ld_v, uint64_t D, LzHeader 
 }
 
 // Classical Gram-Schmidt pass against V[0..k]: c_j = <V_j, w> (partials per
-// block and vector, 16 vectors per blockIdx.y).
+// block and vector, 16 vectors per blockIdx.y). The vector count NJ of the
+// block's group is a template parameter of the loop body, chosen on the
+// device from k: a predicated-off FP64 FMA still takes its issue slot on
+// GB300's slow FP64 pipe, so the body never pads to 16.
+template <int NJ, class X>
+__device__ __forceinline__ void cgs_dots_body(X const* __restrict__ V, uint64_t ld_v, uint64_t D, X const* w,
+                                              uint32_t j0, double* red, double* __restrict__ partial) {
+  double acc[NJ];
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) acc[j] = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    auto const wi = Store<X>::load(w, i);
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) acc[j] += dot_re(Store<X>::load(V + (uint64_t)(j0 + j) * ld_v, i), wi);
+  }
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    double const t = block_sum(acc[j], red);
+    if (threadIdx.x == 0) partial[(uint64_t)(j0 + j) * gridDim.x + blockIdx.x] = t;
+  }
+}
+
 template <class X>
 __global__ void k_cgs_dots(X const* __restrict__ V, uint64_t ld_v, uint64_t D, LzHeader const* h,
                            double* __restrict__ partial /* [m_max][gridDim.x] */) {
@@ -135,19 +157,12 @@ __global__ void k_cgs_dots(X const* __restrict__ V, uint64_t ld_v, uint64_t D, L
   if (j0 > k) return;  // uniform per block
   uint32_t const nj = min(16u, k + 1 - j0);
   X const* w = V + (uint64_t)(k + 1) * ld_v;
-  double acc[16];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) acc[j] = 0.0;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    auto const wi = Store<X>::load(w, i);
-#pragma unroll
-    for (int j = 0; j < 16; ++j)
-      if ((uint32_t)j < nj) acc[j] += dot_re(Store<X>::load(V + (uint64_t)(j0 + j) * ld_v, i), wi);
-  }
-  for (int j = 0; j < 16; ++j) {
-    double const t = block_sum(acc[j], red);
-    if (threadIdx.x == 0 && (uint32_t)j < nj) partial[(uint64_t)(j0 + j) * gridDim.x + blockIdx.x] = t;
+  switch (nj) {
+#define SED_CGS(N) \
+  case N: cgs_dots_body<N, X>(V, ld_v, D, w, j0, red, partial); break;
+    SED_CGS(1) SED_CGS(2) SED_CGS(3) SED_CGS(4) SED_CGS(5) SED_CGS(6) SED_CGS(7) SED_CGS(8)
+    SED_CGS(9) SED_CGS(10) SED_CGS(11) SED_CGS(12) SED_CGS(13) SED_CGS(14) SED_CGS(15) SED_CGS(16)
+#undef SED_CGS
   }
 }
 
