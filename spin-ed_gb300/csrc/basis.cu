@@ -36,9 +36,11 @@ template <class W>
 __global__ void k_mark(__grid_constant__ const PlanView P, uint64_t const* __restrict__ binom, unsigned n, int hw,
                        uint64_t space, uint64_t n_words, uint32_t* __restrict__ bitmap,
                        uint64_t const* __restrict__ seg_begin, uint64_t const* __restrict__ seg_prefix, uint32_t n_seg) {
-  __shared__ uint16_t srow[2048];
+  __shared__ uint16_t srow[2048], sline[2048];
   __shared__ uint64_t sb[kMaxSegs], sp[kMaxSegs + 1];
-  RowTab const RT = stage_rows(P, srow);
+  stage_lines(P, sline);
+  RowTab RT = stage_rows(P, srow);
+  attach_lines(P, sline, RT);
   for (uint32_t q = threadIdx.x; q < n_seg; q += blockDim.x) {
     sb[q] = seg_begin[q];
     sp[q] = seg_prefix[q];
@@ -227,6 +229,7 @@ int basis_upload_plan(BasisData& b, cudaStream_t stream) {
       {p.rot_exp.data(), p.rot_exp.size() * 4, 0},       {p.sh_mask.data(), p.sh_mask.size() * 8, 0},
       {p.sh_rot.data(), p.sh_rot.size() * 4, 0},         {p.sh_exp.data(), p.sh_exp.size() * 4, 0},
       {p.pos.data(), p.pos.size(), 0},
+      {p.line_row.data(), p.line_row.size() * 2, 0},     {p.line_col.data(), p.line_col.size() * 2, 0},
   };
   size_t total = 16;
   for (auto& q : parts) {
@@ -255,6 +258,8 @@ int basis_upload_plan(BasisData& b, cudaStream_t stream) {
   v.sh_rot = (uint32_t const*)(base + parts[12].off);
   v.sh_exp = (uint32_t const*)(base + parts[13].off);
   v.pos = (uint8_t const*)(base + parts[14].off);
+  v.line_row = (uint16_t const*)(base + parts[15].off);
+  v.line_col = (uint16_t const*)(base + parts[16].off);
   b.plan_dev = v;
   std::vector<uint64_t> binom(65 * 65, 0);
   for (unsigned i = 0; i <= 64; ++i) {

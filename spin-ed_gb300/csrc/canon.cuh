@@ -80,6 +80,18 @@ struct PlanView {
   uint64_t const* sh_mask;     // [n_rows][2] shift: image row j <- source row (j + t) mod n_rows
   uint32_t const* sh_rot;      // [n_rows][2]
   uint32_t const* sh_exp;      // [n_rows] exponent of the shift generator
+  // Line tables (rows == 1, line_fast = 1): every row of every coset image
+  // of x is a row or (on a square torus, line_cols = 1) a column of x, read
+  // forwards or backwards from some start. The smallest rotation of an image
+  // row is then a table lookup on that line of x: line_row[v] / line_col[v]
+  // is the smallest of row_min over the orientations (and inversions) in
+  // which the cosets present a row / column with bits v. Column j of x, as
+  // a row value (bit r = bit r * row_bits + j of x), is
+  // (((x >> j) & col_m) * col_k) >> col_s, masked to n_rows bits.
+  uint32_t line_fast, line_cols, col_s;
+  uint64_t col_m, col_k;
+  uint16_t const* line_row;  // [1 << row_bits]
+  uint16_t const* line_col;  // [1 << row_bits]
 };
 
 struct IndexView {
@@ -186,6 +198,8 @@ SED_HD W apply2(W y, uint64_t m0, uint64_t m1, unsigned r0, unsigned r1) {
 struct RowTab {
   uint16_t const* min;  // smallest rotation of a row
   uint16_t const* set;  // rotations reaching it
+  uint16_t const* lrow = nullptr;  // line tables (PlanView::line_row / line_col), when staged
+  uint16_t const* lcol = nullptr;
 };
 // Both routines enumerate the H-images (of y, and of ~y with inversion) that
 // can be the smallest one: the smallest image has the smallest top row (most
@@ -330,6 +344,24 @@ SED_HD bool chain_each(W y, W mask, PlanView const& P, F&& f) {
 #ifdef __CUDACC__
 // Copies the row tables into shared memory (2048 uint16 slots) and returns
 // them. Every thread of the block must call it.
+// Line tables into sm[0 .. 2048) (rows == 1, line_fast); call before
+// stage_rows, whose barrier publishes them, then attach with attach_lines.
+__device__ __forceinline__ void stage_lines(PlanView const& P, uint16_t* sm) {
+  if (P.rows == 1 && P.line_fast) {
+    unsigned const n = 1u << P.row_bits;
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+      sm[i] = P.line_row[i];
+      sm[1024 + i] = P.line_cols ? P.line_col[i] : (uint16_t)0;
+    }
+  }
+}
+__device__ __forceinline__ void attach_lines(PlanView const& P, uint16_t const* sm, RowTab& T) {
+  if (P.rows == 1 && P.line_fast) {
+    T.lrow = sm;
+    T.lcol = sm + 1024;
+  }
+}
+
 __device__ __forceinline__ RowTab stage_rows(PlanView const& P, uint16_t* sm) {
   if (P.rows == 1) {
     unsigned const n = 1u << P.row_bits;
@@ -491,8 +523,28 @@ SED_HD uint32_t representative_weight(W x, PlanView const& P, RowTab const& T) {
   if (P.rows == 1) {
     uint32_t const rm = (uint32_t)P.row_mask;
     uint32_t const xt = (uint32_t)(x >> ((P.n_rows - 1) * P.row_bits));
-    for (uint32_t c = 0; c < P.n_cosets; ++c)  // pass A with early rejection
-      if (rows_min_top<W>(coset_apply<W>(x, P, c), P, T) < xt) return 0;
+    if (T.lrow) {  // pass A from the lines of x: the image rows of all cosets at once
+      W v = x;
+#pragma unroll
+      for (uint32_t k = 0; k < SED_MAX_ROWS; ++k) {
+        if (k < P.n_rows) {
+          if (T.lrow[(uint32_t)v & rm] < xt) return 0;
+          v >>= P.row_bits;
+        }
+      }
+      if (P.line_cols) {
+#pragma unroll
+        for (uint32_t j = 0; j < SED_MAX_ROWS; ++j) {
+          if (j < P.row_bits) {
+            uint64_t const col = ((((uint64_t)x >> j) & P.col_m) * P.col_k) >> P.col_s;
+            if (T.lcol[(uint32_t)col & rm] < xt) return 0;
+          }
+        }
+      }
+    } else {
+      for (uint32_t c = 0; c < P.n_cosets; ++c)  // pass A with early rejection
+        if (rows_min_top<W>(coset_apply<W>(x, P, c), P, T) < xt) return 0;
+    }
     for (uint32_t c = 0; c < P.n_cosets; ++c) {  // pass B: images whose top row equals x's
       W const y = coset_apply<W>(x, P, c);
       for (uint32_t k = 0; k < P.n_rows; ++k) {

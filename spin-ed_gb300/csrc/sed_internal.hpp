@@ -124,6 +124,10 @@ struct SymPlanHost {
   std::vector<uint16_t> row_min, row_set;
   std::vector<uint64_t> rot_mask, sh_mask;
   std::vector<uint32_t> rot_rot, rot_exp, sh_rot, sh_exp;
+  // line tables (see PlanView::line_fast)
+  unsigned line_fast = 0, line_cols = 0, col_s = 0;
+  uint64_t col_m = 0, col_k = 0;
+  std::vector<uint16_t> line_row, line_col;
   PlanView view() const;
 };
 

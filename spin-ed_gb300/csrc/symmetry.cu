@@ -510,6 +510,82 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
           out.row_min[v] = (uint16_t)best;
           out.row_set[v] = (uint16_t)set;
         }
+        // Line tables: image row k of coset representative c takes source
+        // bits p[k B + t], t < B (image bit j <- source bit p[j]). Each must be
+        // a row (same source row, within-row positions stepping by +1 or -1
+        // cyclically) or, when there are as many rows as bits per row, a
+        // column (same source column, rows stepping by +1 or -1); and each
+        // (kind, direction) that occurs must occur for every line of its
+        // kind. Then the image rows of all cosets are exactly those lines.
+        unsigned const R = out.n_rows;
+        uint32_t used[2][2] = {{0, 0}, {0, 0}};  // [row, column][forward, backward]: lines seen
+        bool lines_ok = true;
+        for (size_t c = 0; c < cosets.size() && lines_ok; ++c) {
+          auto const& p = elems[cosets[c]];
+          for (unsigned k = 0; k < R && lines_ok; ++k) {
+            unsigned sp[64];  // source bit of image bit t of row k
+            for (unsigned t = 0; t < B; ++t) sp[t] = p[k * B + t];
+            int kind = -1, dir = -1;
+            unsigned line = 0;
+            bool same_row = true, same_col = true;
+            for (unsigned t = 0; t < B; ++t) {
+              same_row = same_row && sp[t] / B == sp[0] / B;
+              same_col = same_col && sp[t] % B == sp[0] % B;
+            }
+            if (same_row) {
+              unsigned const a = sp[0] % B;
+              bool f = true, b = true;
+              for (unsigned t = 0; t < B; ++t) {
+                f = f && sp[t] % B == (a + t) % B;
+                b = b && sp[t] % B == (a + B - t) % B;
+              }
+              if (f || b) kind = 0, dir = f ? 0 : 1, line = sp[0] / B;
+            } else if (same_col && R == B) {
+              unsigned const a = sp[0] / B;
+              bool f = true, b = true;
+              for (unsigned t = 0; t < B; ++t) {
+                f = f && sp[t] / B == (a + t) % R;
+                b = b && sp[t] / B == (a + R - t) % R;
+              }
+              if (f || b) kind = 1, dir = f ? 0 : 1, line = sp[0] % B;
+            }
+            if (kind < 0) lines_ok = false;
+            else used[kind][dir] |= 1u << line;
+          }
+        }
+        uint32_t const all_rows = (1u << R) - 1u, all_cols = (1u << B) - 1u;
+        for (int d = 0; d < 2 && lines_ok; ++d)
+          lines_ok = (used[0][d] == 0 || used[0][d] == all_rows) && (used[1][d] == 0 || used[1][d] == all_cols);
+        if (lines_ok) {
+          auto rev = [&](unsigned v) {
+            unsigned r = 0;
+            for (unsigned t = 0; t < B; ++t) r |= ((v >> t) & 1u) << (B - 1 - t);
+            return r;
+          };
+          auto table = [&](uint32_t const (&u)[2], std::vector<uint16_t>& out_tab) {
+            out_tab.assign(nv, 0xFFFF);
+            for (unsigned v = 0; v < nv; ++v)
+              for (int d = 0; d < 2; ++d) {
+                if (!u[d]) continue;
+                unsigned const w = d ? rev(v) : v;
+                out_tab[v] = std::min(out_tab[v], out.row_min[w]);
+                if (spin_inversion) out_tab[v] = std::min(out_tab[v], out.row_min[w ^ (nv - 1)]);
+              }
+          };
+          table(used[0], out.line_row);
+          out.line_cols = (used[1][0] | used[1][1]) ? 1u : 0u;
+          if (out.line_cols) {
+            table(used[1], out.line_col);
+            out.col_s = (R - 1) * (B - 1);
+            out.col_m = 0;
+            out.col_k = 0;
+            for (unsigned r = 0; r < R; ++r) {
+              out.col_m |= (uint64_t)1 << (r * B);
+              out.col_k |= (uint64_t)1 << (out.col_s - r * (B - 1));
+            }
+          }
+          out.line_fast = 1;
+        }
       }
       if (!ok) out.rows = 0;
     }
@@ -544,13 +620,26 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
         same = same && representative_weight<uint64_t>(r, vx) == representative_weight<uint64_t>(r, ve);
       }
       if (!same) return fail(LS_SYSTEM_ERROR, "structured subgroup walk disagrees with the explicit list");
+      if (out.line_fast) {  // the line-table test of the row path against the explicit list
+        RowTab const TL{out.row_min.data(), out.row_set.data(), out.line_row.data(),
+                        out.line_cols ? out.line_col.data() : nullptr};
+        uint64_t const r = canonicalize<uint64_t>(x, ve).rep;
+        bool const lines_same =
+            width == 32
+                ? representative_weight<uint32_t>((uint32_t)x, vx, TL) == representative_weight<uint32_t>((uint32_t)x, ve) &&
+                      representative_weight<uint32_t>((uint32_t)r, vx, TL) ==
+                          representative_weight<uint32_t>((uint32_t)r, ve)
+                : representative_weight<uint64_t>(x, vx, TL) == representative_weight<uint64_t>(x, ve) &&
+                      representative_weight<uint64_t>(r, vx, TL) == representative_weight<uint64_t>(r, ve);
+        if (!lines_same) return fail(LS_SYSTEM_ERROR, "line tables disagree with the explicit list");
+      }
     }
   }
   if (logging_enabled())
     log_line("symmetry plan: |G| = %u (x%u inversion), |H| = %u (cyclic product: %u, rows: %u of %u bits, "
-             "mode %u), cosets = %u, stages = %u, terms = %u",
+             "mode %u), cosets = %u, stages = %u, terms = %u, line tables: %u (columns: %u)",
              G, spin_inversion ? 2u : 1u, out.n_h, out.cyc, out.n_rows, out.row_bits, out.rows, out.n_cosets,
-             out.n_stages, out.n_terms);
+             out.n_stages, out.n_terms, out.line_fast, out.line_cols);
   return LS_SUCCESS;
 }
 
@@ -582,6 +671,13 @@ PlanView SymPlanHost::view() const {
   v.rot_phase = rot_phase;
   v.shift_phase = shift_phase;
   v.row_mask = row_mask;
+  v.line_fast = line_fast;
+  v.line_cols = line_cols;
+  v.col_s = col_s;
+  v.col_m = col_m;
+  v.col_k = col_k;
+  v.line_row = line_row.data();
+  v.line_col = line_col.data();
   v.row_min = row_min.data();
   v.row_set = row_set.data();
   v.rot_mask = rot_mask.data();
