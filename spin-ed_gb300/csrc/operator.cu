@@ -429,6 +429,25 @@ __device__ __forceinline__ RankTab stage_rank(uint64_t const* __restrict__ binom
   return RankTab{nullptr, 0, 0};
 }
 
+// Table index on a row-structured group: the stored words (rows_rot_min
+// classes) have a smallest-rotation top row T, so the table is laid out as
+// one segment per such T, of the ranks of the lower bits in their weight
+// class: index = seg_off[T] + rank(low bits). seg_off[T] is ~0 for a top
+// row that cannot occur.
+struct RowIndex {
+  uint64_t const* seg_off;  // [1 << row_bits], or null: plain colex rank of the whole word
+  uint64_t low_mask;
+  uint32_t top_shift;
+};
+
+__device__ __forceinline__ uint64_t table_index(uint64_t w, int hw, RankTab const& RK, uint64_t const* bin,
+                                                RowIndex const& RI) {
+  if (!RI.seg_off) return word_rank_tab(w, hw, RK, bin);
+  uint64_t const off = __ldg(RI.seg_off + (w >> RI.top_shift));
+  if (off == ~(uint64_t)0) return off;
+  return off + word_rank_tab(w & RI.low_mask, hw, RK, bin);
+}
+
 // On a row-structured group (a torus: one generator rotates every row, the
 // other shifts rows) the table stores, of each set {row rotations of z and of
 // ~z}, only the smallest word: it has the smallest rotation of z's (or ~z's)
@@ -480,7 +499,8 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
                                                        uint64_t D, int hw, uint64_t const* __restrict__ binom,
                                                        uint32_t* __restrict__ table, uint64_t space,
                                                        int* __restrict__ error, uint64_t const* __restrict__ rank_tab,
-                                                       uint32_t rank_words, uint32_t n_chunks, uint32_t wp1) {
+                                                       uint32_t rank_words, uint32_t n_chunks, uint32_t wp1,
+                                                       RowIndex RI) {
   extern __shared__ uint64_t dyn_rank[];
   __shared__ uint16_t rows_s[2048];
   uint64_t const* const bin = dyn_rank;
@@ -527,7 +547,7 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
       uint32_t const tt = k + 1 == P.n_rows ? 0u : k + 1;
       uint64_t ph = (uint64_t)pc + (uint64_t)P.rot_exp[br] * P.rot_phase + (uint64_t)P.sh_exp[tt] * P.shift_phase;
       if (binv) ph += P.inv_phase;
-      uint64_t const k0 = word_rank_tab((uint64_t)best, hw, RK, bin);
+      uint64_t const k0 = table_index((uint64_t)best, hw, RK, bin, RI);
       if (k0 < space) table[k0] = (uint32_t)j | ((ph % P.L) ? kTabSign : 0u);
       else *error = 1;
     }
@@ -542,7 +562,7 @@ __global__ void __launch_bounds__(256) k_orbit_scatter(__grid_constant__ const P
       w = (W)(~z & mask);
       pw = add_phase(ph, P.inv_phase, P.L);
     }
-    uint64_t const k0 = word_rank_tab((uint64_t)w, hw, RK, bin);
+    uint64_t const k0 = table_index((uint64_t)w, hw, RK, bin, RI);
     if (k0 < space) table[k0] = (uint32_t)j | (pw ? kTabSign : 0u);
     else *error = 1;
   }
@@ -561,7 +581,7 @@ __global__ void __launch_bounds__(256) k_record_table(__grid_constant__ const Pl
                                                       int* __restrict__ error, bool inv_half, bool inv_sign,
                                                       uint32_t n_bits, uint64_t word_mask,
                                                       uint64_t const* __restrict__ rank_tab, uint32_t rank_words,
-                                                      uint32_t n_chunks, uint32_t wp1) {
+                                                      uint32_t n_chunks, uint32_t wp1, RowIndex RI) {
   extern __shared__ uint64_t dyn_rank[];
   __shared__ uint16_t rows_s[2048];
   uint64_t const* const bin = dyn_rank;
@@ -592,7 +612,7 @@ __global__ void __launch_bounds__(256) k_record_table(__grid_constant__ const Pl
           w = ~st & word_mask;
           flip = inv_sign;
         }
-        uint64_t const k = word_rank_tab(w, hw, RK, bin);
+        uint64_t const k = table_index(w, hw, RK, bin, RI);
         if (k < space) v = __ldg(table + k);
         else *error = 1;
         if (flip && v != kNull) v ^= kTabSign;
@@ -873,10 +893,30 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
   // orbit-table path: real characters, a weight class small enough to tabulate
   uint64_t space = 0;
   bool use_table = false;
+  // row-structured plans: one segment per possible top row (see table_index)
+  std::vector<uint64_t> seg_off;
   if (n_slices && g_record_mode != SED_RECORD_CANONICALISE && characters_real(b) && D < kTabSign) {
     bool const half = b.plan.inv != 0;
     if (b.hw >= 0 && b.hw <= 32 && b.n <= 64) space = host_binom(half ? b.n - 1 : b.n, (unsigned)b.hw);
     else if (b.hw < 0 && b.n <= 34) space = (uint64_t)1 << (half ? b.n - 1 : b.n);
+    if (space && b.plan.rows == 1 && b.plan.row_bits <= 10 && b.n > b.plan.row_bits) {
+      unsigned const B = b.plan.row_bits, L = b.n - B;
+      uint32_t const rm = (1u << B) - 1u;
+      uint64_t total = 0;
+      seg_off.assign((size_t)1 << B, ~(uint64_t)0);
+      for (uint32_t T = 0; T <= rm; ++T) {
+        bool ok = b.plan.row_min[T] == T;
+        if (b.plan.inv) ok = ok && b.plan.row_min[T ^ rm] >= T;
+        int const need = b.hw - __builtin_popcount(T);
+        uint64_t const cnt = b.hw < 0 ? ((uint64_t)1 << L)
+                                      : (need < 0 || (unsigned)need > L ? 0 : host_binom(L, (unsigned)need));
+        if (ok) {
+          seg_off[T] = total;
+          total += cnt;
+        }
+      }
+      space = total;
+    }
     size_t fr = 0, tt = 0;
     SED_TRY_CUDA(cudaMemGetInfo(&fr, &tt));
     use_table = space > 0 && space * 4 <= fr / 5 * 2;
@@ -890,6 +930,14 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     DeviceBuffer err;
     if (int st = err.allocate(16)) return st;
     if (int st = krylov_take(space * 4, table)) return st;
+    DeviceBuffer seg_buf;
+    RowIndex RI{nullptr, 0, 0};
+    if (!seg_off.empty()) {
+      if (int st = seg_buf.allocate(seg_off.size() * 8)) return st;
+      SED_TRY_CUDA(cudaMemcpyAsync(seg_buf.ptr, seg_off.data(), seg_off.size() * 8, cudaMemcpyHostToDevice, stream));
+      unsigned const L = b.n - b.plan.row_bits;
+      RI = RowIndex{seg_buf.as<uint64_t>(), ((uint64_t)1 << L) - 1, L};
+    }
     SED_TRY_CUDA(cudaMemsetAsync(table.ptr, 0xFF, space * 4, stream));
     SED_TRY_CUDA(cudaMemsetAsync(err.ptr, 0, 16, stream));
     // chunked rank table (6-bit chunks) when it fits in 96 KB of shared memory
@@ -927,10 +975,10 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     uint64_t const* rtab = rank_words ? rank_buf.as<uint64_t>() : nullptr;
     if (wide) {
       cudaFuncSetAttribute(k_orbit_scatter<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
-      { k_orbit_scatter<uint64_t><<<sgrid, 256, dsmem, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>(), rtab, rank_words, n_chunks, wp1); note_launches(1); }
+      { k_orbit_scatter<uint64_t><<<sgrid, 256, dsmem, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>(), rtab, rank_words, n_chunks, wp1, RI); note_launches(1); }
     } else {
       cudaFuncSetAttribute(k_orbit_scatter<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
-      { k_orbit_scatter<uint32_t><<<sgrid, 256, dsmem, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>(), rtab, rank_words, n_chunks, wp1); note_launches(1); }
+      { k_orbit_scatter<uint32_t><<<sgrid, 256, dsmem, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>(), rtab, rank_words, n_chunks, wp1, RI); note_launches(1); }
     }
     SED_TRY_CUDA(cudaGetLastError());
     IndexView const I = b.index_view();
@@ -939,7 +987,7 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
       using W = decltype(w_tag);
       constexpr bool R = decltype(real_tag)::value;
       cudaFuncSetAttribute(k_record_table<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
-      { k_record_table<W, R><<<rgrid, 256, dsmem, stream>>>(b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask, rtab, rank_words, n_chunks, wp1); note_launches(1); }
+      { k_record_table<W, R><<<rgrid, 256, dsmem, stream>>>(b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices, sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(), sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), table.as<uint32_t>(), b.hw, b.binom.as<uint64_t>(), space, err.as<int>(), b.plan.inv != 0, b.plan.inv_phase != 0, b.plan.n_bits, b.plan.mask, rtab, rank_words, n_chunks, wp1, RI); note_launches(1); }
     };
     if (wide) {
       if (op.is_real) rec(uint64_t{}, std::true_type{});
