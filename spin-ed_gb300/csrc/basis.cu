@@ -534,10 +534,11 @@ int ls_get_states(ls_states** ptr, ls_spin_basis const* basis) {
   if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
   try {
     auto* s = new ls_states;
-    s->data.resize(b.D);
+    s->data.reset(new uint64_t[b.D ? b.D : 1]);
+    s->size = b.D;
     ScopedDevice dev(b.device);
     if (b.D) {
-      cudaError_t e = cudaMemcpy(s->data.data(), b.reps.ptr, b.D * 8, cudaMemcpyDeviceToHost);
+      cudaError_t e = cudaMemcpy(s->data.get(), b.reps.ptr, b.D * 8, cudaMemcpyDeviceToHost);
       if (e != cudaSuccess) {
         delete s;
         return fail(LS_CUDA_ERROR, std::string("ls_get_states: ") + cudaGetErrorString(e));
@@ -551,9 +552,9 @@ int ls_get_states(ls_states** ptr, ls_spin_basis const* basis) {
 }
 
 uint64_t const* ls_states_get_data(ls_states const* states) {
-  return states ? states->data.data() : nullptr;
+  return states ? states->data.get() : nullptr;
 }
-uint64_t ls_states_get_size(ls_states const* states) { return states ? states->data.size() : 0; }
+uint64_t ls_states_get_size(ls_states const* states) { return states ? states->size : 0; }
 void ls_destroy_states(ls_states* states) { delete states; }
 
 int sed_basis_get_norms(ls_spin_basis const* basis, double* out) {

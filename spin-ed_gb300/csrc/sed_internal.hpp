@@ -249,7 +249,8 @@ struct ls_spin_basis {
   std::shared_ptr<sed::BasisData> d;
 };
 struct ls_states {
-  std::vector<uint64_t> data;
+  std::unique_ptr<uint64_t[]> data;  // host copy of the representatives (not zero-filled first)
+  uint64_t size = 0;
 };
 struct ls_interaction {
   sed::InteractionData d;

@@ -596,7 +596,7 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
     ve.cyc = 0;
     ve.rows = 0;
     uint64_t rng = 0x9E3779B97F4A7C15ull;
-    for (int t = 0; t < 2048; ++t) {
+    for (int t = 0; t < 256; ++t) {  // 256 random words and their representatives (about 3 ms)
       rng ^= rng << 13;
       rng ^= rng >> 7;
       rng ^= rng << 17;

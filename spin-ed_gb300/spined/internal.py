@@ -23,6 +23,7 @@ Vectors may be numpy arrays (host) or CUDA tensors exposing data_ptr()
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 from typing import Sequence
 
@@ -190,15 +191,18 @@ def build_basis(basis: SpinBasis, representatives: np.ndarray | None = None) -> 
 
 
 def basis_get_states(basis: SpinBasis) -> np.ndarray:
-    """Internal.hs:238-244 (host copy owned by a states object)."""
+    """Internal.hs:238-244: a view of the host copy owned by a states object,
+    which is destroyed when the array (and every view of it) is collected,
+    as the reference's ForeignPtr finaliser does."""
     lib = L.load()
     states = _mk(lib.ls_get_states, basis.ptr)
-    try:
-        n = lib.ls_states_get_size(states)
-        data = lib.ls_states_get_data(states)
-        out = np.ctypeslib.as_array(C.cast(data, C.POINTER(C.c_uint64)), shape=(n,)).copy() if n else np.zeros(0, np.uint64)
-    finally:
+    n = lib.ls_states_get_size(states)
+    if not n:
         lib.ls_destroy_states(states)
+        return np.zeros(0, np.uint64)
+    data = lib.ls_states_get_data(states)
+    out = np.ctypeslib.as_array(C.cast(data, C.POINTER(C.c_uint64)), shape=(n,))
+    weakref.finalize(out, lib.ls_destroy_states, states)
     return out
 
 
