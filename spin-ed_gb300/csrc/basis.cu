@@ -155,8 +155,10 @@ __global__ void k_write(uint64_t const* __restrict__ binom, unsigned n, int hw, 
 template <class W>
 __global__ void k_weights(__grid_constant__ const PlanView P, uint64_t const* __restrict__ reps, uint64_t D,
                           uint32_t* __restrict__ weights) {
-  __shared__ uint16_t srow[2048];
-  RowTab const RT = stage_rows(P, srow);
+  __shared__ uint16_t srow[2048], sline[2048];
+  stage_lines(P, sline);
+  RowTab RT = stage_rows(P, srow);
+  attach_lines(P, sline, RT);
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
        i += (uint64_t)gridDim.x * blockDim.x)
     weights[i] = representative_weight<W>((W)reps[i], P, RT);
@@ -166,8 +168,10 @@ template <class W>
 __global__ void k_check_reps(__grid_constant__ const PlanView P, uint64_t const* __restrict__ reps, uint64_t D,
                              uint32_t* __restrict__ weights, unsigned n, int hw,
                              uint32_t* __restrict__ bad) {
-  __shared__ uint16_t srow[2048];
-  RowTab const RT = stage_rows(P, srow);
+  __shared__ uint16_t srow[2048], sline[2048];
+  stage_lines(P, sline);
+  RowTab RT = stage_rows(P, srow);
+  attach_lines(P, sline, RT);
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
        i += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t const x = reps[i];
