@@ -144,3 +144,43 @@ def test_plan_canonicalises_like_oracle(sed, oracle, name, n, hw, inv, kind, sec
         assert r == r2, (x, r, r2)
         if ob.representative_weight(r2):
             assert ph * Lo == ph2 * L
+
+
+def _shear(L):
+    """(x, y) -> (x, y + x): maps the rows of an L x L torus onto diagonals."""
+    idx = lambda x, y: (y % L) * L + (x % L)
+    return [idx(x, y + x) for y in range(L) for x in range(L)]
+
+
+LINE_CASES = [
+    # name, n, hw, inv, generators (permutation, sector), line tables, columns
+    ("square4_full", 16, 8, 1, lambda lt: [(g, 0) for g in lt.square_symmetries(4)], 1, 1),
+    ("square6_inv-", 36, 18, -1, lambda lt: [(g, 0) for g in lt.square_symmetries(6)], 1, 1),
+    ("square6_C4_only", 36, 18, 1, lambda lt: [(g, 0) for g in lt.square_symmetries(6)[:2] + lt.square_symmetries(6)[4:]], 1, 1),
+    ("square4_momentum", 16, 8, None, lambda lt: [(g, s) for g, s in zip(lt.square_symmetries(4)[:2], (1, 2))], 1, 0),
+    ("rect6x4_reflections", 24, 12, 1, lambda lt: [(g, 0) for g in lt.rect_translations(6, 4)] + [
+        ([(y * 6) + (5 - x) for y in range(4) for x in range(6)], 0),
+        ([((3 - y) * 6) + x for y in range(4) for x in range(6)], 0)], 1, 0),
+    ("square4_shear", 16, 8, None, lambda lt: [(g, 0) for g in lt.square_symmetries(4)[:2]] + [(_shear(4), 0)], 0, 0),
+]
+
+
+@pytest.mark.parametrize("name,n,hw,inv,gens,lines,cols", LINE_CASES, ids=[c[0] for c in LINE_CASES])
+def test_line_table_plans(sed, capfd, name, n, hw, inv, gens, lines, cols):
+    """Row-structured plans: the line tables are built exactly when every row
+    of every coset image is a row or a column of the word; the plan builder
+    checks the line-table test against the explicit group on random words
+    and fails the basis creation on any mismatch."""
+    from spined import _lib as L, lattices
+    lib = L.load()
+    lib.ls_enable_logging()
+    try:
+        g = sed.mk_group([sed.mk_symmetry(p, s) for p, s in gens(lattices)])
+        sed.mk_basis(g, n, hw, inv)
+    finally:
+        lib.ls_disable_logging()
+    err = capfd.readouterr().err
+    assert "mode 1" in err, err  # every case is row-structured
+    m = re.search(r"line tables: (\d) \(columns: (\d)\)", err)
+    assert m, err
+    assert (int(m.group(1)), int(m.group(2))) == (lines, cols), err
