@@ -27,6 +27,15 @@ CASES = {
                                    [(lattices.HEISENBERG, lattices.square_bonds(4))]),
     "torus6x4_w11": lattices.Model("t6x4", 24, 11, None, [(g, 0) for g in lattices.rect_translations(6, 4)],
                                    [(lattices.HEISENBERG, lattices.rect_bonds(6, 4))]),
+    # line tables: rotations without reflections (rows and columns in one
+    # direction each), and reflections of a 6x4 torus (rows only)
+    "square4_C4": lattices.Model("sq4c4", 16, 8, 1,
+                                 [(g, 0) for g in lattices.square_symmetries(4)[:2] + lattices.square_symmetries(4)[4:]],
+                                 [(lattices.HEISENBERG, lattices.square_bonds(4))]),
+    "torus6x4_refl": lattices.Model("t6x4r", 24, 12, 1, [(g, 0) for g in lattices.rect_translations(6, 4)] + [
+        ([(y * 6) + (5 - x) for y in range(4) for x in range(6)], 0),
+        ([((3 - y) * 6) + x for y in range(4) for x in range(6)], 0)],
+        [(lattices.HEISENBERG, lattices.rect_bonds(6, 4))]),
 }
 
 
