@@ -16,10 +16,11 @@
 // |c_r|^2 from ground states the solver computed at neighbouring couplings;
 // the start vector is v_r = prior(r) sign(s) exp(a) / n_r.
 //
-// GEMMs here are SIMT tiles (64 x 64 outputs per 256-thread block, 16-deep K
-// steps through shared memory, 4 x 4 outputs per thread) with arbitrary
-// strides, so one kernel serves every product of the forward and backward
-// passes.
+// Training GEMMs are SIMT tiles (64 x 64 outputs per 256-thread block,
+// 16-deep K steps through shared memory, 4 x 4 outputs per thread) with
+// arbitrary strides, so one kernel serves every product of the forward and
+// backward passes. Inference (forward and start vector) runs the whole
+// network on the tensor cores in one persistent kernel, k_mlp_forward_tc.
 #include <cuda_bf16.h>
 
 #include <algorithm>
