@@ -306,9 +306,8 @@ def forms_arm(stream):
     start = torch.empty(D, dtype=torch.float64, device="cuda")
     net.start_vector(b.basis, out=start)
     for prec, name in ((L.SED_PRECISION_FP64, "learned_fp64"), (L.SED_PRECISION_MIXED, "learned_mixed")):
-        def run():
+        def run():  # the solver normalises the start vector itself
             net.start_vector(b.basis, out=start)
-            start.div_(torch.linalg.norm(start))
             return I.eigh(op0, tol=1e-8, out=v, start=start, precision=prec)
         t, r = timed(run)
         t_inf, _ = timed(lambda: net.start_vector(b.basis, out=start))

@@ -74,9 +74,8 @@ def run(L: int = 6, j2s=None, precision: str = "mixed", epochs: int = 8, per_poi
             row["warm"] = {"seconds": t, "steps": r.iterations, "E0": float(r.eigenvalues[0]),
                            "residual": float(r.residuals[0])}
         if data is not None:
-            def learned():
+            def learned():  # the solver normalises the start vector itself
                 net.start_vector(b.basis, out=start)
-                start.div_(torch.linalg.norm(start))
                 return I.eigh(op, tol=1e-8, out=psi, start=start, precision=prec)
             t, r = timed(learned)
             row["learned"] = {"seconds": t, "steps": r.iterations, "E0": float(r.eigenvalues[0]),
