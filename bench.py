@@ -223,7 +223,9 @@ def gpu_arm(args, rank, world, dist):
     spmv_ms = e0.elapsed_time(e1) / reps_n
     E_tot = op.stream_elements
     s_bytes = 8
-    alg = E_tot * 4 + D * 9 + D * s_bytes + E_tot * s_bytes + D * s_bytes  # SURVEY 8d form for the stream matvec
+    # algorithmic bytes of one streamed matvec: entries, diagonal + row class,
+    # x_i, the gathered x_j (one per element) and y
+    alg = E_tot * 4 + D * 9 + D * s_bytes + E_tot * s_bytes + D * s_bytes
     compulsory = E_tot * 4 + D * 9 + 2 * D * s_bytes
     peak, peak_kind = peaks()
     achieved = alg / (spmv_ms * 1e-3) / 1e9
