@@ -406,6 +406,21 @@ def cpu_sample(workload: str, budget_s: float = 8.0):
     }
 
 
+# the 6x6 workload's fixed sizes (sector dimension by Burnside's lemma, stored
+# elements and stream-form bytes as recorded), so that the CPU arm can state
+# the same config as the GPU arm
+SQUARE6_D = 15_804_956
+SQUARE6_ELEMENTS = 585_262_534
+SQUARE6_STREAM_BYTES = 2.73e9
+
+
+def workload_config(workload, precision, D, E_tot, stream_bytes, world):
+    name = (f"{workload}: Heisenberg, D={D}, plain FP64 Lanczos to resid<=1e-8, seed 1234"
+            if precision == "fp64" else f"{workload}: mixed precision")
+    return {"workload": name, "D": D, "elements_per_matvec": E_tot, "parallelism": f"replicas x{world}",
+            "l2": "working set (stream form %.2f GB) exceeds L2" % (stream_bytes / 1e9)}
+
+
 def reference_arm(args, rank):
     if rank != 0:
         return
@@ -421,7 +436,8 @@ def reference_arm(args, rank):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (lattice generated in code)",
-        "config": {"workload": args.workload},
+        "config": workload_config(args.workload, "fp64", SQUARE6_D, SQUARE6_ELEMENTS, SQUARE6_STREAM_BYTES, args.gpus)
+                  if args.workload == "square6" else {"workload": args.workload},
         "cpu_baseline": {"value": v, "unit": "s", "cores": s0["cores"], "kind": "port", "sample": s0["sample"]},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU restatement (oracle/), not the reference binary: GHC and the unpinned "
@@ -515,10 +531,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-stored/f64",
             "data": "synthetic (lattice generated in code; no dataset)",
-            "config": {"workload": f"{args.workload}: Heisenberg, D={r['D']}, plain FP64 Lanczos to resid<=1e-8, seed 1234"
-                       if args.precision == "fp64" else f"{args.workload}: mixed precision",
-                       "D": r["D"], "elements_per_matvec": r["E_tot"], "parallelism": f"replicas x{world}",
-                       "l2": "working set (stream form %.2f GB) exceeds L2" % (r["stream_bytes"] / 1e9)},
+            "config": workload_config(args.workload, args.precision, r["D"], r["E_tot"], r["stream_bytes"], world),
             "gpu_launches": r["launches"],
             "e2e": {"value": r["e2e_s"], "unit": "s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
             "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
