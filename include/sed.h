@@ -267,15 +267,21 @@ SED_API int sed_operator_matmat_device(ls_operator const* op, int dtype, uint64_
  * must be device memory; at most 64 columns per call. It performs no device
  * allocation: the operator must already be prepared (sed_operator_prepare,
  * or an earlier ls_operator_matmat); the streamed form is used if recorded,
- * else the on-the-fly form, and neither is recorded here. Partial sums live
- * in a 66 KiB scratch array in the library's static device memory (held on
- * every GPU that loads the library until exit) and shared by all calls: calls
- * that overlap on the GPU race on it. The first call on each device looks up
- * the scratch address (cudaGetSymbolAddress), so make that first call before
- * any stream capture. */
+ * else the on-the-fly form, and neither is recorded here. The work is
+ * enqueued on `stream` (a cudaStream_t): pass the stream on which x was
+ * written, so that the matvec reads x only after those writes. NULL selects
+ * the operator's own non-blocking stream, which is ordered with nothing the
+ * caller enqueued: x must then be complete (and y no longer in use) before
+ * the call, e.g. after a cudaDeviceSynchronize. The call waits for `stream`
+ * to finish before it returns, so `out` holds the results on return. Partial
+ * sums live in a 66 KiB scratch array in the library's static device memory
+ * (held on every GPU that loads the library until exit) and shared by all
+ * calls: calls that overlap on the GPU race on it. The first call on each
+ * device looks up the scratch address (cudaGetSymbolAddress), so make that
+ * first call before any stream capture. */
 SED_API int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, uint64_t size,
                                              uint64_t block_size, void const* x, uint64_t x_stride,
-                                             void* y, uint64_t y_stride, void* out);
+                                             void* y, uint64_t y_stride, void* out, void* stream);
 
 /* Many Hamiltonians in one persistent launch. No counterpart in the
  * reference, which solves one operator per run. The lowest opts->nev (<= 4)

@@ -1597,7 +1597,11 @@ constexpr unsigned kNoAllocPartials = 4096;  // partial sums shared by all colum
 static __device__ __align__(256) double2 g_noalloc_scratch[kNoAllocPartials + kNoAllocCols];
 
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[64] = {nullptr};  // device address of the scratch, per device
+// Device address of the scratch, per device, looked up on the first call on
+// that device. A device reset (cudaDeviceReset) invalidates it together with
+// every libsed handle's device memory, so handles and this cache go stale at
+// the same moment: after a reset, no libsed object may be used again.
+void* g_noalloc_addr[64] = {nullptr};
 
 // Set-up, once per device and with that device current: the host-side name of
 // g_noalloc_scratch is not a device address, so look the address up.
@@ -1658,7 +1662,7 @@ __global__ void k_sum_partials_noalloc(double2 const* __restrict__ partial, unsi
 
 extern "C" int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, uint64_t size,
                                                 uint64_t block_size, void const* x, uint64_t x_stride,
-                                                void* y, uint64_t y_stride, void* out) {
+                                                void* y, uint64_t y_stride, void* out, void* stream) {
   using namespace sed;
   if (!op || !out || (block_size && (!x || !y)))
     return fail(LS_INVALID_ARGUMENT, "sed_operator_expectation_noalloc: NULL argument");
@@ -1679,7 +1683,10 @@ extern "C" int sed_operator_expectation_noalloc(ls_operator const* op, int dtype
   ScopedDevice dev(d.basis->device);
   double2* scratch = nullptr;
   if (int st = noalloc_scratch(d.basis->device, &scratch)) return st;
-  cudaStream_t s = d.cuda_stream;
+  // The caller's stream orders this work after the caller's writes of x (and
+  // of y); NULL means the operator's own stream, which is ordered with
+  // nothing the caller enqueued.
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : d.cuda_stream;
   bool const use_stream = d.stream.ready && d.form != SED_FORM_ON_THE_FLY;
   size_t const es = (size_t)elem_size(dtype);
   unsigned const per_col = std::max(1u, std::min(grid_size(size, d.basis->device, 4),

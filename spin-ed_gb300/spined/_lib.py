@@ -132,7 +132,7 @@ SIGNATURES = [
     ("sed_operator_stream_bytes", _U64, [_P]),
     ("sed_operator_stream_elements", _U64, [_P]),
     ("sed_operator_matmat_device", _I, [_P, _I, _U64, _U64, _P, _U64, _P, _U64, _P]),
-    ("sed_operator_expectation_noalloc", _I, [_P, _I, _U64, _U64, _P, _U64, _P, _U64, _P]),
+    ("sed_operator_expectation_noalloc", _I, [_P, _I, _U64, _U64, _P, _U64, _P, _U64, _P, _P]),
     ("sed_basis_get_norms", _I, [_P, _P]),
     ("sed_basis_device_states", _P, [_P]),
     ("sed_basis_index", _I, [_P, _U64, C.POINTER(_U64)]),

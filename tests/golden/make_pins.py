@@ -8,6 +8,7 @@ tests can check the oracle and the library against them on machines where
 the reference is not mounted.
 
 Usage: python tests/golden/make_pins.py /path/to/reference
+(or set SPINED_REFERENCE_DIR)
 """
 from __future__ import annotations
 
@@ -67,6 +68,25 @@ def main(ref: str) -> None:
     pins.append({"id": "spec_real_interaction", "source": f"test/Spec.hs:{n}",
                  "value": {"matrix": [[1.0, 0.0], [0.0, -1.0]], "sites": [[0], [2]], "is_real": True}})
 
+    # example/*.yaml: the lattice tables of the 6x6 and chain-40 workloads
+    def ints(block):
+        return [int(v) for v in re.findall(r"-?\d+", block)]
+
+    sq = open(os.path.join(ref, "example", "heisenberg_square_6x6.yaml")).read()
+    sq_lines = sq.splitlines()
+    n, _ = line_of(sq_lines, r"permutation:")
+    pairs = ints(re.search(r"sites:\s*\[(.*?)\]\]", sq, re.S).group(1) + "]")
+    pins.append({"id": "example_square6_tables", "source": f"example/heisenberg_square_6x6.yaml:{n}",
+                 "value": {"permutations": [ints(b) for b in re.findall(r"permutation:\s*\[([^\]]*)\]", sq)],
+                           "bonds": [pairs[i:i + 2] for i in range(0, len(pairs), 2)]},
+                 "what": "generators and nearest-neighbour bonds of the 6x6 periodic square lattice"})
+    ch = open(os.path.join(ref, "example", "heisenberg_chain_40.yaml")).read()
+    n, _ = line_of(ch.splitlines(), r"permutation:")
+    perms = re.findall(r"permutation:\s*\[([^\]]*)\]", ch)
+    pins.append({"id": "example_chain40_tables", "source": f"example/heisenberg_chain_40.yaml:{n}",
+                 "value": {"translation": ints(perms[0]), "parity": ints(perms[1])},
+                 "what": "translation and parity generators of the 40-site chain"})
+
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_pins.json")
     with open(out, "w") as f:
         json.dump({"reference": "twesterhout/spin-ed", "generated_by": "tests/golden/make_pins.py",
@@ -75,4 +95,7 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    where = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPINED_REFERENCE_DIR")
+    if not where:
+        raise SystemExit("usage: make_pins.py REFERENCE_DIR (or set SPINED_REFERENCE_DIR)")
+    main(where)

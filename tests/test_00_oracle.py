@@ -8,7 +8,8 @@ import numpy as np
 import pytest
 
 HEIS = np.array([[1, 0, 0, 0], [0, -1, 2, 0], [0, 2, -1, 0], [0, 0, 0, 1]], dtype=complex)
-REF = "/root/reference"
+# the reference's source tree, when mounted (only for checks that read it)
+REF = os.environ.get("SPINED_REFERENCE_DIR", "")
 
 
 def ring(n, dist=1):
@@ -152,25 +153,36 @@ def test_lanczos_oracle_vs_eigsh(oracle):
     assert res[0] <= 1e-8
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not mounted")
-def test_lattice_tables_match_reference_examples():
-    """The generated 6x6 / chain-40 tables equal the reference's example YAML."""
-    import re
+def test_lattice_tables_match_reference_examples(pins):
+    """The generated 6x6 / chain-40 tables equal the reference's example YAML
+    (example/heisenberg_square_6x6.yaml, example/heisenberg_chain_40.yaml),
+    as recorded in the golden pins."""
     from spined import lattices
+    sq = pins["example_square6_tables"]["value"]
+    assert sq["permutations"] == lattices.square_symmetries(6)
+    assert sq["bonds"] == lattices.square_bonds(6)
+    ch = pins["example_chain40_tables"]["value"]
+    assert ch["translation"] == lattices.chain_translation(40)
+    assert ch["parity"] == lattices.chain_parity(40)
 
-    def ints(block):
-        return [int(v) for v in re.findall(r"-?\d+", block)]
 
-    txt = open(os.path.join(REF, "example", "heisenberg_square_6x6.yaml")).read()
-    perms = re.findall(r"permutation:\s*\[([^\]]*)\]", txt)
-    assert [ints(p) for p in perms] == lattices.square_symmetries(6)
-    sites = re.search(r"sites:\s*\[(.*?)\]\]", txt, re.S).group(1) + "]"
-    pairs = ints(sites)
-    assert [pairs[i:i + 2] for i in range(0, len(pairs), 2)] == lattices.square_bonds(6)
-    txt = open(os.path.join(REF, "example", "heisenberg_chain_40.yaml")).read()
-    perms = re.findall(r"permutation:\s*\[([^\]]*)\]", txt)
-    assert ints(perms[0]) == lattices.chain_translation(40)
-    assert ints(perms[1]) == lattices.chain_parity(40)
+@pytest.mark.skipif(not os.path.isdir(REF), reason="SPINED_REFERENCE_DIR does not name the reference tree")
+def test_pins_regenerate_from_reference(pins, tmp_path):
+    """The committed pins are what make_pins.py extracts from the reference."""
+    import json
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    pins_file = os.path.join(here, "golden", "reference_pins.json")
+    before = open(pins_file).read()
+    try:
+        subprocess.check_call([sys.executable, os.path.join(here, "golden", "make_pins.py"), REF],
+                              stdout=subprocess.DEVNULL)
+        after = json.load(open(pins_file))
+        assert {p["id"]: p for p in after["pins"]} == pins
+    finally:
+        with open(pins_file, "w") as f:
+            f.write(before)
 
 
 @pytest.mark.parametrize("n,w,inv,k", [(12, 6, 1, 0), (12, 6, -1, 6), (14, 5, None, 3), (10, None, 1, 0), (16, 8, -1, 0)])

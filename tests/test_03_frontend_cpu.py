@@ -79,9 +79,13 @@ def test_complex_entries_and_errors():
         CF.loads_config(README_CONFIG.replace("observables: []", ""))
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/example"), reason="reference examples not present")
+REF = os.environ.get("SPINED_REFERENCE_DIR", "")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "example")),
+                    reason="SPINED_REFERENCE_DIR does not name the reference tree")
 def test_reference_examples_parse():
-    files = sorted(glob.glob("/root/reference/example/*.yaml"))
+    files = sorted(glob.glob(os.path.join(REF, "example", "*.yaml")))
     assert files
     for f in files:
         c = CF.read_config(f)
