@@ -518,6 +518,20 @@ static void mv_emit(void* p, uint64_t j, double re, double im) {
   c->acc[1] += re * xi + im * xr;
 }
 
+int or_matvec_rows(const or_operator* op, uint64_t D, const uint64_t* reps, const unsigned* weights,
+                   const double* x, double* y_rows, uint64_t row_begin, uint64_t row_end) {
+  if (row_end > D) row_end = D;
+  if (row_begin > row_end) row_begin = row_end;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (uint64_t i = row_begin; i < row_end; ++i) {
+    mv_ctx c = {x, {0.0, 0.0}};
+    row_elements(op, D, reps, weights, i, mv_emit, &c);
+    y_rows[2 * (i - row_begin)] = c.acc[0];
+    y_rows[2 * (i - row_begin) + 1] = c.acc[1];
+  }
+  return OR_OK;
+}
+
 int or_matvec(const or_operator* op, uint64_t D, const uint64_t* reps, const unsigned* weights,
               const double* x, double* y, uint64_t row_begin, uint64_t row_end) {
   if (row_end > D) row_end = D;

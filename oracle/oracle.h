@@ -98,6 +98,11 @@ void or_operator_destroy(or_operator* op);
 int or_matvec(const or_operator* op, uint64_t D, const uint64_t* reps, const unsigned* weights,
               const double* x, double* y, uint64_t row_begin, uint64_t row_end);
 
+/* Rows [row_begin, row_end) of y = H x into y_rows (interleaved complex,
+ * row_end - row_begin entries); reps/weights/x as for or_matvec. */
+int or_matvec_rows(const or_operator* op, uint64_t D, const uint64_t* reps, const unsigned* weights,
+                   const double* x, double* y_rows, uint64_t row_begin, uint64_t row_end);
+
 /* Explicit matrix in COO form (duplicates summed per row). Call with
  * rows == NULL to get nnz. */
 int or_matrix_coo(const or_operator* op, uint64_t D, const uint64_t* reps, const unsigned* weights,

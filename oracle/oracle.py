@@ -78,6 +78,7 @@ def lib() -> C.CDLL:
         L.or_operator_create.argtypes = [C.POINTER(p), p, u, p, p, p, p]
         L.or_operator_destroy.argtypes = [p]
         L.or_matvec.argtypes = [p, u64, p, p, p, p, u64, u64]
+        L.or_matvec_rows.argtypes = [p, u64, p, p, p, p, u64, u64]
         L.or_matrix_coo.argtypes = [p, u64, p, p, p, p, p, u64, C.POINTER(u64)]
         L.or_row_work.argtypes = [p, p, u64, C.POINTER(u64)]
         L.or_row_work.restype = u64
@@ -180,6 +181,16 @@ class Basis:
         self.reps, self.weights = reps[:D], w[:D]
         return self.reps
 
+    def slice(self, rank_begin: int, rank_end: int) -> tuple[np.ndarray, np.ndarray]:
+        """Representatives and stabiliser orders of the word ranks
+        [rank_begin, rank_end), without replacing the built list."""
+        saved = self.reps, self.weights
+        try:
+            reps = self.build(rank_begin, rank_end)
+            return reps.copy(), self.weights.copy()
+        finally:
+            self.reps, self.weights = saved
+
     def norms(self) -> np.ndarray:
         """||P r|| = sqrt(S / |G|) per representative."""
         return np.sqrt(self.weights.astype(np.float64) / float(self.group_order))
@@ -252,6 +263,23 @@ class Operator:
         lib().or_matvec(self._h, self.dim, _ptr(b.reps), _ptr(b.weights), _ptr(x.view(np.float64)),
                         _ptr(y.view(np.float64)), row_begin, re)
         return y
+
+    def matvec_rows(self, reps: np.ndarray, weights: np.ndarray, x: np.ndarray, row_begin: int,
+                    row_end: int) -> np.ndarray:
+        """Rows [row_begin, row_end) of H x over a representative list given
+        by the caller (sorted, with stabiliser orders): the pull form of
+        src/SpinED/Internal.hs:411-429, index lookups into `reps` included."""
+        reps = np.ascontiguousarray(reps, dtype=np.uint64)
+        weights = np.ascontiguousarray(weights, dtype=np.uint32)
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        D = len(reps)
+        row_end = min(row_end, D)
+        y = np.zeros(max(row_end - row_begin, 1), dtype=np.complex128)
+        st = lib().or_matvec_rows(self._h, D, _ptr(reps), _ptr(weights), _ptr(x.view(np.float64)),
+                                  _ptr(y.view(np.float64)), row_begin, row_end)
+        if st:
+            raise OracleError(st, "matvec_rows")
+        return y[:max(row_end - row_begin, 0)]
 
     def coo(self):
         b = self.basis

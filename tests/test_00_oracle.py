@@ -201,3 +201,17 @@ def test_burnside_square4(oracle):
     gens = [(g, 0) for g in lattices.square_symmetries(4)]
     b = oracle.Basis(16, 8, 1, gens)
     assert sector_dimension(b.group, 16, 8, 1) == 107 == len(b.build())
+
+
+@pytest.mark.parametrize("n", [4, 6, 8, 10, 12, 14])
+def test_bethe_ansatz_matches_dense(oracle, pins, n):
+    """The Bethe-ansatz ring energy (tests/_bethe.py, an exact method that
+    pins the chain workloads on the GPU) equals the oracle's sector matrix
+    ground state; n = 4 is the README's -8."""
+    from _bethe import heisenberg_ring_e0
+    b = oracle.Basis(n, n // 2, None, [])
+    op = oracle.Operator(b, [oracle.Term(HEIS, ring(n))])
+    e0 = np.linalg.eigvalsh(op.dense().real)[0]
+    assert heisenberg_ring_e0(n) == pytest.approx(e0, rel=1e-13, abs=1e-13)
+    if n == 4:
+        assert heisenberg_ring_e0(4) == pytest.approx(pins["readme_ring4_e0"]["value"], abs=1e-13)
