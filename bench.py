@@ -15,10 +15,15 @@ Hamiltonian, and plain FP64 Lanczos from the Philox seed-1234 start vector to
          bytes per launch / its CUDA-event duration against the measured HBM
          copy bandwidth
   cpu_baseline  the CPU restatement (oracle/) on the host cores, on bounded
-         samples of the same workload, extrapolated to one solve
+         samples of the same workload (complete rows with index lookups),
+         scaled to one solve and flagged as extrapolated
+  chain24_cpu_vs_gpu  config 1 (chain N=24) solved completely on the CPU
+         restatement and on the GPU, both measured end to end
 
 `--impl reference` times the reference's CPU path (the oracle restatement;
-the reference itself cannot be built without GHC) on the same workload.
+the reference itself cannot be built without GHC) on the same workload: its
+steps together do one complete basis build and one complete matvec, and its
+value is the solve modelled from those two measured components.
 Multi-GPU runs are replicas (one independent solve per rank).
 """
 from __future__ import annotations
@@ -41,9 +46,13 @@ METRIC = "time-to-ground-state (resid<=1e-8) vs plain FP64 GPU Lanczos; matvec H
 # seed-1234 Philox start vector (the CPU restatement runs the same algorithm
 # from the same start vector and needs the same number of matvecs).
 SQUARE6_STEPS = 57  # 56 Lanczos steps + the final residual check
+# the same count per workload (chain 24: 50 steps + the residual check)
+SOLVE_MATVECS = {"square6": SQUARE6_STEPS, "chain24": 51}
 # DRAM bytes (read + write) of one k_spmv launch on the 6x6 workload, from one
-# ncu capture (profiles/k_spmv_square6_traffic.md): 4 935 736 320 read +
-# 124 209 920 written.
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
+#       -k regex:k_spmv -s 40 -c 1 python bench.py --once
+# 4 935 736 320 read + 124 209 920 written.
 SPMV_TRAFFIC_BYTES = 4935736320 + 124209920
 
 
@@ -223,9 +232,11 @@ def gpu_arm(args, rank, world, dist):
     spmv_ms = e0.elapsed_time(e1) / reps_n
     E_tot = op.stream_elements
     s_bytes = 8
-    # algorithmic bytes of one streamed matvec: entries, diagonal + row class,
-    # x_i, the gathered x_j (one per element) and y
-    alg = E_tot * 4 + D * 9 + D * s_bytes + E_tot * s_bytes + D * s_bytes
+    # algorithmic bytes of one matvec (k = 1): representatives D*8, x_i D*s,
+    # the gathered x_j E_tot*s, y D*s
+    alg = D * 8 + D * s_bytes + E_tot * s_bytes + D * s_bytes
+    # what the stream form must move at least: its entries (4 B each), the
+    # diagonal and row class (9 B per row), x and y once
     compulsory = E_tot * 4 + D * 9 + 2 * D * s_bytes
     peak, peak_kind = peaks()
     achieved = alg / (spmv_ms * 1e-3) / 1e9
@@ -235,7 +246,7 @@ def gpu_arm(args, rank, world, dist):
         "spmv_ms": spmv_ms, "alg_bytes": alg, "compulsory_bytes": compulsory, "achieved": achieved,
         "peak": peak, "peak_kind": peak_kind, "stream_bytes": op.stream_bytes,
         "E0": float(res.eigenvalues[0]), "residual": float(res.residuals[0]),
-        "steps_lanczos": res.iterations,
+        "steps_lanczos": res.iterations, "basis": built.basis,
     }
 
 
@@ -361,49 +372,122 @@ def batched_arm():
 
 # ------------------------------------------------------------------ CPU --
 
-def cpu_sample(workload: str, budget_s: float = 8.0):
-    """Times the CPU restatement on bounded samples of the workload and
-    extrapolates one solve: basis scan + SQUARE6_STEPS on-the-fly matvecs."""
+def _oracle_workload(workload: str):
     import numpy as np
     import oracle as O
     m = workload_model(workload)
     b = O.Basis(m.number_spins, m.hamming_weight, m.spin_inversion, m.symmetries)
+    op = O.Operator(b, [O.Term(np.array(a, dtype=complex), np.array(s)) for a, s in m.terms], build=False)
+    return O, m, b, op
+
+
+def cpu_sample(workload: str, reps=None, weights=None, budget_s: float = 8.0):
+    """The CPU restatement on bounded samples of the workload, scaled to one
+    solve (basis + SQUARE6_STEPS matvecs): the basis scan on a stratified
+    sample of the word space (each of 16 equal rank strata timed on a
+    sub-slice and scaled by its own size), and complete pull-form rows, index
+    lookups into the full representative list included, on row chunks
+    spread over the sector. `reps`/`weights` is that list (the GPU's, which
+    the parity tests check against the oracle); without it the rows are
+    drawn from the sampled slices and only generation + canonicalisation is
+    timed."""
+    import numpy as np
+    O, m, b, op = _oracle_workload(workload)
     space = b.space_size()
-    # Basis: 8 slices spread over the word space.
-    slices, per = 8, 1 << 16
+    strata, per = 16, 1 << 14
     while True:
-        t0 = time.perf_counter()
-        reps = []
-        for k in range(slices):
-            start = (space // slices) * k
-            reps.append(b.build(start, start + per))
-        tb = time.perf_counter() - t0
-        if tb > budget_s / 2 or per >= space // slices:
+        t_basis, found, t_spent = 0.0, [], 0.0
+        for k in range(strata):
+            lo = space * k // strata
+            hi = space * (k + 1) // strata
+            t0 = time.perf_counter()
+            r, _ = b.slice(lo, min(hi, lo + per))
+            dt = time.perf_counter() - t0
+            t_spent += dt
+            t_basis += dt * (hi - lo) / min(hi - lo, per)
+            found.append(r)
+        if t_spent > budget_s / 2 or per * strata >= space:
             break
         per *= 4
-    scanned = slices * per
-    t_basis = tb * space / scanned
-    D_est = sum(len(r) for r in reps) * space / scanned
-    rows = np.concatenate(reps)
-    op = O.Operator(b, [O.Term(np.array(a, dtype=complex), np.array(s)) for a, s in m.terms], build=False)
-    n = min(len(rows), 2000)
-    while True:
+    sample_b = f"basis: {strata} strata x {per} words of {space}"
+    rows_t, n_rows, lookups = 0.0, 0, reps is not None
+    if lookups:
+        D = len(reps)
+        x = np.random.default_rng(0).uniform(-1, 1, D).astype(np.complex128)
+        chunk, n_chunks = 256, 16
+        while True:
+            starts = np.linspace(0, max(0, D - chunk), n_chunks).astype(np.int64)
+            t0 = time.perf_counter()
+            for a in starts:
+                op.matvec_rows(reps, weights, x, int(a), int(a) + chunk)
+            rows_t = time.perf_counter() - t0
+            n_rows = n_chunks * min(chunk, D)
+            if rows_t > budget_s / 2 or n_rows >= D:
+                break
+            chunk *= 4
+        t_matvec = rows_t * D / n_rows
+        sample_m = f"matvec: {n_rows} complete rows (index lookups included) in {n_chunks} chunks"
+    else:
+        rows = np.concatenate(found)
+        D = SQUARE6_D if workload == "square6" else len(rows)
+        n = min(len(rows), 2000)
         t0 = time.perf_counter()
-        ne = op.row_work(rows[:n])
-        tm = time.perf_counter() - t0
-        if tm > budget_s / 2 or n >= len(rows):
-            break
-        n = min(len(rows), n * 4)
-    D = 15_804_956 if workload == "square6" else D_est
-    t_matvec = tm * D / n
-    steps = SQUARE6_STEPS
-    total = t_basis + steps * t_matvec
-    return {
-        "value": total, "cores": O.num_threads(), "t_basis_s": t_basis, "t_matvec_s": t_matvec,
-        "sample": (f"basis: {slices} slices x {per} words of {space} (fraction {scanned / space:.2e}); "
-                   f"matvec: element generation + canonicalisation of {n} sampled rows "
-                   f"({ne} elements; index lookups excluded); solve = basis + {steps} matvecs"),
-    }
+        op.row_work(rows[:n])
+        t_matvec = (time.perf_counter() - t0) * D / max(n, 1)
+        sample_m = f"matvec: element generation + canonicalisation of {n} rows (no index lookups)"
+    steps = SOLVE_MATVECS.get(workload, SQUARE6_STEPS)
+    return {"value": t_basis + steps * t_matvec, "cores": O.num_threads(), "t_basis_s": t_basis,
+            "t_matvec_s": t_matvec,
+            "sample": f"{sample_b}; {sample_m}; scaled to one solve = basis + {steps} matvecs"}
+
+
+def cpu_chain24_solve():
+    """Config 1 end to end on the CPU restatement, all of it measured: the
+    chain-24 basis (D = 28 968), then plain FP64 Lanczos with full
+    reorthogonalisation from the seed-1234 Philox start to ||H psi - E psi||
+    <= 1e-8, every matvec the oracle's pull form with index lookups; plus
+    scipy's eigsh on the oracle's explicit sector matrix as a cross-check."""
+    import numpy as np
+    import scipy.sparse.linalg as sla
+    O, m, b, op = _oracle_workload("chain24")
+    t0 = time.perf_counter()
+    b.build()
+    t_basis = time.perf_counter() - t0
+    D = len(b.reps)
+    t0 = time.perf_counter()
+    ev, _, res, it = O.lanczos_ground_state(lambda v: op.matvec(v).real, O.start_vector(1234, D))
+    t_lanczos = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    A = op.sparse()
+    e_sp = float(sla.eigsh(A, k=1, which="SA", tol=1e-12)[0][0])
+    t_eigsh = time.perf_counter() - t0
+    return {"D": D, "cores": O.num_threads(), "basis_s": t_basis, "lanczos_s": t_lanczos,
+            "solve_s": t_basis + t_lanczos, "E0": float(ev[0]), "residual": float(res[0]), "lanczos_steps": it,
+            "scipy_eigsh": {"E0": e_sp, "seconds": t_eigsh}}
+
+
+def gpu_chain24_solve(reps_n: int = 5):
+    """The same config-1 solve through the C ABI from host arrays (lattice
+    tables copied in, representatives and eigenvector copied out), wall
+    clock per complete solve, median of `reps_n`."""
+    import numpy as np
+    import torch
+    from spined import internal as I
+    from spined.model import build_model
+    m = workload_model("chain24")
+    times, r = [], None
+    for k in range(reps_n + 2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b = build_model(m)
+        reps = I.basis_get_states(b.basis)
+        r = I.eigh(b.hamiltonian, tol=1e-8, seed=1234)
+        torch.cuda.synchronize()
+        if k >= 2:
+            times.append(time.perf_counter() - t0)
+        del b, reps
+    return {"solve_s": statistics.median(times), "E0": float(r.eigenvalues[0]), "residual": float(r.residuals[0]),
+            "lanczos_steps": r.iterations}
 
 
 # the 6x6 workload's fixed sizes (sector dimension by Burnside's lemma, stored
@@ -412,6 +496,7 @@ def cpu_sample(workload: str, budget_s: float = 8.0):
 SQUARE6_D = 15_804_956
 SQUARE6_ELEMENTS = 585_262_534
 SQUARE6_STREAM_BYTES = 2.73e9
+CHAIN24_D = 28_968
 
 
 def workload_config(workload, precision, D, E_tot, stream_bytes, world):
@@ -421,24 +506,74 @@ def workload_config(workload, precision, D, E_tot, stream_bytes, world):
             "l2": "working set (stream form %.2f GB) exceeds L2" % (stream_bytes / 1e9)}
 
 
+def _reference_config(workload, world):
+    if workload == "square6":
+        return workload_config("square6", "fp64", SQUARE6_D, SQUARE6_ELEMENTS, SQUARE6_STREAM_BYTES, world)
+    return {"workload": workload}
+
+
 def reference_arm(args, rank):
+    """The reference's CPU path (the oracle restatement on all host cores)
+    doing COMPLETE work: the K steps together build the whole basis (rank
+    slices of the word space, the first half of the steps) and then apply one
+    whole matvec, index lookups included (row chunks, the second half). Each
+    step's wall time is measured; their sum is one basis build plus one
+    matvec. A complete Lanczos solve needs SQUARE6_STEPS matvecs and does not
+    fit in a bench run (about an hour on 16 cores), so `value` is the model
+    basis + SQUARE6_STEPS x matvec built from the two measured components and
+    the line says so ("extrapolated": true)."""
     if rank != 0:
         return
+    import numpy as np
     t_all = time.perf_counter()
-    samples = []
-    for _ in range(args.warmup):
-        cpu_sample(args.workload, budget_s=args.cpu_budget)
-    for _ in range(args.steps):
-        samples.append(cpu_sample(args.workload, budget_s=args.cpu_budget))
-    v = statistics.median(s["value"] for s in samples)
-    s0 = samples[0]
+    O, m, b, op = _oracle_workload(args.workload)
+    space = b.space_size()
+    K = max(1, args.steps)
+    kb = max(1, K // 2)                 # steps that scan the basis
+    km = max(1, K - kb)                 # steps that apply the matvec
+    step_s, parts_r, parts_w = [], [], []
+    for j in range(kb):
+        lo, hi = space * j // kb, space * (j + 1) // kb
+        t0 = time.perf_counter()
+        r, w = b.slice(lo, hi)
+        parts_r.append(r)
+        parts_w.append(w)
+        step_s.append(time.perf_counter() - t0)
+    reps = np.concatenate(parts_r)
+    weights = np.concatenate(parts_w)
+    del parts_r, parts_w
+    t_basis = sum(step_s)
+    D = len(reps)
+    x = O.start_vector(1234, D).astype(np.complex128)
+    mv = []
+    for j in range(km):
+        a, bnd = D * j // km, D * (j + 1) // km
+        t0 = time.perf_counter()
+        op.matvec_rows(reps, weights, x, a, bnd)
+        mv.append(time.perf_counter() - t0)
+    if K == 1:  # one step did both halves
+        step_s = [t_basis + sum(mv)]
+    else:
+        step_s += mv
+    t_matvec = sum(mv)
+    n_mv = SOLVE_MATVECS.get(args.workload, SQUARE6_STEPS)
+    v = t_basis + n_mv * t_matvec
+    measured = sum(step_s)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": measured / K * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (lattice generated in code)",
-        "config": workload_config(args.workload, "fp64", SQUARE6_D, SQUARE6_ELEMENTS, SQUARE6_STREAM_BYTES, args.gpus)
-                  if args.workload == "square6" else {"workload": args.workload},
-        "cpu_baseline": {"value": v, "unit": "s", "cores": s0["cores"], "kind": "port", "sample": s0["sample"]},
+        "config": _reference_config(args.workload, args.gpus),
+        "extrapolated": True,
+        "measured": {"basis_build_s": t_basis, "matvec_s": t_matvec, "D": D, "cores": O.num_threads(),
+                     "steps_s": step_s, "total_s": measured,
+                     "what": "one complete basis build and one complete pull-form matvec (index lookups "
+                             "included) on the CPU restatement; each step a slice of that work"},
+        "model": f"value = basis_build_s + {n_mv} x matvec_s (the matvecs plain FP64 Lanczos takes "
+                 f"on this workload); ms_per_step = total_s / steps (the work actually done)",
+        "cpu_baseline": {"value": v, "unit": "s", "cores": O.num_threads(), "kind": "port",
+                         "sample": f"complete basis build ({space} words) + one complete matvec ({D} rows), "
+                                   f"scaled to basis + {n_mv} matvecs"},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU restatement (oracle/), not the reference binary: GHC and the unpinned "
                 "lattice-symmetries/PRIMME sources are unavailable",
@@ -457,7 +592,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="square6")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--cpu-budget", type=float, default=6.0, help="seconds of CPU work per baseline sample")
+    ap.add_argument("--cpu-budget", type=float, default=16.0, help="seconds of CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the forms and batched measurements")
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
@@ -520,11 +655,26 @@ def main():
         import torch
         extras["forms"] = forms_arm(torch.cuda.current_stream())
         extras["batched"] = batched_arm()
+    if rank == 0 and not args.no_extras and world == 1:
+        gpu24 = gpu_chain24_solve()
+        cpu24 = cpu_chain24_solve()
+        extras["chain24_cpu_vs_gpu"] = {
+            "workload": "chain N=24, w=12, k=0, P+, Z+ (D=28968): basis + plain FP64 Lanczos to resid<=1e-8, "
+                        "seed 1234, both complete and measured",
+            "gpu": gpu24, "cpu": cpu24, "cpu_over_gpu": cpu24["solve_s"] / gpu24["solve_s"],
+            "eigenvalue_abs_diff": abs(cpu24["E0"] - gpu24["E0"])}
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and world == 1:
-            c = cpu_sample(args.workload, budget_s=args.cpu_budget)
-            cpu = {"value": c["value"], "unit": "s", "cores": c["cores"], "kind": "port", "sample": c["sample"]}
+            from spined import internal as I
+            import numpy as np
+            reps = I.basis_get_states(r["basis"])
+            G = 2 * I.get_group_size(r["basis"].group) if r["basis"].spin_inversion else I.get_group_size(r["basis"].group)
+            norms = r["basis"].norms()
+            weights = np.rint(norms * norms * G).astype(np.uint32)
+            c = cpu_sample(args.workload, reps, weights, budget_s=args.cpu_budget)
+            cpu = {"value": c["value"], "unit": "s", "cores": c["cores"], "kind": "port", "sample": c["sample"],
+                   "extrapolated": True, "basis_s": c["t_basis_s"], "matvec_s": c["t_matvec_s"]}
         ph = r["phases"][-1]
         line = {
             "metric": METRIC, "value": r["ms"] / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -538,7 +688,8 @@ def main():
                          "frac": r["achieved"] / r["peak"],
                          "traffic": SPMV_TRAFFIC_BYTES if args.workload == "square6" else None,
                          "kernel": "k_spmv (streamed SELL-32 SpMV, FP64)", "spmv_ms": r["spmv_ms"],
-                         "alg_bytes": r["alg_bytes"], "compulsory_bytes": r["compulsory_bytes"],
+                         "alg_bytes": r["alg_bytes"], "alg_bytes_formula": "D*8 + D*8 + E_tot*8 + D*8",
+                         "compulsory_bytes": r["compulsory_bytes"],
                          "matvec_gstates_per_s": r["D"] / (r["spmv_ms"] * 1e-3) / 1e9,
                          "peak_kind": r["peak_kind"]},
             "clocks": r["clocks"],

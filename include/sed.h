@@ -19,6 +19,12 @@
  *  - x/y block arguments may be host memory (pageable or pinned) or device
  *    memory of the current device; the library detects which. Blocks are
  *    column-major with the given column strides (Internal.hs:411-429).
+ *  - Calls that take caller buffers and return when done (ls_operator_matmat,
+ *    ls_operator_expectation, ls_build_unsafe, sed_eigh, sed_eigh_batched,
+ *    sed_mlp_*) first wait for all work queued on the device when any of
+ *    those buffers is device memory, so a buffer the caller has just written
+ *    on a stream of its own is complete before libsed reads it. Calls that
+ *    take a stream argument order their work on that stream instead.
  *  - dtype codes: 0 = float32, 1 = float64, 2 = complex64, 3 = complex128
  *    (Internal.hs:404-409).
  *  - A permutation p acts on a spin configuration x as y_i = x_{p[i]}; a

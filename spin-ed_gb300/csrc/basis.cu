@@ -519,6 +519,10 @@ int ls_build_unsafe(ls_spin_basis* basis, uint64_t size, uint64_t const represen
   if (!basis || (size && !representatives)) return fail(LS_INVALID_ARGUMENT, "ls_build_unsafe: NULL argument");
   std::lock_guard<std::mutex> lock(basis->d->mu);
   try {
+    {
+      ScopedDevice dev(basis->d->device);
+      if (int st = wait_for_caller({representatives})) return st;
+    }
     return build_impl(*basis->d, representatives, size);
   } catch (std::exception const& e) {
     return fail(LS_SYSTEM_ERROR, e.what());

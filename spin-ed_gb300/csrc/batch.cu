@@ -831,6 +831,9 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
       if (int st = operator_record_stream(op, op.cuda_stream)) return st;
   }
   for (unsigned i = 0; i < count; ++i) SED_TRY_CUDA(cudaStreamSynchronize(od[i]->cuda_stream));
+  if (eigenvectors)
+    for (unsigned i = 0; i < count; ++i)
+      if (int st = wait_for_caller({eigenvectors[i]})) return st;
   auto t_setup = std::chrono::steady_clock::now();
   cudaStream_t stream = nullptr;
   SED_TRY_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));

@@ -962,6 +962,7 @@ int sed_mlp_uses_tensor_cores(sed_mlp const* m) { return m && tc_eligible(m->d) 
 int sed_mlp_get_params(sed_mlp const* m, float* out) {
   if (!m || !out) return fail(LS_INVALID_ARGUMENT, "sed_mlp_get_params: NULL argument");
   ScopedDevice dev(m->d.device);
+  if (int st = wait_for_caller({out})) return st;
   SED_TRY_CUDA(cudaMemcpy(out, m->d.p.ptr, m->d.n_params * 4, cudaMemcpyDefault));
   return LS_SUCCESS;
 }
@@ -970,6 +971,7 @@ int sed_mlp_set_params(sed_mlp* m, float const* in) {
   if (!m || !in) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_params: NULL argument");
   MlpData& d = m->d;
   ScopedDevice dev(d.device);
+  if (int st = wait_for_caller({in})) return st;
   SED_TRY_CUDA(cudaMemcpy(d.p.ptr, in, d.n_params * 4, cudaMemcpyDefault));
   if (int st = refresh_bf16(d)) return st;
   SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
@@ -980,6 +982,7 @@ int sed_mlp_forward(sed_mlp* m, uint64_t const* states, uint64_t n, float* out) 
   if (!m || (n && (!states || !out))) return fail(LS_INVALID_ARGUMENT, "sed_mlp_forward: NULL argument");
   MlpData& d = m->d;
   ScopedDevice dev(d.device);
+  if (int st = wait_for_caller({states, out})) return st;
   uint64_t const chunk = 1u << 18;
   DeviceBuffer sbuf;
   if (n)
@@ -1006,6 +1009,7 @@ int sed_mlp_loss_grad(sed_mlp* m, uint64_t const* states, float const* t_abs, fl
   if (n > (1u << 20)) return fail(LS_INVALID_ARGUMENT, "sed_mlp_loss_grad: at most 2^20 samples per call");
   MlpData& d = m->d;
   ScopedDevice dev(d.device);
+  if (int st = wait_for_caller({states, t_abs, t_sign, grads})) return st;
   DeviceBuffer sb, ta, ts;
   if (int st = stage(sb, states, n * 8, d.stream)) return st;
   if (int st = stage(ta, t_abs, n * 4, d.stream)) return st;
@@ -1024,6 +1028,7 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
   if (batch > (1u << 20)) return fail(LS_INVALID_ARGUMENT, "sed_mlp_train: batch must be <= 2^20");
   MlpData& d = m->d;
   ScopedDevice dev(d.device);
+  if (int st = wait_for_caller({states, t_abs, t_sign})) return st;
   // the data set is shuffled on the host once per epoch (an index permutation
   // from mt19937_64(seed)) and uploaded; batches are contiguous slices of it
   std::vector<uint64_t> hs(n);
@@ -1083,6 +1088,7 @@ int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64_t n, ui
   if (b.D == 0) return fail(LS_INVALID_ARGUMENT, "sed_mlp_sample: empty basis");
   if (n == 0) return LS_SUCCESS;
   ScopedDevice dev(b.device);
+  if (int st = wait_for_caller({psi, states, t_abs, t_sign})) return st;
   cudaStream_t s = nullptr;
   SED_TRY_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   struct StreamGuard {
@@ -1136,6 +1142,7 @@ int sed_mlp_start_vector(sed_mlp* m, ls_spin_basis const* basis, double* out) {
   if (b.n != d.n_in) return fail(LS_DIMENSION_MISMATCH, "sed_mlp_start_vector: network inputs != number of spins");
   if (b.D == 0) return LS_SUCCESS;
   ScopedDevice dev(d.device);
+  if (int st = wait_for_caller({out})) return st;
   uint64_t const D = b.D, chunk = 1u << 18;
   DeviceBuffer amp, part, vout;
   if (int st = amp.allocate(D * 8)) return st;  // (a, s) pairs

@@ -718,6 +718,15 @@ bool is_device_pointer(void const* p) {
 
 }  // namespace
 
+int wait_for_caller(std::initializer_list<void const*> buffers) {
+  for (void const* p : buffers)
+    if (p && is_device_pointer(p)) {
+      SED_TRY_CUDA(cudaDeviceSynchronize());
+      return LS_SUCCESS;
+    }
+  return LS_SUCCESS;
+}
+
 OperatorData::~OperatorData() {
   tables.reset();
   if (cuda_stream) {
@@ -1374,6 +1383,7 @@ int host_blocks(OperatorData& op, int dtype, uint64_t size, uint64_t block, void
   BasisData& b = *op.basis;
   size_t const es = (size_t)elem_size(dtype);
   bool const x_dev = is_device_pointer(x), y_dev = is_device_pointer(y);
+  if (x_dev || y_dev) SED_TRY_CUDA(cudaDeviceSynchronize());  // the caller's writes of x, reads of y
   cudaStream_t s = op.cuda_stream;
   DeviceBuffer xb, yb;
   void const* xd = x;
@@ -1507,6 +1517,7 @@ int ls_operator_expectation(ls_operator const* op, int dtype, uint64_t size, uin
     if (int st = operator_ensure_ready(d)) return st;
     size_t const es = (size_t)elem_size(dtype);
     cudaStream_t s = d.cuda_stream;
+    if (int st = wait_for_caller({x})) return st;
     DeviceBuffer xb, yb, part;
     if (int st = xb.allocate(size * block_size * es)) return st;
     if (int st = yb.allocate(size * block_size * es)) return st;

@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <memory>
+#include <initializer_list>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -215,6 +216,12 @@ struct OperatorData {
 };
 
 int operator_upload_terms(OperatorData& op);
+// Entry points that take caller buffers and run on a libsed stream call this
+// first: when any of the pointers is device memory, it waits for all work
+// already queued on the device, since the caller may have written the buffer
+// (or may still be reading it) on a stream of its own. Host pointers need no
+// wait. Returns a status.
+int wait_for_caller(std::initializer_list<void const*> buffers);
 int operator_record_stream(OperatorData& op, cudaStream_t stream);
 int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void const* x,
                           uint64_t ldx, void* y, uint64_t ldy, cudaStream_t stream, int form);
