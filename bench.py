@@ -598,9 +598,10 @@ def main():
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
     ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
     ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
-    ap.add_argument("--profile-case", default=None, choices=["mlp", "batch16"],
+    ap.add_argument("--profile-case", default=None, choices=["mlp", "batch16", "spmv"],
                     help="one small run of a single kernel family, for profilers: the tensor-core MLP "
-                         "inference over 2^20 random 36-spin states, or a 16-chain batched solve")
+                         "inference over 2^20 random 36-spin states, a 16-chain batched solve, or 10 "
+                         "matvecs of the 6x6 stream form (about 3.5 GB on the device)")
     args = ap.parse_args()
     args.precision_code = 0 if args.precision == "fp64" else 1
     rank = int(os.environ.get("RANK", "0"))
@@ -625,6 +626,21 @@ def main():
         out = net.forward(st)
         print(json.dumps({"case": "mlp", "states": len(st), "tensor_cores": net.uses_tensor_cores,
                           "max_abs": float(np.abs(out).max())}))
+        return
+    if args.profile_case == "spmv":
+        from spined import internal as I, _lib as L
+        from spined.model import build_model
+        b = build_model(workload_model("square6"))
+        op = b.hamiltonian
+        op.prepare(L.SED_FORM_STREAM)
+        L.load().sed_release_workspace()
+        D = I.get_number_states(b.basis)
+        x = torch.randn(D, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(10):
+            I.inplace_apply(op, x, y)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": "spmv", "D": D, "elements": op.stream_elements, "y_norm": float(y.norm())}))
         return
     if args.profile_case == "batch16":
         from spined import internal as I, lattices

@@ -1217,6 +1217,7 @@ int sed_eigh(ls_operator const* op, int dtype, sed_eigh_options const* opts, dou
     ScopedDevice dev(d.basis->device);
     if (int st = operator_ensure_ready(d)) return st;
     if (int st = wait_for_caller({o.start == SED_START_GIVEN ? o.start_vectors : nullptr, eigenvectors})) return st;
+    if (int st = fix_wait(d)) return st;  // matvecs still queued on callers' streams share the workspace
     if (dtype >= 2 || !d.is_real) return solve<double2>(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);
     if (o.max_basis > 0 && o.max_basis <= 32 && o.block_size <= 1)
       return solve_thick(d, dtype, o, eigenvalues, eigenvectors, ldv, residuals, info);

@@ -306,6 +306,251 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// ------------------------------------------------ fixed-point matvec ----
+// (the mathematics is at FixView in operator_impl.cuh)
+
+// Largest |x_j| of column blockIdx.y as a bit pattern (for finite
+// non-negative doubles the integer order is the numeric order; NaN and
+// infinity patterns are larger than every finite one). `max_bits` must be
+// zero on entry.
+__global__ void __launch_bounds__(kBlock) k_fix_max(double const* __restrict__ x, uint64_t ldx, uint64_t D,
+                                                    unsigned long long* __restrict__ max_bits, Indirect ind) {
+  __shared__ unsigned long long red[kBlock / 32];
+  if (ind.stop && *ind.stop) return;
+  if (ind.k) x += (uint64_t)*ind.k * ind.ld;
+  x += (uint64_t)blockIdx.y * ldx;
+  unsigned long long m = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (uint64_t)gridDim.x * blockDim.x)
+    m = max(m, (unsigned long long)__double_as_longlong(x[i]) & 0x7FFFFFFFFFFFFFFFull);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (unsigned w = 1; w < kBlock / 32; ++w) m = max(m, red[w]);
+    atomicMax(max_bits + blockIdx.y, m);
+  }
+}
+
+// u_j = round(sqrt(S_j) x_j 2^F) for column blockIdx.y; block 0 stores F.
+// The class of row j comes from the stream form's row_class, or from the
+// stabiliser orders when there is no stream form.
+__global__ void __launch_bounds__(kBlock) k_fix_convert(double const* __restrict__ x, uint64_t ldx, uint64_t D,
+                                                        uint8_t const* __restrict__ row_class,
+                                                        uint32_t const* __restrict__ weights, CodeView C, FixView fv,
+                                                        unsigned long long const* __restrict__ max_bits,
+                                                        int64_t* __restrict__ F_out, int64_t* __restrict__ u,
+                                                        uint64_t ldu, Indirect ind) {
+  __shared__ double fac[kFixMaxClasses];
+  if (ind.stop && *ind.stop) return;
+  if (ind.k) x += (uint64_t)*ind.k * ind.ld;
+  x += (uint64_t)blockIdx.y * ldx;
+  u += (uint64_t)blockIdx.y * ldu;
+  int64_t const F = fix_exponent(max_bits[blockIdx.y], fv.bound);
+  if (blockIdx.x == 0 && threadIdx.x == 0) F_out[blockIdx.y] = F;
+  // x 2^F sqrt(S) as (x 2^F1) (sqrt(S) 2^F2): F1 = 0 unless 2^F is not a
+  // normal double (vectors whose largest entry is below about 1e-290 or
+  // above about 1e290)
+  int64_t const F1 = (F == kFixBad || (F >= -1000 && F <= 1000)) ? 0 : F / 2;
+  double const p1 = fix_pow2(F1);
+  double const p2 = F == kFixBad ? 0.0 : fix_pow2(F - F1);
+  for (uint32_t c = threadIdx.x; c < fv.n_div; c += blockDim.x) fac[c] = fv.sqrt_s[c] * p2;
+  __syncthreads();
+  if (F1 == 0) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (uint64_t)gridDim.x * blockDim.x) {
+      uint32_t const cls = row_class ? (uint32_t)row_class[i] : divisor_class(weights[i], C);
+      u[i] = F == kFixBad ? 0 : fix_round(x[i] * fac[cls]);
+    }
+  } else {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (uint64_t)gridDim.x * blockDim.x) {
+      uint32_t const cls = row_class ? (uint32_t)row_class[i] : divisor_class(weights[i], C);
+      u[i] = fix_round((x[i] * p1) * fac[cls]);
+    }
+  }
+}
+
+// Adds +-g to the accumulator of value index t >> 1 (sign t & 1).
+template <int NV>
+__device__ __forceinline__ void fix_add(int64_t (&acc)[NV], uint32_t t, int64_t g) {
+  int64_t const v = (t & 1u) ? -g : g;
+  if constexpr (NV == 1) {
+    acc[0] += v;
+  } else {
+    uint32_t const q = t >> 1;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (q == (uint32_t)k) acc[k] += v;
+  }
+}
+
+// The row's epilogue, shared by every fixed-point kernel so that all of them
+// round identically: y_i = d_i x_i + f_i sum_v c_v (acc_v 2^-F).
+template <int NV>
+__device__ __forceinline__ double fix_row(int64_t const (&acc)[NV], FixView const& fv, int64_t F, double dg,
+                                          double xi, double f) {
+  if (F == kFixBad) return __longlong_as_double(0x7FF8000000000000ll);  // NaN in x gives NaN out
+  double sum = __dmul_rn(fv.c[0], fix_ldexp(__ll2double_rn(acc[0]), -F));
+#pragma unroll
+  for (int k = 1; k < NV; ++k) sum = __fma_rn(fv.c[k], fix_ldexp(__ll2double_rn(acc[k]), -F), sum);
+  return __dadd_rn(__dmul_rn(dg, xi), __dmul_rn(f, sum));
+}
+
+// Streamed SpMV over SELL-32 slices in fixed point (real operators). Four
+// entries per step: their loads, then their gathers, are issued back to back
+// (a padding slot gathers nothing and adds zero). Indirect (Krylov) mode as
+// in k_spmv.
+template <bool Packed, int NV>
+__global__ void __launch_bounds__(kBlock) k_spmv_fix(StreamView S, FixView fv, uint64_t D,
+                                                     double const* __restrict__ x, int64_t const* __restrict__ u,
+                                                     int64_t const* __restrict__ F_in, double* __restrict__ y,
+                                                     Indirect ind) {
+  extern __shared__ uint8_t code8[];
+  __shared__ double red[kBlock / 32];
+  if (ind.stop && *ind.stop) return;  // uniform across the grid
+  if (ind.k) {
+    uint64_t const k = *ind.k;
+    x += k * ind.ld;
+    y += (k + 1) * ind.ld;
+  }
+  for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
+  __syncthreads();
+  int64_t const F = F_in[0];
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  double part = 0.0;
+  if ((s << 5) < D) {
+    uint32_t const lane = threadIdx.x & 31;
+    uint64_t const base = S.slice_ptr[s];
+    uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
+    uint32_t const col_mask = Packed ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
+    int64_t acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0;
+    uint32_t const* ent = S.entries + base + lane;
+    constexpr uint32_t U = 4;
+    uint32_t e = 0;
+    for (; e + U <= width; e += U) {
+      uint32_t v[U];
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) v[q] = __ldcs(ent + (uint64_t)(e + q) * 32);
+      int64_t g[U];
+      uint32_t t[U];
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) {
+        g[q] = 0;
+        t[q] = 0;
+        if (v[q] != kNull) {
+          uint32_t const code =
+              Packed ? (v[q] >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)(e + q) * 32);
+          g[q] = u[v[q] & col_mask];
+          t[q] = code8[code];
+        }
+      }
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) fix_add<NV>(acc, t[q], g[q]);
+    }
+    for (; e < width; ++e) {
+      uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
+      if (v != kNull) {
+        uint32_t const code = Packed ? (v >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)e * 32);
+        fix_add<NV>(acc, code8[code], u[v & col_mask]);
+      }
+    }
+    if (i < D) {
+      double const xi = x[i];
+      double const yi = fix_row<NV>(acc, fv, F, static_cast<double const*>(S.diag)[i], xi,
+                                    S.inv_sqrt_s[S.row_class[i]]);
+      y[i] = yi;
+      part = xi * yi;
+    }
+  }
+  if (ind.partial) {
+    double const tot = block_sum(part, red);
+    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
+  }
+}
+
+// Block form in fixed point: K columns, u column c at u + c * D, F_in[c].
+template <bool Packed, int NV, int K>
+__global__ void __launch_bounds__(kBlock) k_spmv_block_fix(StreamView S, FixView fv, uint64_t D,
+                                                           double const* __restrict__ x, uint64_t ldx,
+                                                           int64_t const* __restrict__ u,
+                                                           int64_t const* __restrict__ F_in, double* __restrict__ y,
+                                                           uint64_t ldy) {
+  extern __shared__ uint8_t code8[];
+  for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
+  __syncthreads();
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  if ((s << 5) >= D) return;
+  uint32_t const lane = threadIdx.x & 31;
+  uint64_t const base = S.slice_ptr[s];
+  uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
+  uint32_t const col_mask = Packed ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
+  int64_t acc[K][NV];
+#pragma unroll
+  for (int c = 0; c < K; ++c)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[c][k] = 0;
+  uint32_t const* ent = S.entries + base + lane;
+  for (uint32_t e = 0; e < width; ++e) {
+    uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
+    if (v != kNull) {
+      uint32_t const col = v & col_mask;
+      uint32_t const code = Packed ? (v >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)e * 32);
+      uint32_t const t = code8[code];
+#pragma unroll
+      for (int c = 0; c < K; ++c) fix_add<NV>(acc[c], t, u[(uint64_t)c * D + col]);
+    }
+  }
+  if (i < D) {
+    double const f = S.inv_sqrt_s[S.row_class[i]];
+    double const dg = static_cast<double const*>(S.diag)[i];
+#pragma unroll
+    for (int c = 0; c < K; ++c) y[(uint64_t)c * ldy + i] = fix_row<NV>(acc[c], fv, F_in[c], dg, x[(uint64_t)c * ldx + i], f);
+  }
+}
+
+// On-the-fly matvec in fixed point: the same integer sums as k_spmv_fix
+// (in another order, which integers do not notice) and the same epilogue.
+template <class W, int NV>
+__global__ void __launch_bounds__(kBlock)
+    k_otf_fix(__grid_constant__ const PlanView P, IndexView I, TermsView T, CodeView C,
+              uint32_t const* __restrict__ weights, FixView fv, double const* __restrict__ inv_sqrt_s,
+              double const* __restrict__ x, int64_t const* __restrict__ u, int64_t const* __restrict__ F_in,
+              double* __restrict__ y, Indirect ind) {
+  __shared__ double red[kBlock / 32];
+  __shared__ uint16_t srow[2048];
+  if (ind.stop && *ind.stop) return;
+  RowTab const RT = stage_rows(P, srow);
+  if (ind.k) {
+    uint64_t const k = *ind.k;
+    x += k * ind.ld;
+    y += (k + 1) * ind.ld;
+  }
+  int64_t const F = F_in[0];
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double part = 0.0;
+  if (i < I.D) {
+    uint64_t const r = I.reps[i];
+    int64_t acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0;
+    walk_row(r, T, [&](uint32_t, uint64_t st, uint32_t vid) {
+      auto const c = canonicalize<W>((W)st, P, RT);
+      int64_t const j = find_index((uint64_t)c.rep, I);
+      if (j >= 0) fix_add<NV>(acc, vid << 1 | (c.phase != 0u ? 1u : 0u), u[(uint64_t)j]);
+    });
+    double const xi = x[i];
+    double const yi = fix_row<NV>(acc, fv, F, row_diag<double>(r, T), xi, inv_sqrt_s[divisor_class(weights[i], C)]);
+    y[i] = yi;
+    part = xi * yi;
+  }
+  if (ind.partial) {
+    double const tot = block_sum(part, red);
+    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
+  }
+}
+
 template <class X>
 __global__ void k_dot_conj(X const* __restrict__ x, X const* __restrict__ y, uint64_t n,
                            double2* __restrict__ partial) {
@@ -692,6 +937,31 @@ int build_tables(OperatorData& op) {
   t->code.n_ph = n_ph;
   t->code.real_phase = real_phase ? 1u : 0u;
   t->n_codes = (uint32_t)n_codes;
+  // fixed-point form: real values and characters, few distinct values
+  if (op.is_real && real_phase && n_val <= kFixMaxValues && n_div <= kFixMaxClasses && n_codes <= 16384 &&
+      op.row_bound < (1ull << 40)) {
+    std::vector<uint8_t> fc(n_codes);
+    for (uint32_t v = 0; v < std::max(1u, n_val); ++v)
+      for (uint32_t p = 0; p < n_ph; ++p)
+        for (uint32_t d = 0; d < n_div; ++d) fc[((uint64_t)v * n_ph + p) * n_div + d] = (uint8_t)(v << 1 | p);
+    std::vector<double> sq(n_div);
+    for (uint32_t d = 0; d < n_div; ++d) sq[d] = std::sqrt((double)div[d]);
+    if (int st = t->fix_code.allocate(n_codes)) return st;
+    if (int st = t->fix_sqrt_s.allocate(n_div * 8)) return st;
+    SED_TRY_CUDA(cudaMemcpy(t->fix_code.ptr, fc.data(), n_codes, cudaMemcpyHostToDevice));
+    SED_TRY_CUDA(cudaMemcpy(t->fix_sqrt_s.ptr, sq.data(), n_div * 8, cudaMemcpyHostToDevice));
+    t->fix.code = t->fix_code.as<uint8_t>();
+    t->fix.sqrt_s = t->fix_sqrt_s.as<double>();
+    t->fix.n_codes = (uint32_t)n_codes;
+    t->fix.n_div = n_div;
+    // (row count) x sqrt(S_max), rounded up by a margin far above the
+    // rounding of this product
+    t->fix.bound = (double)std::max<uint64_t>(1, op.row_bound) * sq[n_div - 1] * (1.0 + 1e-9);
+    t->fix.sqrt_s_max = sq[n_div - 1] * (1.0 + 1e-9);
+    for (uint32_t v = 0; v < kFixMaxValues; ++v) t->fix.c[v] = v < n_val ? op.off_values[2 * v] : 0.0;
+    t->fix_nv = n_val <= 1 ? 1u : (n_val <= 2 ? 2u : 4u);
+    t->fix_ok = true;
+  }
   op.tables = std::move(t);
   return LS_SUCCESS;
 }
@@ -729,6 +999,10 @@ int wait_for_caller(std::initializer_list<void const*> buffers) {
 
 OperatorData::~OperatorData() {
   tables.reset();
+  if (fix_event) {
+    ScopedDevice dev(basis ? basis->device : -1);
+    cudaEventDestroy(fix_event);
+  }
   if (cuda_stream) {
     ScopedDevice dev(basis ? basis->device : -1);
     cudaStreamDestroy(cuda_stream);
@@ -772,6 +1046,9 @@ int operator_upload_terms(OperatorData& op) {
         off_vid[(t * 16 + a) * 16 + q] = (uint16_t)vid;
       }
     size_t const n_tuples = term.sites.size() / term.k;
+    unsigned most = 0;
+    for (unsigned a = 0; a < dim; ++a) most = std::max<unsigned>(most, n_off[t * 16 + a]);
+    op.row_bound += (uint64_t)most * n_tuples;
     for (size_t u = 0; u < n_tuples; ++u) {
       uint32_t packed = 0;
       for (unsigned m = 0; m < term.k; ++m) packed |= (uint32_t)term.sites[u * term.k + m] << (8 * m);
@@ -826,6 +1103,7 @@ int operator_ensure_ready(OperatorData& op) {
   if (int st = basis_upload_plan(b, op.cuda_stream)) return st;
   if (int st = operator_upload_terms(op)) return st;
   if (int st = build_tables(op)) return st;
+  if (int st = fix_reserve(op, 1)) return st;
   return LS_SUCCESS;
 }
 
@@ -1051,13 +1329,101 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
   return LS_SUCCESS;
 }
 
+int fix_reserve(OperatorData& op, uint32_t cols) {
+  if (!op.tables || !op.tables->fix_ok || op.fix_cols >= cols) return LS_SUCCESS;
+  uint64_t const D = std::max<uint64_t>(1, op.basis->D);
+  if (int st = op.fix_u.allocate(D * cols * 8)) return st;
+  if (int st = op.fix_slots.allocate((size_t)cols * 16)) return st;
+  if (!op.fix_event) SED_TRY_CUDA(cudaEventCreateWithFlags(&op.fix_event, cudaEventDisableTiming));
+  op.fix_cols = cols;
+  return LS_SUCCESS;
+}
+
+int fix_wait(OperatorData& op) {
+  if (op.fix_event && op.fix_event_recorded) SED_TRY_CUDA(cudaEventSynchronize(op.fix_event));
+  return LS_SUCCESS;
+}
+
 namespace {
+
+template <int NV>
+void launch_spmv_fix(OperatorData& op, StreamView const& S, double const* x, int64_t const* u, int64_t const* F,
+                     double* y, cudaStream_t stream, Indirect ind) {
+  StreamForm const& sf = op.stream;
+  OperatorTables const& tb = *op.tables;
+  unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
+  size_t const smem = tb.fix.n_codes;
+  if (sf.packed) k_spmv_fix<true, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, op.basis->D, x, u, F, y, ind);
+  else k_spmv_fix<false, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, op.basis->D, x, u, F, y, ind);
+  note_launches(1);
+}
+
+template <class W, int NV>
+void launch_otf_fix(OperatorData& op, double const* x, int64_t const* u, int64_t const* F, double* y,
+                    cudaStream_t stream, Indirect ind) {
+  BasisData& b = *op.basis;
+  OperatorTables const& tb = *op.tables;
+  unsigned const grid = (unsigned)((b.D + kBlock - 1) / kBlock);
+  k_otf_fix<W, NV><<<grid, kBlock, 0, stream>>>(b.plan_dev, b.index_view(), op.terms_dev, tb.code,
+                                                b.weights.as<uint32_t>(), tb.fix, tb.inv_sqrt_s.as<double>(), x, u,
+                                                F, y, ind);
+  note_launches(1);
+}
+
+// y = H x in fixed point: max |x|, u = round(sqrt(S) x 2^F), then the SpMV.
+// Outside a Krylov graph the shared workspace is ordered across the callers'
+// streams by fix_event.
+int launch_apply_fix(OperatorData& op, double const* x, double* y, cudaStream_t stream, bool use_stream,
+                     Indirect ind) {
+  BasisData& b = *op.basis;
+  OperatorTables const& tb = *op.tables;
+  uint64_t const D = b.D;
+  auto* mx = op.fix_slots.as<unsigned long long>();
+  auto* F = reinterpret_cast<int64_t*>(mx + op.fix_cols);
+  int64_t* u = op.fix_u.as<int64_t>();
+  bool const ordered = ind.k == nullptr;
+  if (ordered && op.fix_event_recorded) SED_TRY_CUDA(cudaStreamWaitEvent(stream, op.fix_event, 0));
+  SED_TRY_CUDA(cudaMemsetAsync(mx, 0, 8, stream));
+  unsigned const vg = grid_size(D, b.device, 8);
+  k_fix_max<<<vg, kBlock, 0, stream>>>(x, 0, D, mx, ind);
+  k_fix_convert<<<vg, kBlock, 0, stream>>>(x, 0, D, use_stream ? op.stream.row_class.as<uint8_t>() : nullptr,
+                                           b.weights.as<uint32_t>(), tb.code, tb.fix, mx, F, u, D, ind);
+  note_launches(2);
+  if (use_stream) {
+    StreamView const S = stream_view(op);
+    switch (tb.fix_nv) {
+      case 1: launch_spmv_fix<1>(op, S, x, u, F, y, stream, ind); break;
+      case 2: launch_spmv_fix<2>(op, S, x, u, F, y, stream, ind); break;
+      default: launch_spmv_fix<4>(op, S, x, u, F, y, stream, ind); break;
+    }
+  } else if (b.plan.n_bits > 32) {
+    switch (tb.fix_nv) {
+      case 1: launch_otf_fix<uint64_t, 1>(op, x, u, F, y, stream, ind); break;
+      case 2: launch_otf_fix<uint64_t, 2>(op, x, u, F, y, stream, ind); break;
+      default: launch_otf_fix<uint64_t, 4>(op, x, u, F, y, stream, ind); break;
+    }
+  } else {
+    switch (tb.fix_nv) {
+      case 1: launch_otf_fix<uint32_t, 1>(op, x, u, F, y, stream, ind); break;
+      case 2: launch_otf_fix<uint32_t, 2>(op, x, u, F, y, stream, ind); break;
+      default: launch_otf_fix<uint32_t, 4>(op, x, u, F, y, stream, ind); break;
+    }
+  }
+  SED_TRY_CUDA(cudaGetLastError());
+  if (ordered) {
+    SED_TRY_CUDA(cudaEventRecord(op.fix_event, stream));
+    op.fix_event_recorded = true;
+  }
+  return LS_SUCCESS;
+}
 
 template <class X>
 int launch_apply(OperatorData& op, X const* x, X* y, cudaStream_t stream, bool use_stream,
                  Indirect ind) {
   BasisData& b = *op.basis;
   OperatorTables const& tb = *tables_of(op);
+  if constexpr (std::is_same<X, double>::value)
+    if (tb.fix_ok && op.fix_cols >= 1) return launch_apply_fix(op, x, y, stream, use_stream, ind);
   using V = typename Store<X>::V;
   constexpr bool complex_storage = std::is_same<V, cplx>::value;
   uint64_t const D = b.D;
@@ -1127,8 +1493,58 @@ void launch_block_k(unsigned K, StreamView const& S, uint64_t D, X const* x, uin
   }
 }
 
+template <int NV, bool Pk>
+void launch_block_fix_k(unsigned K, StreamView const& S, FixView const& fv, uint64_t D, double const* x, uint64_t ldx,
+                        int64_t const* u, int64_t const* F, double* y, uint64_t ldy, unsigned grid, size_t smem,
+                        cudaStream_t stream) {
+  switch (K) {
+    case 16: k_spmv_block_fix<Pk, NV, 16><<<grid, kBlock, smem, stream>>>(S, fv, D, x, ldx, u, F, y, ldy); break;
+    case 8: k_spmv_block_fix<Pk, NV, 8><<<grid, kBlock, smem, stream>>>(S, fv, D, x, ldx, u, F, y, ldy); break;
+    case 4: k_spmv_block_fix<Pk, NV, 4><<<grid, kBlock, smem, stream>>>(S, fv, D, x, ldx, u, F, y, ldy); break;
+    default: k_spmv_block_fix<Pk, NV, 2><<<grid, kBlock, smem, stream>>>(S, fv, D, x, ldx, u, F, y, ldy); break;
+  }
+  note_launches(1);
+}
+
+// K columns in fixed point (the same per-column sums as launch_apply_fix).
+int launch_block_fix(OperatorData& op, unsigned K, double const* x, uint64_t ldx, double* y, uint64_t ldy,
+                     cudaStream_t stream) {
+  if (int st = fix_reserve(op, K)) return st;
+  BasisData& b = *op.basis;
+  OperatorTables const& tb = *op.tables;
+  StreamForm const& sf = op.stream;
+  uint64_t const D = b.D;
+  auto* mx = op.fix_slots.as<unsigned long long>();
+  auto* F = reinterpret_cast<int64_t*>(mx + op.fix_cols);
+  int64_t* u = op.fix_u.as<int64_t>();
+  if (op.fix_event_recorded) SED_TRY_CUDA(cudaStreamWaitEvent(stream, op.fix_event, 0));
+  SED_TRY_CUDA(cudaMemsetAsync(mx, 0, (size_t)K * 8, stream));
+  dim3 const vg(grid_size(D, b.device, 8), K);
+  k_fix_max<<<vg, kBlock, 0, stream>>>(x, ldx, D, mx, Indirect{});
+  k_fix_convert<<<vg, kBlock, 0, stream>>>(x, ldx, D, sf.row_class.as<uint8_t>(), b.weights.as<uint32_t>(), tb.code,
+                                           tb.fix, mx, F, u, D, Indirect{});
+  note_launches(2);
+  StreamView const S = stream_view(op);
+  unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
+  size_t const smem = tb.fix.n_codes;
+  switch (tb.fix_nv * 2 + (sf.packed ? 1 : 0)) {
+    case 3: launch_block_fix_k<1, true>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
+    case 2: launch_block_fix_k<1, false>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
+    case 5: launch_block_fix_k<2, true>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
+    case 4: launch_block_fix_k<2, false>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
+    case 9: launch_block_fix_k<4, true>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
+    default: launch_block_fix_k<4, false>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
+  }
+  SED_TRY_CUDA(cudaGetLastError());
+  SED_TRY_CUDA(cudaEventRecord(op.fix_event, stream));
+  op.fix_event_recorded = true;
+  return LS_SUCCESS;
+}
+
 template <class X>
 int launch_block(OperatorData& op, unsigned K, X const* x, uint64_t ldx, X* y, uint64_t ldy, cudaStream_t stream) {
+  if constexpr (std::is_same<X, double>::value)
+    if (op.tables->fix_ok) return launch_block_fix(op, K, x, ldx, y, ldy, stream);
   using V = typename Store<X>::V;
   constexpr bool complex_storage = std::is_same<V, cplx>::value;
   StreamForm const& sf = op.stream;
@@ -1287,6 +1703,121 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// FP32-stored form in fixed point. The stored vector x is FP32; its gather
+// copy u_j = round(sqrt(S_j) x_j 2^F) is int32 (4 bytes streamed per
+// element, like FP32), the row sums are exact in int64 and the matrix
+// values, the diagonal and the row epilogue are FP64; y is stored in FP32.
+__global__ void __launch_bounds__(kBlock) k_fix_max32(float const* __restrict__ x, uint64_t D,
+                                                      unsigned long long* __restrict__ max_bits, Indirect ind) {
+  __shared__ unsigned long long red[kBlock / 32];
+  if (ind.stop && *ind.stop) return;
+  if (ind.k) x += (uint64_t)*ind.k * ind.ld;
+  uint32_t m = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (uint64_t)gridDim.x * blockDim.x)
+    m = max(m, (uint32_t)__float_as_uint(x[i]) & 0x7FFFFFFFu);
+  m = __reduce_max_sync(0xffffffffu, m);
+  // as the double of the same value (finite floats keep their order; a float
+  // NaN or infinity maps to the double infinity pattern or above)
+  unsigned long long d;
+  if (m >= 0x7F800000u) d = 0x7FF0000000000000ull | (m & 0x7FFFFFu);
+  else d = (unsigned long long)__double_as_longlong((double)__uint_as_float(m));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (unsigned w = 1; w < kBlock / 32; ++w) d = max(d, red[w]);
+    atomicMax(max_bits, d);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_fix_convert32(float const* __restrict__ x, uint64_t D,
+                                                          uint8_t const* __restrict__ row_class, FixView fv,
+                                                          unsigned long long const* __restrict__ max_bits,
+                                                          int64_t* __restrict__ F_out, int32_t* __restrict__ u,
+                                                          Indirect ind) {
+  __shared__ double fac[kFixMaxClasses];
+  if (ind.stop && *ind.stop) return;
+  if (ind.k) x += (uint64_t)*ind.k * ind.ld;
+  int64_t const F = fix_exponent32(max_bits[0], fv.sqrt_s_max);
+  if (blockIdx.x == 0 && threadIdx.x == 0) F_out[0] = F;
+  double const p2 = F == kFixBad ? 0.0 : fix_pow2(F);
+  for (uint32_t c = threadIdx.x; c < fv.n_div; c += blockDim.x) fac[c] = fv.sqrt_s[c] * p2;
+  __syncthreads();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (uint64_t)gridDim.x * blockDim.x)
+    u[i] = F == kFixBad ? 0 : (int32_t)fix_round((double)x[i] * fac[row_class[i]]);
+}
+
+template <bool Packed, int NV>
+__global__ void __launch_bounds__(kBlock) k_spmv32_fix(StreamView S, FixView fv, uint64_t D,
+                                                       float const* __restrict__ x, int32_t const* __restrict__ u,
+                                                       int64_t const* __restrict__ F_in, float* __restrict__ y,
+                                                       Indirect ind) {
+  extern __shared__ uint8_t code8[];
+  __shared__ double red[kBlock / 32];
+  if (ind.stop && *ind.stop) return;
+  if (ind.k) {
+    uint64_t const k = *ind.k;
+    x += k * ind.ld;
+    y += (k + 1) * ind.ld;
+  }
+  for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
+  __syncthreads();
+  int64_t const F = F_in[0];
+  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t const s = i >> 5;
+  double part = 0.0;
+  if ((s << 5) < D) {
+    uint32_t const lane = threadIdx.x & 31;
+    uint64_t const base = S.slice_ptr[s];
+    uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
+    uint32_t const col_mask = Packed ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
+    int64_t acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0;
+    uint32_t const* ent = S.entries + base + lane;
+    constexpr uint32_t U = 4;
+    uint32_t e = 0;
+    for (; e + U <= width; e += U) {
+      uint32_t v[U];
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) v[q] = __ldcs(ent + (uint64_t)(e + q) * 32);
+      int32_t g[U];
+      uint32_t t[U];
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) {
+        g[q] = 0;
+        t[q] = 0;
+        if (v[q] != kNull) {
+          uint32_t const code =
+              Packed ? (v[q] >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)(e + q) * 32);
+          g[q] = u[v[q] & col_mask];
+          t[q] = code8[code];
+        }
+      }
+#pragma unroll
+      for (uint32_t q = 0; q < U; ++q) fix_add<NV>(acc, t[q], (int64_t)g[q]);
+    }
+    for (; e < width; ++e) {
+      uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
+      if (v != kNull) {
+        uint32_t const code = Packed ? (v >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)e * 32);
+        fix_add<NV>(acc, code8[code], (int64_t)u[v & col_mask]);
+      }
+    }
+    if (i < D) {
+      double const xi = (double)x[i];
+      double const yi = fix_row<NV>(acc, fv, F, static_cast<double const*>(S.diag)[i], xi,
+                                    S.inv_sqrt_s[S.row_class[i]]);
+      float const yf = (float)yi;
+      y[i] = yf;
+      part = xi * (double)yf;
+    }
+  }
+  if (ind.partial) {
+    double const tot = block_sum(part, red);
+    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
+  }
+}
+
 }  // namespace
 
 int operator_prepare_fp32(OperatorData& op, cudaStream_t stream) {
@@ -1296,6 +1827,10 @@ int operator_prepare_fp32(OperatorData& op, cudaStream_t stream) {
   if (sf.diag_f.ptr) return LS_SUCCESS;
   OperatorTables const& tb = *op.tables;
   uint64_t const D = op.basis->D;
+  if (tb.fix_ok) {
+    if (int st = op.fix_u32.allocate(std::max<uint64_t>(1, D) * 4)) return st;
+    if (int st = op.fix_slots32.allocate(16)) return st;
+  }
   if (int st = sf.diag_f.allocate(std::max<uint64_t>(1, D) * 4)) return st;
   if (int st = sf.table_f.allocate((size_t)tb.n_codes * 4)) return st;
   if (int st = sf.invs_f.allocate((size_t)tb.code.n_div * 4)) return st;
@@ -1308,12 +1843,46 @@ int operator_prepare_fp32(OperatorData& op, cudaStream_t stream) {
 }
 
 namespace {
+template <int NV>
+void launch_spmv32_fix(OperatorData& op, StreamView const& S, float const* x, float* y, Indirect ind,
+                       cudaStream_t stream, unsigned grid) {
+  OperatorTables const& tb = *op.tables;
+  auto* slots = op.fix_slots32.as<unsigned long long>();
+  auto* F = reinterpret_cast<int64_t*>(slots + 1);
+  int32_t* u = op.fix_u32.as<int32_t>();
+  uint64_t const D = op.basis->D;
+  size_t const smem = tb.fix.n_codes;
+  if (op.stream.packed)
+    k_spmv32_fix<true, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, D, x, u, F, y, ind);
+  else
+    k_spmv32_fix<false, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, D, x, u, F, y, ind);
+  note_launches(1);
+}
+
 int launch32(OperatorData& op, float const* x, float* y, Indirect ind, cudaStream_t stream, unsigned* blocks) {
   StreamForm const& sf = op.stream;
   if (!sf.diag_f.ptr) return fail(LS_CACHE_NOT_BUILT, "FP32 companions are not prepared");
   StreamView const S = stream_view(op);
   unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
   if (blocks) *blocks = grid;
+  OperatorTables const& tb = *op.tables;
+  if (tb.fix_ok && op.fix_u32.ptr) {
+    uint64_t const D = op.basis->D;
+    auto* slots = op.fix_slots32.as<unsigned long long>();
+    SED_TRY_CUDA(cudaMemsetAsync(slots, 0, 8, stream));
+    unsigned const vg = grid_size(D, op.basis->device, 8);
+    k_fix_max32<<<vg, kBlock, 0, stream>>>(x, D, slots, ind);
+    k_fix_convert32<<<vg, kBlock, 0, stream>>>(x, D, sf.row_class.as<uint8_t>(), tb.fix, slots,
+                                               reinterpret_cast<int64_t*>(slots + 1), op.fix_u32.as<int32_t>(), ind);
+    note_launches(2);
+    switch (tb.fix_nv) {
+      case 1: launch_spmv32_fix<1>(op, S, x, y, ind, stream, grid); break;
+      case 2: launch_spmv32_fix<2>(op, S, x, y, ind, stream, grid); break;
+      default: launch_spmv32_fix<4>(op, S, x, y, ind, stream, grid); break;
+    }
+    SED_TRY_CUDA(cudaGetLastError());
+    return LS_SUCCESS;
+  }
   // size the table to the codes: a large carve-out would shrink L1 for the gathers
   size_t const smem = S.n_codes <= 8192u ? (size_t)S.n_codes * 4 : 0;
   if (sf.packed)

@@ -123,6 +123,84 @@ __device__ __forceinline__ cplx row_diag<cplx>(uint64_t r, TermsView const& T) {
 }
 
 
+// ------------------------------------------ exact fixed-point accumulation --
+// For a real operator with real characters (chi = +-1) the off-diagonal part
+// of row i is (1/sqrt(S_i)) sum_v c_v sum_{e: value v} chi_e sqrt(S_j) x_j.
+// With u_j = round(sqrt(S_j) x_j 2^F) held as int64 (one pass over x before
+// the matvec, F chosen per vector from max|x_j| so that no row sum can
+// overflow), the inner sums are exact integer sums of +-u_j: one integer
+// accumulator per distinct value c_v, converted and scaled by c_v 2^-F once
+// per row. The only rounding before the row's FP64 epilogue is that of u_j
+// (half an integer step, at most 2^-61 of the largest |u|), and integer sums
+// do not depend on their order, so every form of the matvec agrees bit for
+// bit. The integer pipe is 64x wider than GB300's FP64 pipe, which otherwise
+// bounds the matvec at one FMA per element.
+constexpr unsigned kFixMaxValues = 4;   // accumulators per row
+constexpr unsigned kFixMaxClasses = 256;
+constexpr int64_t kFixBad = INT64_MIN;  // x held a NaN or an infinity
+
+struct FixView {
+  uint8_t const* code;   // [n_codes]: value index << 1 | character sign
+  double const* sqrt_s;  // [n_div]: sqrt(S) per stabiliser class
+  uint32_t n_codes;
+  uint32_t n_div;
+  double bound;          // (largest row count) x sqrt(largest S), rounded up
+  double sqrt_s_max;     // sqrt(largest S), rounded up
+  double c[kFixMaxValues];
+};
+
+// Nearest integer of a finite d with |d| < 2^62 (halves away from zero),
+// from the bit pattern: integer instructions only.
+__device__ __forceinline__ int64_t fix_round(double d) {
+  uint64_t const b = (uint64_t)__double_as_longlong(d);
+  int const e = (int)((b >> 52) & 0x7FF);
+  uint64_t const m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+  int const sh = 1075 - e;  // |d| = m 2^-sh for normal d
+  uint64_t mag;
+  if (sh <= 0)
+    mag = m << (-sh);
+  else if (sh >= 64)
+    mag = 0;
+  else
+    mag = (m + (1ull << (sh - 1))) >> sh;
+  return (b >> 63) ? -(int64_t)mag : (int64_t)mag;
+}
+
+// Scale exponent F for a vector whose largest |x_j| has bit pattern
+// max_bits: bound * max|x| * 2^F < 2^62, so a row's sum of at most
+// (row count) terms |u_j| <= sqrt(S_max) max|x| 2^F stays below 2^62.
+__device__ __forceinline__ int64_t fix_exponent(uint64_t max_bits, double bound) {
+  if (max_bits >= 0x7FF0000000000000ull) return kFixBad;
+  if (max_bits == 0) return 0;
+  double const t = __longlong_as_double((long long)max_bits) * bound;
+  int const e = (int)(((uint64_t)__double_as_longlong(t) >> 52) & 0x7FF) - 1023;  // t < 2^(e+1)
+  return 61 - e;  // in [-963, 1084]: t is finite, at least 2^-1074 before the bound
+}
+
+// The same for 32-bit u (the FP32-stored form): |u_j| < 2^30, sums in int64.
+__device__ __forceinline__ int64_t fix_exponent32(uint64_t max_bits, double sqrt_s_max) {
+  if (max_bits >= 0x7FF0000000000000ull) return kFixBad;
+  if (max_bits == 0) return 0;
+  double const t = __longlong_as_double((long long)max_bits) * sqrt_s_max;
+  int const e = (int)(((uint64_t)__double_as_longlong(t) >> 52) & 0x7FF) - 1023;  // t < 2^(e+1)
+  int64_t F = 29 - e;
+  return F > 1000 ? 1000 : (F < -1000 ? -1000 : F);
+}
+
+// 2^p for |p| <= 1000 (a normal double), built from its bits.
+__device__ __forceinline__ double fix_pow2(int64_t p) {
+  return __longlong_as_double((long long)((uint64_t)(1023 + p) << 52));
+}
+
+// a 2^p for any exponent F can produce (|p| <= 1100): one multiplication
+// when 2^p is a normal double, else two by halves of p (each exact unless
+// the result is subnormal).
+__device__ __forceinline__ double fix_ldexp(double a, int64_t p) {
+  if (p >= -1000 && p <= 1000) return a * fix_pow2(p);
+  int64_t const h = p / 2;
+  return (a * fix_pow2(h)) * fix_pow2(p - h);
+}
+
 struct OperatorTables {
   DeviceBuffer divisors;
   DeviceBuffer table;    // double[n_codes], real operators only
@@ -130,6 +208,12 @@ struct OperatorTables {
   DeviceBuffer inv_sqrt_s;
   CodeView code{};
   uint32_t n_codes = 0;
+  // fixed-point form (fix_ok: the operator qualifies)
+  bool fix_ok = false;
+  uint32_t fix_nv = 1;   // accumulators per row: 1, 2 or 4
+  DeviceBuffer fix_code;
+  DeviceBuffer fix_sqrt_s;
+  FixView fix{};
 };
 
 // One row of the streamed SpMV over a SELL-32 slice (lane = row in slice).

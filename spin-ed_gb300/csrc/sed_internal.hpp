@@ -207,10 +207,22 @@ struct OperatorData {
   DeviceBuffer term_buf;
   TermsView terms_dev{};
   std::vector<double> off_values;  // distinct off-diagonal matrix values (re, im)
+  uint64_t row_bound = 0;          // most off-diagonal elements any row can generate
   StreamForm stream;
   std::unique_ptr<OperatorTables> tables;
   int form = SED_FORM_AUTO;  // selected by sed_operator_prepare
   cudaStream_t cuda_stream = nullptr;
+  // fixed-point matvec workspace (see operator_impl.cuh): u for fix_cols
+  // columns, then per column the max |x| bit pattern and the exponent F;
+  // fix_event orders its reuse across the callers' streams
+  DeviceBuffer fix_u;
+  DeviceBuffer fix_slots;
+  uint32_t fix_cols = 0;
+  cudaEvent_t fix_event = nullptr;
+  bool fix_event_recorded = false;
+  // the FP32-stored Krylov phase's gather copy: u_j in int32, then its slots
+  DeviceBuffer fix_u32;
+  DeviceBuffer fix_slots32;
   std::mutex mu;
   ~OperatorData();
 };
@@ -225,6 +237,11 @@ int wait_for_caller(std::initializer_list<void const*> buffers);
 int operator_record_stream(OperatorData& op, cudaStream_t stream);
 int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void const* x,
                           uint64_t ldx, void* y, uint64_t ldy, cudaStream_t stream, int form);
+// Fixed-point matvec workspace for `cols` columns (no-op when the operator
+// does not qualify or already has it), and a host wait for the last use of
+// that workspace on any caller's stream.
+int fix_reserve(OperatorData& op, uint32_t cols);
+int fix_wait(OperatorData& op);
 // FP32 companions of the stream form (mixed-precision Krylov phase).
 int operator_prepare_fp32(OperatorData& op, cudaStream_t stream);
 

@@ -233,3 +233,37 @@ def test_orbit_table_record_bit_identical(sed, oracle, name):
     assert torch.equal(y1, y2)
     np.testing.assert_allclose(y1.cpu().numpy(), oop.matvec(x.cpu().numpy()).real, rtol=0,
                                atol=1e-12 * max(1.0, float(y1.abs().max())))
+
+
+@pytest.mark.parametrize("name", ["chain24", "chain20_j2", "square4_j2"])
+def test_fixed_point_matvec_scales_and_specials(sed, oracle, name):
+    """The FP64 matvec of real operators with at most 4 distinct couplings
+    accumulates u_j = round(sqrt(S_j) x_j 2^F) in int64 with F chosen per
+    vector from max|x|: results match the oracle at 1e-12 of max|y| at any
+    scale of x, a zero vector gives zeros, a NaN or infinity in x gives NaN
+    everywhere, and entries far below max|x| are carried with an absolute
+    error below 2^-55 max|x|."""
+    import torch
+    built, ob, oop = both(sed, oracle, MODELS[name])
+    op = built.hamiltonian
+    D = len(ob.reps)
+    rng = np.random.default_rng(21)
+    x0 = rng.normal(size=D)
+    for scale in (1e-300, 1e-150, 1e-8, 1.0, 1e8, 1e150, 1e300):
+        x = torch.tensor(x0 * scale, device="cuda")
+        y = sed.apply(op, x).cpu().numpy()
+        want = oop.matvec(x0 * scale).real
+        np.testing.assert_allclose(y, want, rtol=0, atol=RTOL64 * np.abs(want).max())
+    z = sed.apply(op, torch.zeros(D, dtype=torch.float64, device="cuda")).cpu().numpy()
+    assert np.all(z == 0.0)
+    for bad in (np.nan, np.inf):
+        xb = x0.copy()
+        xb[D // 2] = bad
+        yb = sed.apply(op, torch.tensor(xb, device="cuda")).cpu().numpy()
+        assert np.all(np.isnan(yb))
+    # wide dynamic range: half the entries 1e-12 of the others
+    xw = x0.copy()
+    xw[::2] *= 1e-12
+    yw = sed.apply(op, torch.tensor(xw, device="cuda")).cpu().numpy()
+    want = oop.matvec(xw).real
+    assert np.max(np.abs(yw - want)) <= 1e-13 * np.abs(xw).max() * oop.sparse().__abs__().sum(axis=1).max()

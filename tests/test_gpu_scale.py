@@ -215,13 +215,13 @@ def test_chain40_representatives_and_ground_state(sed, oracle):
     ptr = L.load().sed_basis_device_states(built.basis.ptr)
 
     class _Dev:
-        __cuda_array_interface__ = {"shape": (D,), "typestr": "<i8", "data": (ptr, True), "version": 2}
+        __cuda_array_interface__ = {"shape": (D,), "typestr": "<i8", "data": (ptr, False), "version": 2}
 
     dev = torch.as_tensor(_Dev(), device="cuda")  # 40-bit words: int64 view of the uint64 list
     assert bool((dev[1:] > dev[:-1]).all())
     G = ob.group_order
     rng = np.random.default_rng(3)
-    picks = [int(v) for v in dev[torch.linspace(0, D - 1, 8, dtype=torch.int64, device="cuda")].cpu()]
+    picks = [int(dev[(D - 1) * q // 7].item()) for q in range(8)]  # exact integer positions < D
     space = comb(40, 20)
     slices = [(max(0, colex_rank(v, 40) - (1 << 20)), max(0, colex_rank(v, 40) - (1 << 20)) + (1 << 21))
               for v in picks]
