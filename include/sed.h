@@ -264,6 +264,17 @@ SED_API int sed_operator_matmat_device(ls_operator const* op, int dtype, uint64_
                                uint64_t block_size, void const* x, uint64_t x_stride, void* y,
                                uint64_t y_stride, void* stream);
 
+/* Measurement: y = H x for a real operator, x and y FP64 device vectors of
+ * the basis size, `repetitions` times back to back on the operator's stream
+ * after two untimed ones; *ms_matvec is the CUDA-event time per complete
+ * matvec and *ms_kernel the time per launch of the SpMV kernel alone. The
+ * two differ when the matvec runs in exact fixed point (real operators with
+ * real characters and at most 4 distinct off-diagonal values): its pre-pass
+ * turns x into the scaled integer copy the SpMV gathers, and the Lanczos
+ * solver produces that copy inside its vector update instead. */
+SED_API int sed_operator_time_matvec(ls_operator const* op, void const* x, void* y, unsigned repetitions,
+                                     double* ms_matvec, double* ms_kernel);
+
 /* No counterpart in the reference: ls_operator_expectation for callers that
  * cannot let the library allocate device memory (a process whose device
  * memory belongs to its own pool allocator, or a latency-critical loop that
@@ -389,6 +400,29 @@ SED_API int sed_mlp_uses_tensor_cores(sed_mlp const* mlp);
  * about 20 ms per call; it is released automatically when another libsed
  * allocation runs out of memory. This frees it now (all devices). */
 SED_API void sed_release_workspace(void);
+
+/* A cap on the device memory libsed holds (all its buffers on all devices,
+ * the cached Krylov workspace included); 0 removes it. An allocation that
+ * would exceed it first releases the cached workspace, then fails with
+ * LS_OUT_OF_MEMORY, as a cudaMalloc that runs out of memory does. The cap
+ * lets a process that shares a GPU bound libsed's share of it. */
+SED_API void sed_set_device_memory_limit(uint64_t bytes);
+/* Device bytes libsed holds now. */
+SED_API uint64_t sed_device_memory_in_use(void);
+
+/* Bound on every wait inside libsed kernels that wait on other threads or
+ * blocks: the group barriers of sed_eigh_batched's persistent kernel (20 s by
+ * default) and the tensor-core MLP kernel's waits on its copies and MMAs (1 s
+ * by default). A wait that runs out sets an error flag, the kernel drains
+ * and returns, and the call fails with LS_DEVICE_TIMEOUT; the CUDA context
+ * stays usable. seconds <= 0 restores the defaults. Process-wide. */
+SED_API void sed_set_device_wait_limit(double seconds);
+/* Test hook: the number of arrivals each batched group barrier waits for
+ * beyond its own CTAs (0 in normal use). With n > 0 every barrier waits for
+ * CTAs that do not exist, so its bounded wait runs out and sed_eigh_batched
+ * reports LS_DEVICE_TIMEOUT; tests use it to exercise that path without a
+ * GPU fault. Process-wide. */
+SED_API void sed_debug_barrier_extra_arrivals(unsigned n);
 
 /* Number of libsed kernels launched by this process so far (graph replays
  * count their kernel nodes). */

@@ -46,7 +46,7 @@ constexpr int kB = 4;               // block size
 constexpr int kMaxBlocks = 16;      // stored Krylov blocks per cycle (n <= 64)
 constexpr int kMaxN = kB * kMaxBlocks;
 constexpr int kPart = 16 * (kMaxBlocks + 1);  // partial sums per CTA and slot
-constexpr uint64_t kBarrierNs = 20000000000ull;  // 20 s per barrier: far beyond any phase
+constexpr uint64_t kBarrierNs = 20000000000ull;  // default: 20 s per barrier, far beyond any phase
 constexpr size_t kStatsOff = 12 * 8;                // per-problem output record: out[12], stats[4], flag[4], prof[8]
 constexpr size_t kProfOff = kStatsOff + 32;
 constexpr size_t kOutBytes = kProfOff + 64;
@@ -85,6 +85,8 @@ struct BatchArgs {
   uint32_t max_steps;     // block steps per problem in total
   uint32_t rr_every;
   int* error;
+  uint64_t wait_ns;        // bound on every barrier wait
+  uint32_t extra_arrivals; // arrivals a barrier waits for beyond its CTAs (0; see sed_debug_barrier_extra_arrivals)
 };
 
 // One row of a [D][4] block (32 bytes, one sector).
@@ -101,27 +103,33 @@ __device__ __forceinline__ Row4 ldcg4(double const* p) {
   return mk4(a.x, a.y, b.x, b.y);
 }
 
-// Bounded barrier of the `n` CTAs of a group; false (and *error = 2) if it
-// timed out. Every thread of the CTA must call it.
-__device__ bool group_barrier(uint32_t* bar, uint32_t n, int* error) {
+// Bounded barrier of the `n` CTAs of a group; false if it timed out (then
+// *error = 2) or another CTA has already reported an error, which ends the
+// wait early. Every thread of the CTA must call it.
+__device__ bool group_barrier(uint32_t* bar, uint32_t n, BatchArgs const& a) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    if (n > 1) {
+    uint32_t const need = n + a.extra_arrivals;
+    if (need > 1) {
       volatile uint32_t* gen = bar + 1;
       uint32_t const g = *gen;
       __threadfence();
-      if (atomicAdd(bar, 1u) == n - 1) {
+      if (atomicAdd(bar, 1u) == need - 1) {
         atomicExch(bar, 0u);
         __threadfence();
         atomicAdd(bar + 1, 1u);
       } else {
         uint64_t const t0 = tc::global_ns();
         while (*gen == g) {
-          if (tc::global_ns() - t0 > kBarrierNs) {
+          if (*(volatile int*)a.error) {
             ok = 0;
-            atomicExch(error, 2);
+            break;
+          }
+          if (tc::global_ns() - t0 > a.wait_ns) {
+            ok = 0;
+            atomicExch(a.error, 2);
             break;
           }
           __nanosleep(64);
@@ -159,7 +167,7 @@ struct Ctx {
   ChainDesc const& c;
   uint32_t rank, ncta;
   uint32_t* bar;
-  int* error;
+  BatchArgs const* args;
   uint64_t r0, r1;      // own rows
   uint64_t s0, s1;      // own slices
   uint32_t slot;        // partial-sum double buffer
@@ -173,7 +181,7 @@ __device__ bool group_sum(Ctx& x, double const* local, int K, double* total) {
   double* mine = x.c.part + ((size_t)x.slot * x.ncta + x.rank) * kPart;
   for (int k = threadIdx.x; k < K; k += blockDim.x) mine[k] = local[k];
   __threadfence();
-  if (!group_barrier(x.bar, x.ncta, x.error)) return false;
+  if (!group_barrier(x.bar, x.ncta, *x.args)) return false;
   double const* all = x.c.part + (size_t)x.slot * x.ncta * kPart;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double s = 0.0;
@@ -621,7 +629,7 @@ __device__ void random_block(Ctx& x) {
 // couplings), or, after a breakdown, the lowest four alone (explicit restart).
 __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, uint32_t* bar, BatchArgs const& a,
                             double* red, double* tmp, double* C, double* A, double* Q) {
-  Ctx x{c, rank, ncta, bar, a.error, 0, 0, 0, 0, 0, red, tmp};
+  Ctx x{c, rank, ncta, bar, &a, 0, 0, 0, 0, 0, red, tmp};
   x.s0 = c.n_slices * rank / ncta;
   x.s1 = c.n_slices * (rank + 1) / ncta;
   x.r0 = std::min<uint64_t>(c.D, x.s0 * 32);
@@ -653,7 +661,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
     bool broke = false;
     for (;; ++j) {
       double* Vj = c.V + (uint64_t)j * c.D * 4;
-      if (!group_barrier(bar, ncta, a.error)) return;  // V_j complete on every CTA before the gathers
+      if (!group_barrier(bar, ncta, a)) return;  // V_j complete on every CTA before the gathers
       lap(4);
       block_spmv(x, Vj, c.W);
       ++matvecs;
@@ -677,7 +685,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
       bool const full = j + 1 >= c.m_blocks || steps >= a.max_steps || broke;
       if (full || (j + 1) % a.rr_every == 0) {
         __threadfence();
-        if (!group_barrier(bar, ncta, a.error)) return;  // T and B visible to the leader
+        if (!group_barrier(bar, ncta, a)) return;  // T and B visible to the leader
         if (leader) {
           double const worst = rayleigh_ritz(c, j, !broke, A, Q);
           if (threadIdx.x == 0) {
@@ -685,18 +693,18 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
             __threadfence();
           }
         }
-        if (!group_barrier(bar, ncta, a.error)) return;
+        if (!group_barrier(bar, ncta, a)) return;
         lap(3);
         if (ldcg(c.flag) != 0u || full) break;
       }
     }
     bool const thick = !broke && j >= 1 && c.m_blocks >= 3;
     ritz_vectors(x, j, A, thick);  // A: the dynamic shared area, free outside the Jacobi solve
-    if (!group_barrier(bar, ncta, a.error)) return;  // every CTA done reading the old basis
+    if (!group_barrier(bar, ncta, a)) return;  // every CTA done reading the old basis
     if (thick && j + 1 != 2) copy_block(x, c.V + 2 * c.D * 4, c.V + (uint64_t)(j + 1) * c.D * 4);
     copy_block(x, c.V, c.W);
     if (thick) copy_block(x, c.V + c.D * 4, c.W2);
-    if (!group_barrier(bar, ncta, a.error)) return;  // Psi rows visible to every CTA's SpMV gathers
+    if (!group_barrier(bar, ncta, a)) return;  // Psi rows visible to every CTA's SpMV gathers
     lap(4);
     // true residuals of the lowest four Ritz pairs
     block_spmv(x, c.V, c.W);
@@ -770,7 +778,7 @@ __global__ void __launch_bounds__(256, 2) k_batch_lanczos(BatchArgs a) {
     ChainDesc const& c = a.chains[a.order[g.first + q]];
     solve_chain(c, rank, g.ncta, g.bar, a, red, tmp, C, dyn, dyn + kMaxN * kMaxN);
     if (*(volatile int*)a.error) return;
-    if (!group_barrier(g.bar, g.ncta, a.error)) return;
+    if (!group_barrier(g.bar, g.ncta, a)) return;
   }
 }
 
@@ -1023,6 +1031,8 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     a.max_steps = max_steps;
     a.rr_every = 2;
     a.error = reinterpret_cast<int*>(base + off_err);
+    a.wait_ns = device_wait_ns(kBarrierNs);
+    a.extra_arrivals = g_barrier_extra_arrivals.load();
     cudaEvent_t e0, e1;
     SED_TRY_CUDA(cudaEventCreate(&e0));
     SED_TRY_CUDA(cudaEventCreate(&e1));

@@ -4,6 +4,7 @@
 // turned into text by ls_error_to_string and freed by ls_destroy_string. The
 // text carries the description of the code plus the detail recorded by the
 // failing call on the same host thread.
+#include <atomic>
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
@@ -114,9 +115,36 @@ void krylov_give(DeviceBuffer& b) {
   b.reset();
 }
 
+namespace {
+// Device bytes held by libsed buffers (all devices) and the caller's cap on
+// them (sed_set_device_memory_limit; 0 = none).
+std::atomic<uint64_t> g_dev_bytes{0};
+std::atomic<uint64_t> g_dev_limit{0};
+
+bool over_limit(size_t n) {
+  uint64_t const lim = g_dev_limit.load();
+  return lim && g_dev_bytes.load() + n > lim;
+}
+}  // namespace
+
+std::atomic<uint64_t> g_wait_ns{0};
+std::atomic<uint32_t> g_barrier_extra_arrivals{0};
+
+uint64_t device_wait_ns(uint64_t default_ns) {
+  uint64_t const w = g_wait_ns.load();
+  return w ? w : default_ns;
+}
+
 int DeviceBuffer::allocate(size_t n) {
   reset();
   if (int st = current_device(&device)) return st;
+  if (over_limit(n)) {
+    release_cache(device);  // the cached Krylov workspace counts towards the cap
+    if (over_limit(n))
+      return fail(LS_OUT_OF_MEMORY, "libsed device-memory limit of " + std::to_string(g_dev_limit.load()) +
+                                        " bytes: " + std::to_string(g_dev_bytes.load()) + " in use, " +
+                                        std::to_string(n) + " more requested");
+  }
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, n ? n : 1);
   if (e == cudaErrorMemoryAllocation) {
@@ -132,6 +160,7 @@ int DeviceBuffer::allocate(size_t n) {
   }
   ptr = p;
   bytes = n;
+  g_dev_bytes.fetch_add(n);
   return LS_SUCCESS;
 }
 
@@ -142,6 +171,7 @@ void DeviceBuffer::reset() {
     if (device >= 0 && device != prev) cudaSetDevice(device);
     cudaFree(ptr);
     if (device >= 0 && device != prev && prev >= 0) cudaSetDevice(prev);
+    g_dev_bytes.fetch_sub(bytes);
   }
   ptr = nullptr;
   bytes = 0;
@@ -177,6 +207,12 @@ using namespace sed;
 extern "C" {
 
 void sed_release_workspace(void) { release_cache(-1); }
+void sed_set_device_memory_limit(uint64_t bytes) { g_dev_limit.store(bytes); }
+void sed_set_device_wait_limit(double seconds) {
+  g_wait_ns.store(seconds > 0 ? (uint64_t)(seconds * 1e9) : 0);
+}
+void sed_debug_barrier_extra_arrivals(unsigned n) { g_barrier_extra_arrivals.store(n); }
+uint64_t sed_device_memory_in_use(void) { return g_dev_bytes.load(); }
 
 
 char const* ls_error_to_string(int status) {

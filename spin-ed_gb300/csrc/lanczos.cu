@@ -86,19 +86,35 @@ __global__ void k_reduce(double const* __restrict__ partial, unsigned n, LzHeade
 }
 
 template <class X>
-__global__ void k_zero_alpha(LzHeader const* h, double* alpha) {
+__global__ void k_zero_alpha(LzHeader const* h, double* alpha, unsigned long long* wmax) {
   if (h->stop) return;
   alpha[h->k] = 0.0;
+  if (wmax) *wmax = 0;  // fused fixed-point step: k_update's max |w| starts here
 }
+
+// Fused fixed-point Lanczos step (FP64, one vector): k_update leaves max |w|
+// (bit pattern) in *wmax and k_scale_next writes, next to v_{k+1} = w /
+// beta_k, the next matvec's gather copy u = round(sqrt(S) v_{k+1} 2^F) and
+// F, so that matvec skips its own pre-pass. `on` is false otherwise.
+struct FixStep {
+  bool on;
+  unsigned long long* wmax;
+  int64_t* F;
+  int64_t* u;
+  uint8_t const* row_class;
+  FixView fv;
+};
 
 // w = w - alpha_k v_k - beta_{k-1} v_{k-1}; partial ||w||^2.
 template <class X>
 __global__ void k_update(X* __restrict__ V, uint64_t ld_v, uint64_t D, LzHeader const* h,
                          double const* __restrict__ alpha, double const* __restrict__ beta,
-                         double* __restrict__ partial) {
+                         double* __restrict__ partial, unsigned long long* __restrict__ wmax) {
   using Vt = typename Store<X>::V;
   __shared__ double red[kBlock / 32];
+  __shared__ unsigned long long redm[kBlock / 32];
   if (h->stop) return;
+  unsigned long long m = 0;
   uint32_t const k = h->k;
   X* w = V + (uint64_t)(k + 1) * ld_v;
   X const* v = V + (uint64_t)k * ld_v;
@@ -118,9 +134,20 @@ __global__ void k_update(X* __restrict__ V, uint64_t ld_v, uint64_t D, LzHeader 
     }
     Store<X>::store(w, i, wi);
     part += dot_re(wi, wi);
+    if constexpr (std::is_same<Vt, double>::value)
+      m = max(m, (unsigned long long)__double_as_longlong(wi) & 0x7FFFFFFFFFFFFFFFull);
   }
   double const tot = block_sum(part, red);
   if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+  if (wmax) {
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) redm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (unsigned q = 1; q < kBlock / 32; ++q) m = max(m, redm[q]);
+      atomicMax(wmax, m);
+    }
+  }
 }
 
 // Classical Gram-Schmidt pass against V[0..k]: c_j = <V_j, w> (partials per
@@ -216,13 +243,35 @@ __global__ void k_cgs_update(X* __restrict__ V, uint64_t ld_v, uint64_t D, LzHea
 
 template <class X>
 __global__ void k_scale_next(X* __restrict__ V, uint64_t ld_v, uint64_t D, LzHeader const* h,
-                             double const* __restrict__ beta) {
+                             double const* __restrict__ beta, FixStep fx) {
+  __shared__ double fac[kFixMaxClasses];
   if (h->stop) return;
   uint32_t const k = h->k;
   double const b = beta[k];
   if (!(b > 0.0)) return;
   double const inv = 1.0 / b;
   X* w = V + (uint64_t)(k + 1) * ld_v;
+  if constexpr (std::is_same<X, double>::value) {
+    if (fx.on) {
+      // max |v_j| = fl(max |w_j| inv): the rounding of v_j = w_j inv is
+      // monotone in |w_j|, so this bounds every |v_j| exactly
+      double const vmax = __longlong_as_double((long long)*fx.wmax) * inv;
+      int64_t const F = fix_exponent((uint64_t)__double_as_longlong(fabs(vmax)), fx.fv.bound);
+      if (blockIdx.x == 0 && threadIdx.x == 0) *fx.F = F;
+      int64_t const F1 = (F == kFixBad || (F >= -1000 && F <= 1000)) ? 0 : F / 2;
+      double const p1 = fix_pow2(F1);
+      double const p2 = F == kFixBad ? 0.0 : fix_pow2(F - F1);
+      for (uint32_t c = threadIdx.x; c < fx.fv.n_div; c += blockDim.x) fac[c] = fx.fv.sqrt_s[c] * p2;
+      __syncthreads();
+      for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
+           i += (uint64_t)gridDim.x * blockDim.x) {
+        double const v = inv * w[i];
+        w[i] = v;
+        fx.u[i] = F == kFixBad ? 0 : fix_round((F1 ? v * p1 : v) * fac[fx.row_class[i]]);
+      }
+      return;
+    }
+  }
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D;
        i += (uint64_t)gridDim.x * blockDim.x) {
     auto v = Store<X>::load(w, i);
@@ -598,6 +647,7 @@ struct Solver {
   cudaGraphExec_t graph = nullptr;
   size_t graph_kernels = 0;
   LzHeader* hh = nullptr;  // pinned host mirror
+  FixStep fx{};            // fused fixed-point step (FP64, one vector, stream form)
 
   Solver(OperatorData& o, int dt, cudaStream_t s) : op(o), dtype(dt), D(o.basis->D), stream(s) {}
   ~Solver() {
@@ -637,22 +687,38 @@ struct Solver {
     SED_TRY_CUDA(cudaMemcpyAsync(hdr(), hh, sizeof(LzHeader), cudaMemcpyHostToDevice, stream));
     SED_TRY_CUDA(cudaMemsetAsync(ws.alpha.ptr, 0, (size_t)m_max * 8, stream));
     SED_TRY_CUDA(cudaMemsetAsync(ws.beta.ptr, 0, (size_t)m_max * 8, stream));
+    FixSlots fs;
+    if (std::is_same<X, double>::value && !reorth && fix_slots(op, &fs))
+      fx = FixStep{true, fs.max_bits, fs.F, fs.u, fs.row_class, fs.view};
     return LS_SUCCESS;
+  }
+
+  // Fused step: the matvec's pre-pass for the current v_k, needed whenever
+  // v_k was not produced by k_scale_next (the start and every restart) or
+  // the workspace was used by another matvec since.
+  int prescale() {
+    if (!fx.on) return LS_SUCCESS;
+    Indirect ind;
+    ind.k = &hdr()->k;
+    ind.stop = &hdr()->stop;
+    ind.ld = D;
+    return fix_prescale(op, reinterpret_cast<double const*>(V()), ind, stream);
   }
 
   // One Lanczos step (all kernels read k from the header).
   int enqueue_step() {
     LzHeader* h = hdr();
-    { k_zero_alpha<X><<<1, 1, 0, stream>>>(h, ws.alpha.as<double>()); note_launches(1); }
+    { k_zero_alpha<X><<<1, 1, 0, stream>>>(h, ws.alpha.as<double>(), fx.on ? fx.wmax : nullptr); note_launches(1); }
     Indirect ind;
     ind.k = &h->k;
     ind.stop = &h->stop;
     ind.ld = D;
     ind.partial = ws.partial.as<double>();
+    ind.prescaled = fx.on;
     if (int st = operator_apply_krylov(op, dtype, V(), ind, stream, &spmv_blocks)) return st;
     { k_reduce<<<1, kRedThreads, 0, stream>>>(ws.partial.as<double>(), spmv_blocks, h, ws.alpha.as<double>(), 0); note_launches(1); }
     { k_update<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.alpha.as<double>(), ws.beta.as<double>(),
-                                                ws.partial.as<double>()); note_launches(1); }
+                                                ws.partial.as<double>(), fx.on ? fx.wmax : nullptr); note_launches(1); }
     if (hh->reorth) {
       for (int pass = 0; pass < 2; ++pass) {
         dim3 grid(vblocks, (m_max + 15) / 16);
@@ -664,7 +730,7 @@ struct Solver {
       }
     }
     { k_reduce<<<1, kRedThreads, 0, stream>>>(ws.partial.as<double>(), vblocks, h, ws.beta.as<double>(), 1); note_launches(1); }
-    { k_scale_next<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.beta.as<double>()); note_launches(1); }
+    { k_scale_next<X><<<vblocks, kBlock, 0, stream>>>(V(), D, D, h, ws.beta.as<double>(), fx); note_launches(1); }
     { k_tridiag<<<1, 32, 0, stream>>>(h, ws.alpha.as<double>(), ws.beta.as<double>(), ws.s.as<double>(),
                                     ws.work.as<double>()); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
@@ -881,6 +947,7 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
   }
   if (int st = S.normalise_vec(S.V(), nullptr)) return st;
   if (int st = S.capture(check)) return st;
+  if (int st = S.prescale()) return st;
   uint64_t steps = 0, matvecs = 0, restarts = 0;
   std::vector<double> E(nev, 0.0), R(nev, 1e300);
   bool converged = false;
@@ -951,6 +1018,7 @@ int solve(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* ev
     S.hh->tol_est = 0.5 * tol;
     S.hh->reorth = reorth ? 1u : 0u;
     if (int st = S.write_header()) return st;
+    if (int st = S.prescale()) return st;  // the residual matvecs used the workspace
   }
   SED_TRY_CUDA(cudaStreamSynchronize(stream));
   for (uint32_t j = 0; j < nev; ++j) {
@@ -1052,7 +1120,7 @@ int solve_mixed(OperatorData& op, int out_dtype, sed_eigh_options const& o, doub
     int st = LS_SUCCESS;
     unsigned spmv_blocks = 0;
     for (uint32_t i = 0; i < check && st == LS_SUCCESS; ++i) {
-      k_zero_alpha<float><<<1, 1, 0, stream>>>(h, alpha.as<double>());
+      k_zero_alpha<float><<<1, 1, 0, stream>>>(h, alpha.as<double>(), nullptr);
       Indirect ind;
       ind.k = &h->k;
       ind.stop = &h->stop;

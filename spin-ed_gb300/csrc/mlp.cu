@@ -310,7 +310,7 @@ constexpr int kTcMaxStages = 8;                     // ring of weight stages of 
 constexpr int kTcMaxBlocks = 4;                     // H / 128
 constexpr uint32_t kTcCols = 512;                   // TMEM columns per CTA
 constexpr uint32_t kTcH1Col = 256;                  // first TMEM column of h1
-constexpr uint64_t kTcWaitNs = 1000000000ull;       // 1 s per wait: far beyond any MMA or copy
+constexpr uint64_t kTcWaitNs = 1000000000ull;       // default: 1 s per wait, far beyond any MMA or copy
 constexpr size_t kTcSmemLimit = 232448 - 1024;      // opt-in shared memory per CTA, less the static part
 
 struct MlpTcArgs {
@@ -325,6 +325,7 @@ struct MlpTcArgs {
   float const* b3;
   float* out;  // [n][2]
   int* error;
+  uint64_t wait_ns;  // bound on every mbarrier wait
 };
 
 // dynamic shared memory: the X tile, b1, b2, W3 (FP32), two buffers of
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
       int st = 0, u = 0;
       uint32_t use = 0;
       for (; g < total; ++g) {
-        if (use > 0 && !tc::mbar_wait(&empty[st], (use - 1) & 1, kTcWaitNs)) {
+        if (use > 0 && !tc::mbar_wait(&empty[st], (use - 1) & 1, p.wait_ns)) {
           abort_flag = 1;
           break;
         }
@@ -463,7 +464,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
       }
       // never leave with copies in flight: wait for the last stages to land
       for (int64_t h = g > S ? g - S : 0; h < g; ++h)
-        if (!tc::mbar_wait(&full[h % S], (uint32_t)(h / S) & 1, kTcWaitNs)) abort_flag = 1;
+        if (!tc::mbar_wait(&full[h % S], (uint32_t)(h / S) & 1, p.wait_ns)) abort_flag = 1;
     }
     __syncwarp();
   } else if (warp == kTcEpiWarps + 1) {
@@ -476,7 +477,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
     uint32_t sph = 0;    // parity of that stage's current use
     int64_t u = 0;       // accumulator use
     auto take = [&]() {  // wait for the next job's stage to land
-      bool const r = tc::mbar_wait(&full[st], sph, kTcWaitNs);
+      bool const r = tc::mbar_wait(&full[st], sph, p.wait_ns);
       tc::fence_after_sync();
       return __all_sync(0xffffffffu, r);
     };
@@ -488,13 +489,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
       }
     };
     auto slot_free = [&](int64_t uu) {  // the epilogue has drained use uu - 2 of the slot
-      bool const r = uu < 2 || tc::mbar_wait(&acc_empty[uu & 1], (uint32_t)((uu >> 1) - 1) & 1, kTcWaitNs);
+      bool const r = uu < 2 || tc::mbar_wait(&acc_empty[uu & 1], (uint32_t)((uu >> 1) - 1) & 1, p.wait_ns);
       tc::fence_after_sync();
       return __all_sync(0xffffffffu, r);
     };
     for (int it = 0; it < my_tiles && ok; ++it) {
       uint32_t const par = (uint32_t)it & 1;
-      ok = __all_sync(0xffffffffu, tc::mbar_wait(&x_ready, par, kTcWaitNs) && !abort_flag);
+      ok = __all_sync(0xffffffffu, tc::mbar_wait(&x_ready, par, p.wait_ns) && !abort_flag);
       tc::fence_after_sync();
       // layer 1: block q of X W1^T
       for (int q = 0; q < blocks && ok; ++q, ++u) {
@@ -519,7 +520,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
         for (int kg = 0; kg < kjobs && ok; ++kg) {
           // K tiles kb = kg JT .. + JT - 1; h1 block b holds K tiles 2 b, 2 b + 1
           for (int b = (kg * JT) >> 1; q == 0 && ok && b <= (kg * JT + JT - 1) >> 1; ++b) {
-            ok = __all_sync(0xffffffffu, tc::mbar_wait(&h1_ready[b], par, kTcWaitNs) && !abort_flag);
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(&h1_ready[b], par, p.wait_ns) && !abort_flag);
             tc::fence_after_sync();
           }
           if (ok) ok = take();
@@ -547,7 +548,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
     if (tc::elect_one()) {
       if (!ok) abort_flag = 1;
       tc::mma_commit(&drain);
-      if (!tc::mbar_wait(&drain, 0, kTcWaitNs)) abort_flag = 1;
+      if (!tc::mbar_wait(&drain, 0, p.wait_ns)) abort_flag = 1;
     }
     __syncwarp();
   } else {
@@ -568,7 +569,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
     // wait for accumulator use uu and load this warp's 32 columns of it;
     // the slot is handed back as soon as the load has completed
     auto load_acc = [&](int64_t uu, float (&v)[32]) {
-      if (ok) ok = tc::mbar_wait(&acc_full[uu & 1], (uint32_t)(uu >> 1) & 1, kTcWaitNs) && !abort_flag;
+      if (ok) ok = tc::mbar_wait(&acc_full[uu & 1], (uint32_t)(uu >> 1) & 1, p.wait_ns) && !abort_flag;
       tc::fence_after_sync();
       __syncwarp();
       if (!ok) return false;
@@ -842,6 +843,7 @@ int forward_tc(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
   a.b3 = d.p.as<float>() + d.ob3;
   a.out = out;
   a.error = d.tc_error.as<int>();
+  a.wait_ns = device_wait_ns(kTcWaitNs);
   if (d.n_sm == 0) SED_TRY_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, d.device));
   uint64_t const tiles = (n + kTcRows - 1) / kTcRows;
   unsigned const grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)d.n_sm);  // persistent: one CTA per SM

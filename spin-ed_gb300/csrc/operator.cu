@@ -382,16 +382,41 @@ __device__ __forceinline__ void fix_add(int64_t (&acc)[NV], uint32_t t, int64_t 
   }
 }
 
-// The row's epilogue, shared by every fixed-point kernel so that all of them
-// round identically: y_i = d_i x_i + f_i sum_v c_v (acc_v 2^-F).
+// The row factors g[cls NV + v] = (c_v / sqrt(S_cls)) 2^-F, one table per
+// block in shared memory (one rounding of c_v / sqrt(S), then an exact power
+// of two unless the result is subnormal). Every thread of the block calls it;
+// the caller synchronises.
 template <int NV>
-__device__ __forceinline__ double fix_row(int64_t const (&acc)[NV], FixView const& fv, int64_t F, double dg,
-                                          double xi, double f) {
+__device__ __forceinline__ void fix_row_factors(FixView const& fv, double const* __restrict__ inv_sqrt_s, int64_t F,
+                                                double* g) {
+  for (uint32_t t = threadIdx.x; t < fv.n_div * NV; t += blockDim.x)
+    g[t] = F == kFixBad ? 0.0 : fix_ldexp(__dmul_rn(inv_sqrt_s[t / NV], fv.c[t % NV]), -F);
+}
+
+// The row's epilogue, shared by every fixed-point kernel so that all of them
+// round identically: y_i = d_i x_i + sum_v g[cls][v] acc_v, with g from
+// fix_row_factors (g points at the row's class).
+template <int NV>
+__device__ __forceinline__ double fix_row(int64_t const (&acc)[NV], double const* g, int64_t F, double dg, double xi) {
   if (F == kFixBad) return __longlong_as_double(0x7FF8000000000000ll);  // NaN in x gives NaN out
-  double sum = __dmul_rn(fv.c[0], fix_ldexp(__ll2double_rn(acc[0]), -F));
+  double s = __dmul_rn(dg, xi);
 #pragma unroll
-  for (int k = 1; k < NV; ++k) sum = __fma_rn(fv.c[k], fix_ldexp(__ll2double_rn(acc[k]), -F), sum);
-  return __dadd_rn(__dmul_rn(dg, xi), __dmul_rn(f, sum));
+  for (int k = 0; k < NV; ++k) s = __fma_rn(g[k], __ll2double_rn(acc[k]), s);
+  return s;
+}
+
+// Sum of one double per thread over the block, in a fixed order, through
+// shared memory (buf: blockDim.x doubles): the first warp adds eight values
+// per lane, then across lanes. The total is valid in thread 0.
+__device__ __forceinline__ double block_sum_fixed(double v, double* buf) {
+  buf[threadIdx.x] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x < 32) {
+    for (uint32_t q = threadIdx.x; q < blockDim.x; q += 32) s += buf[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  }
+  return s;
 }
 
 // Streamed SpMV over SELL-32 slices in fixed point (real operators). Four
@@ -403,17 +428,20 @@ __global__ void __launch_bounds__(kBlock) k_spmv_fix(StreamView S, FixView fv, u
                                                      double const* __restrict__ x, int64_t const* __restrict__ u,
                                                      int64_t const* __restrict__ F_in, double* __restrict__ y,
                                                      Indirect ind) {
-  extern __shared__ uint8_t code8[];
-  __shared__ double red[kBlock / 32];
+  extern __shared__ double fix_smem[];  // g[n_div NV], then code8[n_codes]
+  __shared__ double red[kBlock];
   if (ind.stop && *ind.stop) return;  // uniform across the grid
   if (ind.k) {
     uint64_t const k = *ind.k;
     x += k * ind.ld;
     y += (k + 1) * ind.ld;
   }
-  for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
-  __syncthreads();
   int64_t const F = F_in[0];
+  double* g = fix_smem;
+  uint8_t* code8 = reinterpret_cast<uint8_t*>(fix_smem + fv.n_div * NV);
+  for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
+  fix_row_factors<NV>(fv, S.inv_sqrt_s, F, g);
+  __syncthreads();
   uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t const s = i >> 5;
   double part = 0.0;
@@ -426,7 +454,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv_fix(StreamView S, FixView fv, u
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0;
     uint32_t const* ent = S.entries + base + lane;
-    constexpr uint32_t U = 4;
+    constexpr uint32_t U = 8;
     uint32_t e = 0;
     for (; e + U <= width; e += U) {
       uint32_t v[U];
@@ -456,15 +484,15 @@ __global__ void __launch_bounds__(kBlock) k_spmv_fix(StreamView S, FixView fv, u
       }
     }
     if (i < D) {
-      double const xi = x[i];
-      double const yi = fix_row<NV>(acc, fv, F, static_cast<double const*>(S.diag)[i], xi,
-                                    S.inv_sqrt_s[S.row_class[i]]);
-      y[i] = yi;
+      double const xi = __ldcs(x + i);
+      double const yi = fix_row<NV>(acc, g + (uint32_t)__ldcs(S.row_class + i) * NV, F,
+                                    __ldcs(static_cast<double const*>(S.diag) + i), xi);
+      __stcs(y + i, yi);
       part = xi * yi;
     }
   }
   if (ind.partial) {
-    double const tot = block_sum(part, red);
+    double const tot = block_sum_fixed(part, red);
     if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
   }
 }
@@ -476,8 +504,11 @@ __global__ void __launch_bounds__(kBlock) k_spmv_block_fix(StreamView S, FixView
                                                            int64_t const* __restrict__ u,
                                                            int64_t const* __restrict__ F_in, double* __restrict__ y,
                                                            uint64_t ldy) {
-  extern __shared__ uint8_t code8[];
+  extern __shared__ double fix_smem[];  // g[K][n_div NV], then code8[n_codes]
+  uint8_t* code8 = reinterpret_cast<uint8_t*>(fix_smem + K * fv.n_div * NV);
   for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
+#pragma unroll
+  for (int c = 0; c < K; ++c) fix_row_factors<NV>(fv, S.inv_sqrt_s, F_in[c], fix_smem + c * fv.n_div * NV);
   __syncthreads();
   uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t const s = i >> 5;
@@ -503,10 +534,12 @@ __global__ void __launch_bounds__(kBlock) k_spmv_block_fix(StreamView S, FixView
     }
   }
   if (i < D) {
-    double const f = S.inv_sqrt_s[S.row_class[i]];
+    uint32_t const cls = S.row_class[i];
     double const dg = static_cast<double const*>(S.diag)[i];
 #pragma unroll
-    for (int c = 0; c < K; ++c) y[(uint64_t)c * ldy + i] = fix_row<NV>(acc[c], fv, F_in[c], dg, x[(uint64_t)c * ldx + i], f);
+    for (int c = 0; c < K; ++c)
+      y[(uint64_t)c * ldy + i] =
+          fix_row<NV>(acc[c], fix_smem + (c * fv.n_div + cls) * NV, F_in[c], dg, x[(uint64_t)c * ldx + i]);
   }
 }
 
@@ -518,16 +551,19 @@ __global__ void __launch_bounds__(kBlock)
               uint32_t const* __restrict__ weights, FixView fv, double const* __restrict__ inv_sqrt_s,
               double const* __restrict__ x, int64_t const* __restrict__ u, int64_t const* __restrict__ F_in,
               double* __restrict__ y, Indirect ind) {
-  __shared__ double red[kBlock / 32];
+  __shared__ double red[kBlock];
+  __shared__ double g[kFixMaxClasses * NV];
   __shared__ uint16_t srow[2048];
   if (ind.stop && *ind.stop) return;
+  int64_t const F = F_in[0];
+  fix_row_factors<NV>(fv, inv_sqrt_s, F, g);
   RowTab const RT = stage_rows(P, srow);
+  __syncthreads();
   if (ind.k) {
     uint64_t const k = *ind.k;
     x += k * ind.ld;
     y += (k + 1) * ind.ld;
   }
-  int64_t const F = F_in[0];
   uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double part = 0.0;
   if (i < I.D) {
@@ -541,12 +577,12 @@ __global__ void __launch_bounds__(kBlock)
       if (j >= 0) fix_add<NV>(acc, vid << 1 | (c.phase != 0u ? 1u : 0u), u[(uint64_t)j]);
     });
     double const xi = x[i];
-    double const yi = fix_row<NV>(acc, fv, F, row_diag<double>(r, T), xi, inv_sqrt_s[divisor_class(weights[i], C)]);
+    double const yi = fix_row<NV>(acc, g + divisor_class(weights[i], C) * NV, F, row_diag<double>(r, T), xi);
     y[i] = yi;
     part = xi * yi;
   }
   if (ind.partial) {
-    double const tot = block_sum(part, red);
+    double const tot = block_sum_fixed(part, red);
     if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
   }
 }
@@ -1352,7 +1388,7 @@ void launch_spmv_fix(OperatorData& op, StreamView const& S, double const* x, int
   StreamForm const& sf = op.stream;
   OperatorTables const& tb = *op.tables;
   unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
-  size_t const smem = tb.fix.n_codes;
+  size_t const smem = (size_t)tb.fix.n_div * NV * 8 + tb.fix.n_codes;
   if (sf.packed) k_spmv_fix<true, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, op.basis->D, x, u, F, y, ind);
   else k_spmv_fix<false, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, op.basis->D, x, u, F, y, ind);
   note_launches(1);
@@ -1383,12 +1419,14 @@ int launch_apply_fix(OperatorData& op, double const* x, double* y, cudaStream_t 
   int64_t* u = op.fix_u.as<int64_t>();
   bool const ordered = ind.k == nullptr;
   if (ordered && op.fix_event_recorded) SED_TRY_CUDA(cudaStreamWaitEvent(stream, op.fix_event, 0));
-  SED_TRY_CUDA(cudaMemsetAsync(mx, 0, 8, stream));
-  unsigned const vg = grid_size(D, b.device, 8);
-  k_fix_max<<<vg, kBlock, 0, stream>>>(x, 0, D, mx, ind);
-  k_fix_convert<<<vg, kBlock, 0, stream>>>(x, 0, D, use_stream ? op.stream.row_class.as<uint8_t>() : nullptr,
-                                           b.weights.as<uint32_t>(), tb.code, tb.fix, mx, F, u, D, ind);
-  note_launches(2);
+  if (!ind.prescaled) {
+    SED_TRY_CUDA(cudaMemsetAsync(mx, 0, 8, stream));
+    unsigned const vg = grid_size(D, b.device, 8);
+    k_fix_max<<<vg, kBlock, 0, stream>>>(x, 0, D, mx, ind);
+    k_fix_convert<<<vg, kBlock, 0, stream>>>(x, 0, D, use_stream ? op.stream.row_class.as<uint8_t>() : nullptr,
+                                             b.weights.as<uint32_t>(), tb.code, tb.fix, mx, F, u, D, ind);
+    note_launches(2);
+  }
   if (use_stream) {
     StreamView const S = stream_view(op);
     switch (tb.fix_nv) {
@@ -1416,6 +1454,36 @@ int launch_apply_fix(OperatorData& op, double const* x, double* y, cudaStream_t 
   }
   return LS_SUCCESS;
 }
+
+}  // namespace
+
+bool fix_slots(OperatorData& op, FixSlots* out) {
+  if (!op.tables || !op.tables->fix_ok || op.fix_cols < 1 || !op.stream.ready || op.form == SED_FORM_ON_THE_FLY)
+    return false;
+  auto* mx = op.fix_slots.as<unsigned long long>();
+  out->max_bits = mx;
+  out->F = reinterpret_cast<int64_t*>(mx + op.fix_cols);
+  out->u = op.fix_u.as<int64_t>();
+  out->row_class = op.stream.row_class.as<uint8_t>();
+  out->view = op.tables->fix;
+  return true;
+}
+
+int fix_prescale(OperatorData& op, double const* base, Indirect ind, cudaStream_t stream) {
+  FixSlots fs;
+  if (!fix_slots(op, &fs)) return fail(LS_SYSTEM_ERROR, "fix_prescale: the operator has no fixed-point form");
+  BasisData& b = *op.basis;
+  SED_TRY_CUDA(cudaMemsetAsync(fs.max_bits, 0, 8, stream));
+  unsigned const vg = grid_size(b.D, b.device, 8);
+  k_fix_max<<<vg, kBlock, 0, stream>>>(base, 0, b.D, fs.max_bits, ind);
+  k_fix_convert<<<vg, kBlock, 0, stream>>>(base, 0, b.D, fs.row_class, b.weights.as<uint32_t>(), op.tables->code,
+                                           fs.view, fs.max_bits, fs.F, fs.u, b.D, ind);
+  note_launches(2);
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
+namespace {
 
 template <class X>
 int launch_apply(OperatorData& op, X const* x, X* y, cudaStream_t stream, bool use_stream,
@@ -1526,7 +1594,8 @@ int launch_block_fix(OperatorData& op, unsigned K, double const* x, uint64_t ldx
   note_launches(2);
   StreamView const S = stream_view(op);
   unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
-  size_t const smem = tb.fix.n_codes;
+  size_t const smem = (size_t)K * tb.fix.n_div * tb.fix_nv * 8 + tb.fix.n_codes;
+  if (smem > 48 * 1024) return fail(LS_SYSTEM_ERROR, "fixed-point block matvec: tables exceed shared memory");
   switch (tb.fix_nv * 2 + (sf.packed ? 1 : 0)) {
     case 3: launch_block_fix_k<1, true>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
     case 2: launch_block_fix_k<1, false>(K, S, tb.fix, D, x, ldx, u, F, y, ldy, grid, smem, stream); break;
@@ -1585,10 +1654,19 @@ int operator_apply_device(OperatorData& op, int dtype, uint64_t block, void cons
   }
   size_t const es = (size_t)elem_size(dtype);
   uint64_t c0 = 0;
-  if (use_stream && block > 1) {
+  // the fixed-point block kernel keeps K tables of row factors in shared
+  // memory: at most kmax columns per pass fit in 48 KB
+  unsigned kmax = 16;
+  if (dtype == 1 && op.tables->fix_ok) {
+    size_t const per = (size_t)op.tables->fix.n_div * op.tables->fix_nv * 8;
+    size_t const room = 48 * 1024 - op.tables->fix.n_codes;
+    kmax = (unsigned)std::min<size_t>(16, room / per);
+  }
+  if (use_stream && block > 1 && kmax >= 2) {
     // K-column passes over the stream form (K = 16, 8, 4, 2)
     while (block - c0 >= 2) {
-      unsigned const K = block - c0 >= 16 ? 16 : block - c0 >= 8 ? 8 : block - c0 >= 4 ? 4 : 2;
+      uint64_t const left = std::min<uint64_t>(block - c0, kmax);
+      unsigned const K = left >= 16 ? 16 : left >= 8 ? 8 : left >= 4 ? 4 : 2;
       void const* xc = static_cast<char const*>(x) + c0 * ldx * es;
       void* yc = static_cast<char*>(y) + c0 * ldy * es;
       int st;
@@ -1751,7 +1829,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv32_fix(StreamView S, FixView fv,
                                                        float const* __restrict__ x, int32_t const* __restrict__ u,
                                                        int64_t const* __restrict__ F_in, float* __restrict__ y,
                                                        Indirect ind) {
-  extern __shared__ uint8_t code8[];
+  extern __shared__ double fix_smem[];  // g[n_div NV], then code8[n_codes]
   __shared__ double red[kBlock / 32];
   if (ind.stop && *ind.stop) return;
   if (ind.k) {
@@ -1759,12 +1837,15 @@ __global__ void __launch_bounds__(kBlock) k_spmv32_fix(StreamView S, FixView fv,
     x += k * ind.ld;
     y += (k + 1) * ind.ld;
   }
-  for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
-  __syncthreads();
   int64_t const F = F_in[0];
+  double* g = fix_smem;
+  uint8_t* code8 = reinterpret_cast<uint8_t*>(fix_smem + fv.n_div * NV);
+  for (uint32_t c = threadIdx.x; c < fv.n_codes; c += blockDim.x) code8[c] = fv.code[c];
+  fix_row_factors<NV>(fv, S.inv_sqrt_s, F, g);
+  __syncthreads();
   uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t const s = i >> 5;
-  double part = 0.0;
+  float part = 0.0f;
   if ((s << 5) < D) {
     uint32_t const lane = threadIdx.x & 31;
     uint64_t const base = S.slice_ptr[s];
@@ -1774,27 +1855,27 @@ __global__ void __launch_bounds__(kBlock) k_spmv32_fix(StreamView S, FixView fv,
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0;
     uint32_t const* ent = S.entries + base + lane;
-    constexpr uint32_t U = 4;
+    constexpr uint32_t U = 8;
     uint32_t e = 0;
     for (; e + U <= width; e += U) {
       uint32_t v[U];
 #pragma unroll
       for (uint32_t q = 0; q < U; ++q) v[q] = __ldcs(ent + (uint64_t)(e + q) * 32);
-      int32_t g[U];
+      int32_t gv[U];
       uint32_t t[U];
 #pragma unroll
       for (uint32_t q = 0; q < U; ++q) {
-        g[q] = 0;
+        gv[q] = 0;
         t[q] = 0;
         if (v[q] != kNull) {
           uint32_t const code =
               Packed ? (v[q] >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)(e + q) * 32);
-          g[q] = u[v[q] & col_mask];
+          gv[q] = u[v[q] & col_mask];
           t[q] = code8[code];
         }
       }
 #pragma unroll
-      for (uint32_t q = 0; q < U; ++q) fix_add<NV>(acc, t[q], (int64_t)g[q]);
+      for (uint32_t q = 0; q < U; ++q) fix_add<NV>(acc, t[q], (int64_t)gv[q]);
     }
     for (; e < width; ++e) {
       uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
@@ -1804,17 +1885,25 @@ __global__ void __launch_bounds__(kBlock) k_spmv32_fix(StreamView S, FixView fv,
       }
     }
     if (i < D) {
-      double const xi = (double)x[i];
-      double const yi = fix_row<NV>(acc, fv, F, static_cast<double const*>(S.diag)[i], xi,
-                                    S.inv_sqrt_s[S.row_class[i]]);
+      float const xf = __ldcs(x + i);
+      double const yi = fix_row<NV>(acc, g + (uint32_t)__ldcs(S.row_class + i) * NV, F,
+                                    __ldcs(static_cast<double const*>(S.diag) + i), (double)xf);
       float const yf = (float)yi;
-      y[i] = yf;
-      part = xi * (double)yf;
+      __stcs(y + i, yf);
+      part = xf * yf;
     }
   }
   if (ind.partial) {
-    double const tot = block_sum(part, red);
-    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
+    // the product of the stored FP32 values summed per warp in FP32, then
+    // per block in FP64 (fixed order)
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.0;
+      for (unsigned w = 0; w < kBlock / 32; ++w) tot += red[w];
+      ind.partial[blockIdx.x] = tot;
+    }
   }
 }
 
@@ -1851,7 +1940,7 @@ void launch_spmv32_fix(OperatorData& op, StreamView const& S, float const* x, fl
   auto* F = reinterpret_cast<int64_t*>(slots + 1);
   int32_t* u = op.fix_u32.as<int32_t>();
   uint64_t const D = op.basis->D;
-  size_t const smem = tb.fix.n_codes;
+  size_t const smem = (size_t)tb.fix.n_div * NV * 8 + tb.fix.n_codes;
   if (op.stream.packed)
     k_spmv32_fix<true, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, D, x, u, F, y, ind);
   else
@@ -2130,6 +2219,59 @@ void sed_set_record_mode(int mode) {
 
 int sed_operator_recorded_with_table(ls_operator const* op) {
   return op && op->d->stream.ready && op->d->stream.orbit_table ? 1 : 0;
+}
+
+int sed_operator_time_matvec(ls_operator const* op, void const* x, void* y, unsigned repetitions,
+                             double* ms_matvec, double* ms_kernel) {
+  if (!op || !x || !y || !ms_matvec || !ms_kernel || repetitions == 0)
+    return fail(LS_INVALID_ARGUMENT, "sed_operator_time_matvec: bad argument");
+  OperatorData& d = *op->d;
+  std::lock_guard<std::mutex> lock(d.mu);
+  if (!d.is_real) return fail(LS_OPERATOR_IS_COMPLEX, "sed_operator_time_matvec: real operators only");
+  try {
+    ScopedDevice dev(d.basis->device);
+    if (int st = operator_ensure_ready(d)) return st;
+    if (!is_device_pointer(x) || !is_device_pointer(y))
+      return fail(LS_INVALID_ARGUMENT, "sed_operator_time_matvec: x and y must be device memory");
+    if (int st = wait_for_caller({x, y})) return st;
+    if (int st = fix_wait(d)) return st;
+    cudaStream_t s = d.cuda_stream;
+    double const* xd = static_cast<double const*>(x);
+    double* yd = static_cast<double*>(y);
+    bool const use_stream = d.stream.ready && d.form != SED_FORM_ON_THE_FLY;
+    cudaEvent_t e0, e1;
+    SED_TRY_CUDA(cudaEventCreate(&e0));
+    SED_TRY_CUDA(cudaEventCreate(&e1));
+    struct EvGuard {
+      cudaEvent_t a, b;
+      ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } eg{e0, e1};
+    auto timed = [&](bool kernel_only, double* out) -> int {
+      for (unsigned r = 0; r < repetitions + 2; ++r) {
+        if (r == 2) SED_TRY_CUDA(cudaEventRecord(e0, s));
+        Indirect ind;
+        ind.prescaled = kernel_only;
+        if (int st = launch_apply<double>(d, xd, yd, s, use_stream, ind)) return st;
+      }
+      SED_TRY_CUDA(cudaEventRecord(e1, s));
+      SED_TRY_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      SED_TRY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      *out = ms / repetitions;
+      return LS_SUCCESS;
+    };
+    if (int st = timed(false, ms_matvec)) return st;  // leaves u and F of x in the workspace
+    FixSlots fs;
+    if (fix_slots(d, &fs)) {
+      if (int st = timed(true, ms_kernel)) return st;
+    } else {
+      *ms_kernel = *ms_matvec;
+    }
+    SED_TRY_CUDA(cudaStreamSynchronize(s));
+    return LS_SUCCESS;
+  } catch (std::exception const& e) {
+    return fail(LS_SYSTEM_ERROR, e.what());
+  }
 }
 
 int sed_operator_prepare(ls_operator* op, int form) {

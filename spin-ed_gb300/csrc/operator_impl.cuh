@@ -270,6 +270,22 @@ __device__ __forceinline__ void const* stage_table(StreamView const& S, unsigned
 }
 
 StreamView stream_view(OperatorData const& op);
+
+// The fixed-point workspace of an operator (column 0), for kernels that
+// prepare u and F themselves.
+struct FixSlots {
+  unsigned long long* max_bits;  // max |x| bit pattern (zero before use)
+  int64_t* F;
+  int64_t* u;
+  uint8_t const* row_class;
+  FixView view;
+};
+// True (and *out filled) when the FP64 matvec of `op` runs in fixed point
+// through the stream form.
+bool fix_slots(OperatorData& op, FixSlots* out);
+// The matvec's pre-pass on its own: max |x|, then u and F, for x = base (+ k
+// ld in Krylov mode).
+int fix_prescale(OperatorData& op, double const* base, Indirect ind, cudaStream_t stream);
 // FP32 streamed SpMV in Krylov-indirect mode (x = base + k ld, y = base +
 // (k+1) ld); FP32 arithmetic, per-block partial sums of x_i y_i in FP64.
 int operator_apply_krylov32(OperatorData& op, float* base, Indirect ind, cudaStream_t stream,

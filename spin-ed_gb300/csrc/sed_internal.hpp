@@ -254,6 +254,13 @@ extern int g_record_mode;
 int solve_thick(OperatorData& op, int out_dtype, sed_eigh_options const& o, double* evals, void* evecs, uint64_t ldv,
                 double* rnorms, sed_eigh_info* info);
 
+// Bound on device-side waits (sed_set_device_wait_limit): the caller's
+// limit in nanoseconds, or `default_ns` when none is set.
+uint64_t device_wait_ns(uint64_t default_ns);
+// Extra arrivals each batched group barrier waits for (0 in normal use; a
+// test sets it so that the bounded barrier wait runs out).
+extern std::atomic<uint32_t> g_barrier_extra_arrivals;
+
 // Kernel-launch accounting (sed_kernel_launches): every launch site calls
 // note_launches(1); launches made while capturing a graph are not counted,
 // the graph's kernel nodes are counted at each replay instead.

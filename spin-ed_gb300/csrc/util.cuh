@@ -107,6 +107,9 @@ struct Indirect {
   uint32_t const* stop = nullptr;
   uint64_t ld = 0;
   double* partial = nullptr;
+  // fixed-point matvec: u and F of x were written by the step that produced
+  // x (Lanczos' scale kernel), so the matvec skips its own pre-pass
+  bool prescaled = false;
 };
 
 inline unsigned grid_size(uint64_t work, int device, unsigned per_sm = 16, unsigned block = kBlock) {

@@ -149,6 +149,11 @@ SIGNATURES = [
     ("sed_mlp_start_vector", _I, [_P, _P, _P]),
     ("sed_mlp_set_path", _I, [_P, _I]),
     ("sed_release_workspace", None, []),
+    ("sed_operator_time_matvec", _I, [_P, _P, _P, C.c_uint, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("sed_set_device_memory_limit", None, [_U64]),
+    ("sed_device_memory_in_use", _U64, []),
+    ("sed_set_device_wait_limit", None, [C.c_double]),
+    ("sed_debug_barrier_extra_arrivals", None, [C.c_uint]),
     ("sed_set_record_mode", None, [_I]),
     ("sed_operator_recorded_with_table", _I, [_P]),
     ("sed_mlp_uses_tensor_cores", _I, [_P]),
