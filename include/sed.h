@@ -300,6 +300,26 @@ SED_API int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, u
                                              uint64_t block_size, void const* x, uint64_t x_stride,
                                              void* y, uint64_t y_stride, void* out, void* stream);
 
+/* V[:, 0..kk) <- V[:, 0..m) Y in place: the basis rotation of a thick
+ * restart (Ritz vectors replacing the first kk Krylov vectors). No
+ * counterpart in the reference (PRIMME's restart is internal to it,
+ * src/SpinED.hs:404). V is FP64, D x m column-major with stride ld >= D; Y
+ * is m x kk row-major FP64; both device memory, 1 <= kk <= m <= 32. Paths:
+ * SED_ROTATE_TENSOR runs it on the tensor cores (kk <= 16) by an error-free
+ * split of both operands into 8-bit slices held exactly in BF16, FP32
+ * accumulation in tensor memory that is exact for these slices, and integer
+ * recombination (the result differs from an FP64 product by the truncation
+ * of each operand to 56 bits below its row or column maximum and the final
+ * rounding); SED_ROTATE_FP64 uses FP64 FMAs on the CUDA cores;
+ * SED_ROTATE_AUTO takes the tensor cores when the shape allows. The work is
+ * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream)
+ * and the call waits for it. sed_set_rotate_path selects the path of the
+ * rotation inside sed_eigh's thick-restart solver (process-wide). */
+enum { SED_ROTATE_AUTO = 0, SED_ROTATE_FP64 = 1, SED_ROTATE_TENSOR = 2 };
+SED_API int sed_rotate_vectors(double* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk, uint64_t D,
+                               int path, void* stream);
+SED_API void sed_set_rotate_path(int path);
+
 /* Many Hamiltonians in one persistent launch. No counterpart in the
  * reference, which solves one operator per run. The lowest opts->nev (<= 4)
  * eigenpairs of every operator by block Lanczos with block size 4 in FP64

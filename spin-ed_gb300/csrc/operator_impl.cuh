@@ -298,4 +298,13 @@ int operator_apply_krylov(OperatorData& op, int dtype, void* base, Indirect ind,
                           unsigned* blocks);
 int operator_ensure_ready(OperatorData& op);
 
+// V[:, 0..kk) <- V[:, 0..m) Y on the tensor cores (rotate_tc.cu): V FP64,
+// D x m with column stride ld, Y m x kk row-major FP64, both on the device;
+// *error_flag (device int) is set to 1 if a bounded wait ran out.
+bool rotate_tc_eligible(uint32_t m, uint32_t kk);
+int rotate_tc(double* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk, uint64_t D, cudaStream_t stream,
+              int* error_flag);
+// Path of the thick restart's basis rotation (sed_set_rotate_path).
+extern int g_rotate_path;
+
 }  // namespace sed

@@ -172,6 +172,31 @@ void launch_trotate(S* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk,
   }
 }
 
+// V[:, 0..kk) <- V[:, 0..m) Y: on the tensor cores for FP64 storage when
+// the shape allows it (and the path setting does not forbid it), else the
+// FP64-FMA kernel above. `err` is a device int for the tensor-core kernel's
+// bounded waits; a set flag is reported as LS_DEVICE_TIMEOUT.
+template <class S>
+int rotate_basis(S* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk, uint64_t D, unsigned vb,
+                 cudaStream_t stream, int path, int* err) {
+  if constexpr (std::is_same<S, double>::value) {
+    if (path != SED_ROTATE_FP64 && rotate_tc_eligible(m, kk)) {
+      SED_TRY_CUDA(cudaMemsetAsync(err, 0, 4, stream));
+      if (int st = rotate_tc(V, ld, m, Y, kk, D, stream, err)) return st;
+      int h = 0;
+      SED_TRY_CUDA(cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, stream));
+      SED_TRY_CUDA(cudaStreamSynchronize(stream));
+      if (h) return fail(LS_DEVICE_TIMEOUT, "basis rotation: a wait on the tensor cores timed out");
+      return LS_SUCCESS;
+    }
+  }
+  if (path == SED_ROTATE_TENSOR)
+    return fail(LS_INVALID_ARGUMENT, "basis rotation on the tensor cores needs FP64, m <= 32 and kk <= 16");
+  launch_trotate<S>(V, ld, m, Y, kk, D, vb, stream);
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
 // psi = sum_{i < m} V[:, i] y[i]  (FP64 output)
 template <class S>
 __global__ void k_tritz(S const* __restrict__ V, uint64_t ld, uint32_t m, double const* __restrict__ yv, uint64_t D,
@@ -321,7 +346,8 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
   int const dev = op.basis->device;
   unsigned const vb = grid_size(D, dev, 4);
   uint32_t const groups = (m + 1 + kDotCols - 1) / kDotCols;
-  DeviceBuffer Vb, wb, w64, part, coef, Yb;
+  DeviceBuffer Vb, wb, w64, part, coef, Yb, rt_err;
+  if (int st = rt_err.allocate(4)) return st;
   if (int st = Vb.allocate((size_t)(m + 1) * D * sizeof(S))) return st;
   if (int st = wb.allocate(D * sizeof(S))) return st;
   if (int st = w64.allocate(D * 8)) return st;
@@ -470,7 +496,8 @@ int thick_run(OperatorData& op, cudaStream_t stream, uint32_t m, uint32_t nev, d
       for (uint32_t q = 0; q < n; ++q)
         for (uint32_t cidx = 0; cidx < keep; ++cidx) Y[(size_t)q * keep + cidx] = Z[(size_t)q * n + cidx];
       SED_TRY_CUDA(cudaMemcpyAsync(Yb.ptr, Y.data(), Y.size() * 8, cudaMemcpyHostToDevice, stream));
-      launch_trotate<S>(V, D, n, Yb.as<double>(), keep, D, vb, stream);
+      if (int st = rotate_basis<S>(V, D, n, Yb.as<double>(), keep, D, vb, stream, g_rotate_path, rt_err.as<int>()))
+        return st;
       if (breakdown) {
         // no continuation vector: a fresh random direction, orthogonalised
         { k_trandom<S><<<vb, 256, 0, stream>>>(V + (uint64_t)keep * D, D, seed + 7919 * (out.restarts + 1)); note_launches(1); }
@@ -586,3 +613,33 @@ int solve_thick(OperatorData& op, int out_dtype, sed_eigh_options const& o, doub
 }
 
 }  // namespace sed
+
+using namespace sed;
+
+extern "C" {
+
+void sed_set_rotate_path(int path) {
+  g_rotate_path = (path == SED_ROTATE_FP64 || path == SED_ROTATE_TENSOR) ? path : SED_ROTATE_AUTO;
+}
+
+int sed_rotate_vectors(double* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk, uint64_t D, int path,
+                       void* stream) {
+  if (!V || !Y || m == 0 || kk == 0 || kk > m || m > (uint32_t)kMaxThick || (D && ld < D))
+    return fail(LS_INVALID_ARGUMENT, "sed_rotate_vectors: needs 1 <= kk <= m <= 32, ld >= D and device pointers");
+  if (path < SED_ROTATE_AUTO || path > SED_ROTATE_TENSOR) return fail(LS_INVALID_ARGUMENT, "sed_rotate_vectors: bad path");
+  if (D == 0) return LS_SUCCESS;
+  try {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int dev = 0;
+    SED_TRY_CUDA(cudaGetDevice(&dev));
+    DeviceBuffer err;
+    if (int st = err.allocate(4)) return st;
+    if (int st = rotate_basis<double>(V, ld, m, Y, kk, D, grid_size(D, dev, 4), s, path, err.as<int>())) return st;
+    SED_TRY_CUDA(cudaStreamSynchronize(s));
+    return LS_SUCCESS;
+  } catch (std::exception const& e) {
+    return fail(LS_SYSTEM_ERROR, e.what());
+  }
+}
+
+}  // extern "C"

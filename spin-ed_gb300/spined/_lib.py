@@ -36,6 +36,7 @@ LS_DEVICE_TIMEOUT = 23
 
 SED_FORM_AUTO, SED_FORM_STREAM, SED_FORM_ON_THE_FLY = 0, 1, 2
 SED_PRECISION_FP64, SED_PRECISION_MIXED = 0, 1
+SED_ROTATE_AUTO, SED_ROTATE_FP64, SED_ROTATE_TENSOR = 0, 1, 2
 SED_START_RANDOM, SED_START_GIVEN = 0, 1
 SED_MLP_PATH_AUTO, SED_MLP_PATH_SIMT = 0, 1
 SED_RECORD_AUTO, SED_RECORD_CANONICALISE = 0, 1
@@ -149,6 +150,8 @@ SIGNATURES = [
     ("sed_mlp_start_vector", _I, [_P, _P, _P]),
     ("sed_mlp_set_path", _I, [_P, _I]),
     ("sed_release_workspace", None, []),
+    ("sed_rotate_vectors", _I, [_P, _U64, C.c_uint32, _P, C.c_uint32, _U64, _I, _P]),
+    ("sed_set_rotate_path", None, [_I]),
     ("sed_operator_time_matvec", _I, [_P, _P, _P, C.c_uint, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("sed_set_device_memory_limit", None, [_U64]),
     ("sed_device_memory_in_use", _U64, []),
