@@ -594,10 +594,12 @@ def main():
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
     ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
     ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
-    ap.add_argument("--profile-case", default=None, choices=["mlp", "batch16", "spmv"],
+    ap.add_argument("--profile-case", default=None, choices=["mlp", "batch16", "spmv", "rotate"],
                     help="one small run of a single kernel family, for profilers: the tensor-core MLP "
-                         "inference over 2^20 random 36-spin states, a 16-chain batched solve, or 10 "
-                         "matvecs of the 6x6 stream form (about 3.5 GB on the device)")
+                         "inference over 2^20 random 36-spin states, a 16-chain batched solve, 10 "
+                         "matvecs of the 6x6 stream form (about 3.5 GB on the device), or the thick-restart "
+                         "basis rotation on 1e8 rows on both paths (--rotate-rows to change)")
+    ap.add_argument("--rotate-rows", type=int, default=100_000_000)
     args = ap.parse_args()
     args.precision_code = 0 if args.precision == "fp64" else 1
     rank = int(os.environ.get("RANK", "0"))
@@ -637,6 +639,37 @@ def main():
             I.inplace_apply(op, x, y)
         torch.cuda.synchronize()
         print(json.dumps({"case": "spmv", "D": D, "elements": op.stream_elements, "y_norm": float(y.norm())}))
+        return
+    if args.profile_case == "rotate":
+        from spined import _lib as L
+        lib = L.load()
+        D = args.rotate_rows
+        out = {"case": "rotate", "rows": D}
+        for m, kk in ((12, 6), (32, 16)):
+            V = torch.randn(m, D, dtype=torch.float64, device="cuda")  # column-major D x m, ld = D
+            Y = torch.randn(m, kk, dtype=torch.float64, device="cuda")
+            s = torch.cuda.current_stream()
+            for path, name in ((L.SED_ROTATE_FP64, "fp64"), (L.SED_ROTATE_TENSOR, "tensor")):
+                for _ in range(2):  # warm-up
+                    I_st = lib.sed_rotate_vectors(C.c_void_p(V.data_ptr()), D, m, C.c_void_p(Y.data_ptr()), kk, D,
+                                                  path, C.c_void_p(s.cuda_stream))
+                    assert I_st == 0, L.error_message(I_st)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                for _ in range(3):
+                    lib.sed_rotate_vectors(C.c_void_p(V.data_ptr()), D, m, C.c_void_p(Y.data_ptr()), kk, D, path,
+                                           C.c_void_p(s.cuda_stream))
+                e1.record(s)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / 3
+                bytes_moved = D * (m + kk) * 8
+                out[f"m{m}_k{kk}_{name}_ms"] = ms
+                out[f"m{m}_k{kk}_{name}_GBps"] = bytes_moved / (ms * 1e-3) / 1e9
+                out[f"m{m}_k{kk}_{name}_TFMAps"] = D * m * kk / (ms * 1e-3) / 1e12
+                V.normal_()  # keep the values finite and O(1) for the next path
+            del V, Y
+            torch.cuda.empty_cache()
+        print(json.dumps(out))
         return
     if args.profile_case == "batch16":
         from spined import internal as I, lattices

@@ -382,23 +382,33 @@ __device__ __forceinline__ void fix_add(int64_t (&acc)[NV], uint32_t t, int64_t 
   }
 }
 
-// The row factors g[cls NV + v] = (c_v / sqrt(S_cls)) 2^-F, one table per
-// block in shared memory (one rounding of c_v / sqrt(S), then an exact power
-// of two unless the result is subnormal). Every thread of the block calls it;
-// the caller synchronises.
+// The row factors g[cls NV + v] = (c_v / sqrt(S_cls)) 2^-min(F, 1000), one
+// table per block in shared memory (one rounding of c_v / sqrt(S), then an
+// exact power of two). F above 1000 only occurs for vectors whose largest
+// entry is below about 1e-290; the rest of the scaling is then applied by
+// fix_row after the sum, so that g stays a normal number. Every thread of
+// the block calls it; the caller synchronises.
 template <int NV>
 __device__ __forceinline__ void fix_row_factors(FixView const& fv, double const* __restrict__ inv_sqrt_s, int64_t F,
                                                 double* g) {
+  int64_t const Fa = F > 1000 ? 1000 : F;
   for (uint32_t t = threadIdx.x; t < fv.n_div * NV; t += blockDim.x)
-    g[t] = F == kFixBad ? 0.0 : fix_ldexp(__dmul_rn(inv_sqrt_s[t / NV], fv.c[t % NV]), -F);
+    g[t] = F == kFixBad ? 0.0 : fix_ldexp(__dmul_rn(inv_sqrt_s[t / NV], fv.c[t % NV]), -Fa);
 }
 
 // The row's epilogue, shared by every fixed-point kernel so that all of them
-// round identically: y_i = d_i x_i + sum_v g[cls][v] acc_v, with g from
-// fix_row_factors (g points at the row's class).
+// round identically: y_i = d_i x_i + sum_v g[cls][v] acc_v (times
+// 2^-(F - 1000) when F > 1000), with g from fix_row_factors (g points at the
+// row's class).
 template <int NV>
 __device__ __forceinline__ double fix_row(int64_t const (&acc)[NV], double const* g, int64_t F, double dg, double xi) {
   if (F == kFixBad) return __longlong_as_double(0x7FF8000000000000ll);  // NaN in x gives NaN out
+  if (F > 1000) {
+    double o = 0.0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) o = __fma_rn(g[k], __ll2double_rn(acc[k]), o);
+    return __fma_rn(o, fix_pow2(1000 - F), __dmul_rn(dg, xi));
+  }
   double s = __dmul_rn(dg, xi);
 #pragma unroll
   for (int k = 0; k < NV; ++k) s = __fma_rn(g[k], __ll2double_rn(acc[k]), s);
