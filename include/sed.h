@@ -349,6 +349,12 @@ typedef struct sed_batch_info {
 SED_API int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options const* opts,
                              double* eigenvalues, double* residuals, void* const eigenvectors[],
                              uint64_t const ldv[], sed_batch_info* info);
+/* Fixes the launch shape of sed_eigh_batched instead of tuning it: 128 or
+ * 256 threads per CTA and 1 to 3 CTAs per SM (a shape that is not
+ * co-resident on the device makes sed_eigh_batched fail with
+ * LS_INVALID_ARGUMENT). threads_per_cta = 0 returns to tuning, which times
+ * every such shape on a short trial run. Process-wide. */
+SED_API void sed_set_batched_launch(unsigned threads_per_cta, unsigned ctas_per_sm);
 
 /* Norms ||P r|| = sqrt(S / |G|) of the representatives (host array). */
 SED_API int sed_basis_get_norms(ls_spin_basis const* basis, double* out);

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -797,6 +798,9 @@ struct Plan {
   unsigned threads = 256, ctas_per_sm = 1;
 };
 
+// Caller's fixed launch shape (sed_set_batched_launch); threads == 0: tune.
+std::atomic<unsigned> g_force_threads{0}, g_force_per_sm{0};
+
 std::mutex g_tune_mu;
 std::map<std::tuple<int, unsigned, uint64_t>, Plan> g_tuned;
 
@@ -855,8 +859,12 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
   SED_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
   if (!coop) return fail(LS_CUDA_ERROR, "sed_eigh_batched: device lacks cooperative launch");
   SED_TRY_CUDA(cudaFuncSetAttribute(k_batch_lanczos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem()));
-  int max_per_sm = 0;
-  SED_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, k_batch_lanczos, 256, dyn_smem()));
+  // co-resident CTAs per SM for each block size (the cooperative launch
+  // needs the whole grid resident)
+  int occ128 = 0, occ256 = 0;
+  SED_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ128, k_batch_lanczos, 128, dyn_smem()));
+  SED_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ256, k_batch_lanczos, 256, dyn_smem()));
+  int const max_per_sm = std::min(3, std::max(occ128, occ256));
   if (max_per_sm < 1) return fail(LS_CUDA_ERROR, "sed_eigh_batched: kernel does not fit on an SM");
 
   // work model per problem: streamed bytes of a block matvec plus the FP64
@@ -890,16 +898,29 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     off_out[i] = take(kOutBytes);
   }
 
-  // Candidate launch shapes; the autotuner times each on a short trial (two
-  // block steps of every problem) and keeps the fastest per (device, count, size).
+  // Candidate launch shapes: 128 or 256 threads per CTA, 1 to 3 CTAs per SM
+  // (as many as stay co-resident); the autotuner times each on a short trial
+  // (two block steps of every problem) and keeps the fastest per (device,
+  // count, size). A caller-fixed shape replaces the candidates.
   std::vector<Plan> cands;
-  for (unsigned per = 1; per <= (unsigned)std::min(max_per_sm, 2); ++per) cands.push_back(Plan{256, per});
+  for (unsigned th : {256u, 128u}) {
+    int const occ = th == 128 ? occ128 : occ256;
+    for (unsigned per = 1; per <= (unsigned)std::min(occ, 3); ++per) cands.push_back(Plan{th, per});
+  }
+  if (unsigned const ft = g_force_threads.load()) {
+    unsigned const fp = g_force_per_sm.load();
+    int const occ = ft == 128 ? occ128 : occ256;
+    if ((ft != 128 && ft != 256) || fp < 1 || (int)fp > std::min(occ, 3))
+      return fail(LS_INVALID_ARGUMENT, "sed_eigh_batched: the fixed launch shape (" + std::to_string(ft) + " threads, " +
+                                           std::to_string(fp) + " CTAs per SM) is not co-resident on this device");
+    cands.assign(1, Plan{ft, fp});
+  }
   uint64_t sumD = 0;
   for (unsigned i = 0; i < count; ++i) sumD += od[i]->basis->D;
   auto key = std::make_tuple(device, count, sumD);
   Plan plan = cands[0];
-  bool tuned = false;
-  {
+  bool tuned = cands.size() == 1;  // a fixed shape needs no trial runs
+  if (!tuned) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) {
@@ -971,7 +992,9 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     return L;
   };
 
-  unsigned const max_grid = (unsigned)sms * (unsigned)std::min(max_per_sm, 2);
+  unsigned max_per_cand = 1;
+  for (Plan const& p : cands) max_per_cand = std::max(max_per_cand, p.ctas_per_sm);
+  unsigned const max_grid = (unsigned)sms * max_per_cand;
   size_t const part_bytes = 2 * (size_t)max_grid * kPart * 8;
   std::vector<size_t> off_part(count);
   for (unsigned i = 0; i < count; ++i) off_part[i] = take(part_bytes);  // enough for any group size
@@ -1156,3 +1179,8 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
 }
 
 }  // extern "C"
+
+extern "C" void sed_set_batched_launch(unsigned threads_per_cta, unsigned ctas_per_sm) {
+  sed::g_force_threads.store(threads_per_cta ? threads_per_cta : 0u);
+  sed::g_force_per_sm.store(threads_per_cta ? ctas_per_sm : 0u);
+}

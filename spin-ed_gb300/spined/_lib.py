@@ -150,6 +150,7 @@ SIGNATURES = [
     ("sed_mlp_start_vector", _I, [_P, _P, _P]),
     ("sed_mlp_set_path", _I, [_P, _I]),
     ("sed_release_workspace", None, []),
+    ("sed_set_batched_launch", None, [C.c_uint, C.c_uint]),
     ("sed_rotate_vectors", _I, [_P, _U64, C.c_uint32, _P, C.c_uint32, _U64, _I, _P]),
     ("sed_set_rotate_path", None, [_I]),
     ("sed_operator_time_matvec", _I, [_P, _P, _P, C.c_uint, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -91,3 +91,24 @@ def test_j1j2_chains_128(sed):
     for i in big:
         one = sed.eigh(built[i].hamiltonian, nev=4)
         np.testing.assert_allclose(res.eigenvalues[i], one.eigenvalues, rtol=EV_RTOL)
+
+
+@pytest.mark.parametrize("threads,per_sm", [(128, 1), (128, 2), (256, 1), (256, 2)])
+def test_fixed_launch_shapes_agree(sed, oracle, threads, per_sm):
+    """Every launch shape the autotuner chooses among gives the same pairs:
+    each shape, fixed through sed_set_batched_launch, against dense
+    diagonalisation of the oracle's sector matrices."""
+    from spined import _lib as L
+    lib = L.load()
+    models = [lattices.heisenberg_chain(n, j2=0.1 * k) for k, n in enumerate((12, 14, 16, 18, 14))]
+    pairs = [both(sed, oracle, m) for m in models]
+    try:
+        lib.sed_set_batched_launch(threads, per_sm)
+        res = sed.eigh_batched([b.hamiltonian for b, _, _ in pairs], nev=4)
+    finally:
+        lib.sed_set_batched_launch(0, 0)
+    assert res.ctas_per_sm == per_sm
+    for i, (b, ob, oop) in enumerate(pairs):
+        want = np.linalg.eigvalsh(oop.dense().real)[:4]
+        np.testing.assert_allclose(res.eigenvalues[i], want, rtol=EV_RTOL, atol=0)
+        assert np.all(res.residuals[i] <= RES_TOL)
