@@ -529,7 +529,7 @@ __global__ void k_compact24(uint32_t const* __restrict__ entries, uint64_t n, ui
 // k_spmv_fix over the compact entries: 3 bytes per slot instead of 4, no
 // value codes (one accumulator, every character +1). The same integer sums
 // and the same epilogue as k_spmv_fix<.., 1>, so the results are identical.
-__global__ void __launch_bounds__(kBlock) k_spmv_fix24(StreamView S, FixView fv, uint64_t D,
+__global__ void __launch_bounds__(kBlock, 8) k_spmv_fix24(StreamView S, FixView fv, uint64_t D,
                                                        uint16_t const* __restrict__ lo16,
                                                        uint8_t const* __restrict__ hi8, double const* __restrict__ x,
                                                        int64_t const* __restrict__ u, int64_t const* __restrict__ F_in,

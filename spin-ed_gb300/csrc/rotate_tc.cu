@@ -55,10 +55,6 @@ struct RtArgs {
   uint64_t wait_ns;
 };
 
-__device__ __forceinline__ int rt_expo(double v) {  // biased exponent, 1 for subnormals and zero
-  int const e = (int)(((uint64_t)__double_as_longlong(v) >> 52) & 0x7FF);
-  return e ? e : 1;
-}
 
 // floor(|v| 2^(56 - R)) with R = Emax - 1022 (Emax: the largest biased
 // exponent of the row or column): an integer below 2^56.
@@ -107,15 +103,47 @@ __device__ __forceinline__ void rt_put_row(uint8_t* base, uint32_t r, uint64_t c
   }
 }
 
+// (h 2^32 + l) 2^sc as a double, rounded to nearest even, from integer
+// operations only (h: |h| < 2^51; l in [0, 2^32)); results outside the normal
+// range go through FP64 arithmetic, which rounds the same way.
+__device__ __forceinline__ double rt_ldexp(double a, int p);
+__device__ __forceinline__ double rt_compose(int64_t h, int64_t l, int sc) {
+  __int128 const T = ((__int128)h << 32) + (__int128)l;
+  if (T == 0) return 0.0;
+  uint64_t const sign = T < 0 ? 1ull : 0ull;
+  unsigned __int128 const u = (unsigned __int128)(T < 0 ? -T : T);
+  uint64_t const uh = (uint64_t)(u >> 64), ul = (uint64_t)u;
+  int const top = uh ? 127 - __clzll((long long)uh) : 63 - __clzll((long long)ul);
+  uint64_t mant;
+  int e = top;
+  if (top <= 52) {
+    mant = ul << (52 - top);
+  } else {
+    int const r = top - 52;  // 1 .. 30
+    mant = (uint64_t)(u >> r);
+    uint64_t const rem = ul & ((1ull << r) - 1ull), half = 1ull << (r - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+    if (mant >> 53) {
+      mant >>= 1;
+      ++e;
+    }
+  }
+  int const biased = e + sc + 1023;
+  if (biased < 1 || biased > 2046)
+    return rt_ldexp(__fma_rn((double)h, 4294967296.0, (double)l), sc);
+  return __longlong_as_double((long long)((sign << 63) | ((uint64_t)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
 __device__ __forceinline__ double rt_ldexp(double a, int p) {
   if (p >= -1000 && p <= 1000) return a * fix_pow2(p);
   int const h = p / 2;
   return (a * fix_pow2(h)) * fix_pow2(p - h);
 }
 
-// KS: K columns per slice (16 or 32, at least m); KT: 64-column K tiles.
-template <int KS>
-__global__ void __launch_bounds__(kRtRows) k_rotate_tc(RtArgs a) {
+// KS: K columns per slice (16 or 32, at least m); KT: 64-column K tiles; NJ:
+// output columns handled (8 when kk <= 8, else 16; the MMA is always N = 16).
+template <int KS, int NJ>
+__global__ void __launch_bounds__(kRtRows, (KS == 16 && NJ == 8) ? 4 : 3) k_rotate_tc(RtArgs a) {
   constexpr int KT = (kRtSlices * KS + 63) / 64;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t done, drain;
@@ -135,21 +163,21 @@ __global__ void __launch_bounds__(kRtRows) k_rotate_tc(RtArgs a) {
   }
   // B: thread j < 16 writes column j of Y as row j (zero rows beyond kk)
   if (t < kRtN) {
-    double y[KS];
+    uint64_t yb[KS];
     int emax = 1, bad = 0;
 #pragma unroll
     for (int k = 0; k < KS; ++k) {
-      y[k] = ((uint32_t)k < m && (uint32_t)t < a.kk) ? a.Y[(uint64_t)k * a.kk + t] : 0.0;
-      int const e = rt_expo(y[k]);
+      yb[k] = ((uint32_t)k < m && (uint32_t)t < a.kk) ? (uint64_t)__double_as_longlong(a.Y[(uint64_t)k * a.kk + t]) : 0ull;
+      int const e = (int)((yb[k] >> 52) & 0x7FF);
       if (e == 0x7FF) bad = 1;
-      emax = max(emax, e);
+      emax = max(emax, e ? e : 1);
     }
     uint64_t mag[KS];
     uint32_t neg = 0;
 #pragma unroll
     for (int k = 0; k < KS; ++k) {
-      mag[k] = bad ? 0 : rt_mag(y[k], emax);
-      neg |= (y[k] < 0.0 ? 1u : 0u) << k;
+      mag[k] = bad ? 0 : rt_mag(__longlong_as_double((long long)yb[k]), emax);
+      neg |= (uint32_t)(yb[k] >> 63) << k;
     }
     rt_put_row<KS, KT, kRtN>(B, (uint32_t)t, mag, neg, m);
     bad_col[t] = bad;
@@ -169,24 +197,22 @@ __global__ void __launch_bounds__(kRtRows) k_rotate_tc(RtArgs a) {
   for (uint64_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++it) {
     uint64_t const row = tile * kRtRows + (uint64_t)t;
     bool const live = row < a.D;
-    // ---- this thread's row of V: scale, slices into A
-    double v[KS];
+    // ---- this thread's row of V: scale, slices into A (integer operations)
     int emax = 1, bad = 0;
-#pragma unroll
-    for (int k = 0; k < KS; ++k) {
-      v[k] = (live && (uint32_t)k < m) ? __ldcs(a.V + (uint64_t)k * a.ld + row) : 0.0;
-      int const e = rt_expo(v[k]);
-      if (e == 0x7FF) bad = 1;
-      emax = max(emax, e);
-    }
+    uint32_t neg = 0;
     {
-      uint64_t mag[KS];
-      uint32_t neg = 0;
+      uint64_t vb[KS];
 #pragma unroll
       for (int k = 0; k < KS; ++k) {
-        mag[k] = bad ? 0 : rt_mag(v[k], emax);
-        neg |= (v[k] < 0.0 ? 1u : 0u) << k;
+        vb[k] = (live && (uint32_t)k < m) ? (uint64_t)__double_as_longlong(__ldcs(a.V + (uint64_t)k * a.ld + row)) : 0ull;
+        int const e = (int)((vb[k] >> 52) & 0x7FF);
+        if (e == 0x7FF) bad = 1;
+        emax = max(emax, e ? e : 1);
+        neg |= (uint32_t)(vb[k] >> 63) << k;
       }
+      uint64_t mag[KS];
+#pragma unroll
+      for (int k = 0; k < KS; ++k) mag[k] = bad ? 0 : rt_mag(__longlong_as_double((long long)vb[k]), emax);
       rt_put_row<KS, KT, kRtRows>(A, (uint32_t)t, mag, neg, m);
     }
     tc::fence_proxy_async_smem();
@@ -214,7 +240,7 @@ __global__ void __launch_bounds__(kRtRows) k_rotate_tc(RtArgs a) {
       }
       __syncwarp();
     }
-    // ---- every thread: wait for the MMAs, read its lane's 8 x 16 sums
+    // ---- every thread: wait for the MMAs, read its lane's 8 groups x NJ sums
     if (!tc::mbar_wait(&done, it & 1u, a.wait_ns)) {
       ok = false;
       atomicExch(a.error, 1);
@@ -222,44 +248,36 @@ __global__ void __launch_bounds__(kRtRows) k_rotate_tc(RtArgs a) {
     tc::fence_after_sync();
     ok = __syncthreads_and(ok);
     if (!ok) break;
-    int64_t hi[kRtN], lo[kRtN];
+    int64_t hi[NJ], lo[NJ];
 #pragma unroll
-    for (int j = 0; j < kRtN; ++j) hi[j] = lo[j] = 0;
+    for (int j = 0; j < NJ; ++j) hi[j] = lo[j] = 0;
     uint32_t const lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
-    for (int q = 0; q < kRtGroups / 2; ++q) {  // two groups per 32-column load
-      float p[32];
-      tc::tmem_ld32(lane_addr + (uint32_t)(q * 32), p);
+    for (int g = 0; g < kRtGroups; ++g) {
+      float p[NJ];
+      tc::tmem_ld(lane_addr + (uint32_t)(g * kRtN), p);
+      int const sh = 8 * (7 - g);
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        int const g = 2 * q + h, sh = 8 * (7 - g);
-#pragma unroll
-        for (int j = 0; j < kRtN; ++j) {
-          int64_t const pv = (int64_t)__float2int_rz(p[h * kRtN + j]);  // an exact integer below 2^24
-          if (sh >= 32) {
-            hi[j] += pv << (sh - 32);
-          } else {
-            hi[j] += pv >> (32 - sh);
-            lo[j] += (int64_t)(((uint64_t)pv << sh) & 0xFFFFFFFFull);
-          }
+      for (int j = 0; j < NJ; ++j) {
+        int64_t const pv = (int64_t)__float2int_rz(p[j]);  // an exact integer below 2^24
+        if (sh >= 32) {
+          hi[j] += pv << (sh - 32);
+        } else {
+          hi[j] += pv >> (32 - sh);
+          lo[j] += (int64_t)(((uint64_t)pv << sh) & 0xFFFFFFFFull);
         }
       }
     }
     tc::fence_before_sync();
-    // ---- T = hi 2^32 + lo, one rounding to FP64, exact scaling; in place
+    // ---- T = hi 2^32 + lo rounded to FP64 and scaled, in place
     if (live) {
+      int const scr = emax - 1022 - 72;
 #pragma unroll
-      for (int j = 0; j < kRtN; ++j) {
+      for (int j = 0; j < NJ; ++j) {
         if ((uint32_t)j >= a.kk) break;
-        int64_t const h = hi[j] + (lo[j] >> 32);
-        int64_t const l = lo[j] & 0xFFFFFFFFll;
-        double r;
-        if (bad || bad_col[j]) {
-          r = __longlong_as_double(0x7FF8000000000000ll);
-        } else {
-          double const T = __fma_rn((double)h, 4294967296.0, (double)l);
-          r = rt_ldexp(T, (emax - 1022) + (ecol[j] - 1022) - 72);
-        }
+        double const r = (bad || bad_col[j])
+                             ? __longlong_as_double(0x7FF8000000000000ll)
+                             : rt_compose(hi[j] + (lo[j] >> 32), lo[j] & 0xFFFFFFFFll, scr + (ecol[j] - 1022));
         __stcs(a.V + (uint64_t)j * a.ld + row, r);
       }
     }
@@ -309,16 +327,17 @@ int rotate_tc(double* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk, 
   a.error = error_flag;
   a.wait_ns = device_wait_ns(kRtWaitNs);
   uint64_t const tiles = (D + kRtRows - 1) / kRtRows;
-  unsigned const grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)sms * 3);  // 3 x 128 TMEM columns per SM
-  if (m <= 16) {
-    size_t const smem = 1024 + (size_t)((kRtSlices * 16 + 63) / 64) * (kRtRows + kRtN) * 128;
-    SED_TRY_CUDA(cudaFuncSetAttribute(k_rotate_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_rotate_tc<16><<<grid, kRtRows, smem, stream>>>(a);
-  } else {
-    size_t const smem = 1024 + (size_t)((kRtSlices * 32 + 63) / 64) * (kRtRows + kRtN) * 128;
-    SED_TRY_CUDA(cudaFuncSetAttribute(k_rotate_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_rotate_tc<32><<<grid, kRtRows, smem, stream>>>(a);
-  }
+  unsigned const grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)sms * 4);  // 4 x 128 TMEM columns per SM
+  auto go = [&](auto kern, int ks) -> int {
+    size_t const smem = 1024 + (size_t)((kRtSlices * ks + 63) / 64) * (kRtRows + kRtN) * 128;
+    SED_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, kRtRows, smem, stream>>>(a);
+    return LS_SUCCESS;
+  };
+  int st;
+  if (m <= 16) st = kk <= 8 ? go(k_rotate_tc<16, 8>, 16) : go(k_rotate_tc<16, 16>, 16);
+  else st = kk <= 8 ? go(k_rotate_tc<32, 8>, 32) : go(k_rotate_tc<32, 16>, 32);
+  if (st) return st;
   note_launches(1);
   SED_TRY_CUDA(cudaGetLastError());
   return LS_SUCCESS;
