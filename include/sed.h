@@ -311,7 +311,8 @@ SED_API int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, u
  * recombination (the result differs from an FP64 product by the truncation
  * of each operand to 56 bits below its row or column maximum and the final
  * rounding); SED_ROTATE_FP64 uses FP64 FMAs on the CUDA cores;
- * SED_ROTATE_AUTO takes the tensor cores when the shape allows. The work is
+ * SED_ROTATE_AUTO takes the tensor cores when the shape allows and m >= 16
+ * (where they measured faster than the FP64 pipe). The work is
  * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream)
  * and the call waits for it. sed_set_rotate_path selects the path of the
  * rotation inside sed_eigh's thick-restart solver (process-wide). */

@@ -507,86 +507,6 @@ __global__ void __launch_bounds__(kBlock) k_spmv_fix(StreamView S, FixView fv, u
   }
 }
 
-// The compact entries (StreamForm::compact24) from the packed ones; sets
-// *flag if an element carries a value index or a sign (then the compact
-// form cannot represent the operator and is dropped).
-__global__ void k_compact24(uint32_t const* __restrict__ entries, uint64_t n, uint32_t col_bits,
-                            uint8_t const* __restrict__ code8, uint16_t* __restrict__ lo16, uint8_t* __restrict__ hi8,
-                            int* __restrict__ flag) {
-  uint32_t const mask = (1u << col_bits) - 1u;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t const v = entries[i];
-    uint32_t col = 0xFFFFFFu;
-    if (v != kNull) {
-      col = v & mask;
-      if (code8[v >> col_bits] != 0) atomicOr(flag, 1);
-    }
-    lo16[i] = (uint16_t)(col & 0xFFFFu);
-    hi8[i] = (uint8_t)(col >> 16);
-  }
-}
-
-// k_spmv_fix over the compact entries: 3 bytes per slot instead of 4, no
-// value codes (one accumulator, every character +1). The same integer sums
-// and the same epilogue as k_spmv_fix<.., 1>, so the results are identical.
-__global__ void __launch_bounds__(kBlock, 8) k_spmv_fix24(StreamView S, FixView fv, uint64_t D,
-                                                       uint16_t const* __restrict__ lo16,
-                                                       uint8_t const* __restrict__ hi8, double const* __restrict__ x,
-                                                       int64_t const* __restrict__ u, int64_t const* __restrict__ F_in,
-                                                       double* __restrict__ y, Indirect ind) {
-  extern __shared__ double fix_smem[];  // g[n_div]
-  __shared__ double red[kBlock];
-  if (ind.stop && *ind.stop) return;  // uniform across the grid
-  if (ind.k) {
-    uint64_t const k = *ind.k;
-    x += k * ind.ld;
-    y += (k + 1) * ind.ld;
-  }
-  int64_t const F = F_in[0];
-  double* g = fix_smem;
-  fix_row_factors<1>(fv, S.inv_sqrt_s, F, g);
-  __syncthreads();
-  uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t const s = i >> 5;
-  double part = 0.0;
-  if ((s << 5) < D) {
-    uint32_t const lane = threadIdx.x & 31;
-    uint64_t const base = S.slice_ptr[s];
-    uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
-    int64_t acc[1] = {0};
-    uint16_t const* lo = lo16 + base + lane;
-    uint8_t const* hi = hi8 + base + lane;
-    constexpr uint32_t U = 8;
-    uint32_t e = 0;
-    for (; e + U <= width; e += U) {
-      uint32_t c[U];
-#pragma unroll
-      for (uint32_t q = 0; q < U; ++q)
-        c[q] = (uint32_t)__ldcs(lo + (uint64_t)(e + q) * 32) | ((uint32_t)__ldcs(hi + (uint64_t)(e + q) * 32) << 16);
-      int64_t gv[U];
-#pragma unroll
-      for (uint32_t q = 0; q < U; ++q) gv[q] = c[q] != 0xFFFFFFu ? u[c[q]] : 0;
-#pragma unroll
-      for (uint32_t q = 0; q < U; ++q) acc[0] += gv[q];
-    }
-    for (; e < width; ++e) {
-      uint32_t const c = (uint32_t)__ldcs(lo + (uint64_t)e * 32) | ((uint32_t)__ldcs(hi + (uint64_t)e * 32) << 16);
-      if (c != 0xFFFFFFu) acc[0] += u[c];
-    }
-    if (i < D) {
-      double const xi = __ldcs(x + i);
-      double const yi = fix_row<1>(acc, g + (uint32_t)__ldcs(S.row_class + i), F,
-                                   __ldcs(static_cast<double const*>(S.diag) + i), xi);
-      __stcs(y + i, yi);
-      part = xi * yi;
-    }
-  }
-  if (ind.partial) {
-    double const tot = block_sum_fixed(part, red);
-    if (threadIdx.x == 0) ind.partial[blockIdx.x] = tot;
-  }
-}
-
 // Block form in fixed point: K columns, u column c at u + c * D, F_in[c].
 template <bool Packed, int NV, int K>
 __global__ void __launch_bounds__(kBlock) k_spmv_block_fix(StreamView S, FixView fv, uint64_t D,
@@ -1446,26 +1366,6 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
   sf.n_codes = tb.n_codes;
   sf.ready = true;
   sf.orbit_table = use_table;
-  // compact entries for the fixed-point SpMV when the operator allows them
-  if (packed && tb.fix_ok && tb.fix_nv == 1 && D < 0xFFFFFFull && n_entries) {
-    DeviceBuffer flag;
-    if (flag.allocate(4) == LS_SUCCESS && sf.lo16.allocate(n_entries * 2) == LS_SUCCESS &&
-        sf.hi8.allocate(n_entries) == LS_SUCCESS) {
-      SED_TRY_CUDA(cudaMemsetAsync(flag.ptr, 0, 4, stream));
-      { k_compact24<<<grid_size(n_entries, b.device, 8), kBlock, 0, stream>>>(
-            sf.entries.as<uint32_t>(), n_entries, col_bits, tb.fix.code, sf.lo16.as<uint16_t>(), sf.hi8.as<uint8_t>(),
-            flag.as<int>()); note_launches(1); }
-      int h = 1;
-      SED_TRY_CUDA(cudaMemcpyAsync(&h, flag.ptr, 4, cudaMemcpyDeviceToHost, stream));
-      SED_TRY_CUDA(cudaStreamSynchronize(stream));
-      sf.compact24 = h == 0;
-    }
-    if (!sf.compact24) {
-      sf.lo16.reset();
-      sf.hi8.reset();
-      cudaGetLastError();
-    }
-  }
   sf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (logging_enabled())
     log_line("stream form: %llu elements, %llu slots (%s), %.1f MB, %.3f s (%s)",
@@ -1498,12 +1398,6 @@ void launch_spmv_fix(OperatorData& op, StreamView const& S, double const* x, int
   StreamForm const& sf = op.stream;
   OperatorTables const& tb = *op.tables;
   unsigned const grid = (unsigned)((sf.n_slices * 32 + kBlock - 1) / kBlock);
-  if (NV == 1 && sf.compact24) {
-    k_spmv_fix24<<<grid, kBlock, (size_t)tb.fix.n_div * 8, stream>>>(S, tb.fix, op.basis->D, sf.lo16.as<uint16_t>(),
-                                                                    sf.hi8.as<uint8_t>(), x, u, F, y, ind);
-    note_launches(1);
-    return;
-  }
   size_t const smem = (size_t)tb.fix.n_div * NV * 8 + tb.fix.n_codes;
   if (sf.packed) k_spmv_fix<true, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, op.basis->D, x, u, F, y, ind);
   else k_spmv_fix<false, NV><<<grid, kBlock, smem, stream>>>(S, tb.fix, op.basis->D, x, u, F, y, ind);

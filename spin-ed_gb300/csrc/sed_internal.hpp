@@ -187,11 +187,6 @@ struct StreamForm {
   unsigned n_codes = 0;
   double seconds = 0;
   bool orbit_table = false;     // recorded through the orbit table
-  // compact copy of the entries for the fixed-point FP64 SpMV when every
-  // element has value index 0 and character +1 and D < 2^24 - 1: 24-bit
-  // columns as a low 16-bit and a high 8-bit array (0xFFFFFF: padding)
-  bool compact24 = false;
-  DeviceBuffer lo16, hi8;
   // FP32 companions for the mixed-precision Krylov phase (real operators)
   DeviceBuffer diag_f;   // float[D]
   DeviceBuffer table_f;  // float[n_codes]

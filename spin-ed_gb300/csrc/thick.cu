@@ -180,7 +180,11 @@ template <class S>
 int rotate_basis(S* V, uint64_t ld, uint32_t m, double const* Y, uint32_t kk, uint64_t D, unsigned vb,
                  cudaStream_t stream, int path, int* err) {
   if constexpr (std::is_same<S, double>::value) {
-    if (path != SED_ROTATE_FP64 && rotate_tc_eligible(m, kk)) {
+    // AUTO takes the tensor cores where they measured faster than the FP64
+    // pipe (m >= 16: 68 against 82 ms for m = 32, kk = 16 on 1e8 rows; at
+    // m = 12, kk = 6 the two tie, 16.1 against 15.7 ms)
+    bool const tc = path == SED_ROTATE_TENSOR || (path == SED_ROTATE_AUTO && m >= 16);
+    if (tc && rotate_tc_eligible(m, kk)) {
       SED_TRY_CUDA(cudaMemsetAsync(err, 0, 4, stream));
       if (int st = rotate_tc(V, ld, m, Y, kk, D, stream, err)) return st;
       int h = 0;

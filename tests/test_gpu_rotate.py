@@ -75,7 +75,7 @@ def test_tensor_rotation_nan_and_errors(sed):
     assert st == L.LS_INVALID_ARGUMENT  # kk > 16 is not a tensor-core shape
     st = lib.sed_rotate_vectors(C.c_void_p(Vd.data_ptr()), 64, 20, C.c_void_p(Yd.data_ptr()), 17, 64,
                                 L.SED_ROTATE_AUTO, None)
-    assert st == 0  # AUTO falls back to the FP64 kernel
+    assert st == 0  # AUTO takes the FP64 kernel for kk > 16
 
 
 def test_thick_restart_rotation_paths_agree(sed, oracle):
