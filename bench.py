@@ -48,12 +48,12 @@ METRIC = "time-to-ground-state (resid<=1e-8) vs plain FP64 GPU Lanczos; matvec H
 SQUARE6_STEPS = 57  # 56 Lanczos steps + the final residual check
 # the same count per workload (chain 24: 50 steps + the residual check)
 SOLVE_MATVECS = {"square6": SQUARE6_STEPS, "chain24": 51}
-# DRAM bytes (read + write) of one k_spmv launch on the 6x6 workload, from one
-# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of
-#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
-#       -k regex:k_spmv -s 40 -c 1 python bench.py --once
-# 4 935 736 320 read + 124 209 920 written.
-SPMV_TRAFFIC_BYTES = 4935736320 + 124209920
+# DRAM bytes (read + write) of one k_spmv_fix launch on the 6x6 workload, from
+# one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of
+#   ncu --set full --clock-control none -k regex:k_spmv_fix -s 3 -c 1
+#       python bench.py --profile-case spmv
+# 4 950 761 000 read + 123 582 976 written.
+SPMV_TRAFFIC_BYTES = 4950761000 + 123582976
 
 
 def workload_model(name: str, hamming_weight: int | None = None):
