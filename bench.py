@@ -596,7 +596,7 @@ def main():
     ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
     ap.add_argument("--profile-case", default=None, choices=["mlp", "batch16", "spmv", "rotate"],
                     help="one small run of a single kernel family, for profilers: the tensor-core MLP "
-                         "inference over 2^20 random 36-spin states, a 16-chain batched solve, 10 "
+                         "inference over 2^20 random 36-spin states, a 16-chain batched solve (one fixed launch shape), 10 "
                          "matvecs of the 6x6 stream form (about 3.5 GB on the device), or the thick-restart "
                          "basis rotation on 1e8 rows on both paths (--rotate-rows to change)")
     ap.add_argument("--rotate-rows", type=int, default=100_000_000)
@@ -674,9 +674,16 @@ def main():
     if args.profile_case == "batch16":
         from spined import internal as I, lattices
         from spined.model import build_model
+        from spined import _lib as L
         built = [build_model(lattices.heisenberg_chain(16 + 2 * (k % 4), j2=0.05 * k)) for k in range(16)]
-        r = I.eigh_batched([b.hamiltonian for b in built], nev=4, vectors=False)
-        print(json.dumps({"case": "batch16", "kernel_ms": r.kernel_ms, "max_residual": float(r.residuals.max())}))
+        # one fixed launch shape, so that the only k_batch_lanczos launch is the solve (no tuning trials)
+        L.load().sed_set_batched_launch(256, 2)
+        try:
+            r = I.eigh_batched([b.hamiltonian for b in built], nev=4, vectors=False)
+        finally:
+            L.load().sed_set_batched_launch(0, 0)
+        print(json.dumps({"case": "batch16", "launch": "256 threads x 2 CTAs per SM", "kernel_ms": r.kernel_ms,
+                          "max_residual": float(r.residuals.max())}))
         return
     if args.once:
         from spined import internal as I
