@@ -594,9 +594,10 @@ def main():
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
     ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
     ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
-    ap.add_argument("--profile-case", default=None, choices=["mlp", "batch16", "spmv", "rotate"],
+    ap.add_argument("--profile-case", default=None, choices=["mlp", "train", "batch16", "spmv", "rotate"],
                     help="one small run of a single kernel family, for profilers: the tensor-core MLP "
-                         "inference over 2^20 random 36-spin states, a 16-chain batched solve (one fixed launch shape), 10 "
+                         "inference over 2^20 random 36-spin states, one tensor-core training epoch (2^18 "
+                         "samples, 64 batches of 4096), a 16-chain batched solve (one fixed launch shape), 10 "
                          "matvecs of the 6x6 stream form (about 3.5 GB on the device), or the thick-restart "
                          "basis rotation on 1e8 rows on both paths (--rotate-rows to change)")
     ap.add_argument("--rotate-rows", type=int, default=100_000_000)
@@ -624,6 +625,17 @@ def main():
         out = net.forward(st)
         print(json.dumps({"case": "mlp", "states": len(st), "tensor_cores": net.uses_tensor_cores,
                           "max_abs": float(np.abs(out).max())}))
+        return
+    if args.profile_case == "train":
+        import numpy as np
+        from spined.learned import Mlp, Samples
+        net = Mlp(36, 512, seed=1)
+        st = np.random.default_rng(0).integers(0, 2 ** 36, size=1 << 18, dtype=np.uint64)
+        data = Samples(st, (st % np.uint64(7)).astype(np.float32) * 0.1, (st & np.uint64(1)).astype(np.float32))
+        t0 = time.perf_counter()
+        loss = net.train(data, epochs=1, batch=4096, lr=3e-3, seed=1)
+        print(json.dumps({"case": "train", "samples": len(st), "steps": len(st) // 4096, "loss": loss,
+                          "tensor_cores": net.uses_tensor_cores, "seconds": time.perf_counter() - t0}))
         return
     if args.profile_case == "spmv":
         from spined import internal as I, _lib as L

@@ -392,7 +392,10 @@ SED_API int sed_mlp_forward(sed_mlp* mlp, uint64_t const* states, uint64_t n, fl
 SED_API int sed_mlp_loss_grad(sed_mlp* mlp, uint64_t const* states, float const* t_abs, float const* t_sign,
                               uint64_t n, double* loss, float* grads);
 /* Adam (0.9, 0.999, 1e-8) on mini-batches of `batch` samples, reshuffled
- * every epoch; final_loss (may be NULL) is the loss of the last batch. */
+ * every epoch (floor(n / batch) batches; the rest of a shuffle is unused);
+ * final_loss (may be NULL) is the loss of the last batch. On the tensor-core
+ * path (sed_mlp_set_path) the shuffle is a keyed permutation made on the
+ * device, at most 2^31 - 1 samples; on the SIMT path a host shuffle. */
 SED_API int sed_mlp_train(sed_mlp* mlp, uint64_t const* states, float const* t_abs, float const* t_sign, uint64_t n,
                           unsigned epochs, unsigned batch, float lr, uint64_t seed, double* final_loss);
 /* Training data from a real vector psi over the built basis: n representatives
@@ -410,13 +413,15 @@ SED_API int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64
  * Pass it to sed_eigh as SED_START_GIVEN. */
 SED_API int sed_mlp_start_vector(sed_mlp* mlp, ls_spin_basis const* basis, double* out);
 
-/* Inference path of sed_mlp_forward and sed_mlp_start_vector. AUTO runs the
- * whole network on the tensor cores (tcgen05, BF16 operands, FP32
- * accumulation in tensor memory, one fused kernel per 128 states) when
- * n_inputs <= 64 and hidden is 128, 256 or 512; there the hidden activations
- * h1 are rounded to BF16 between the layers and tanh is the hardware
- * approximation. SIMT keeps every product on the CUDA cores with FP32
- * activations (the path training uses). */
+/* Path of every pass. AUTO uses the tensor cores (tcgen05, BF16 operands,
+ * FP32 accumulation in tensor memory) when n_inputs <= 64 and hidden is 128,
+ * 256 or 512. Inference (sed_mlp_forward, sed_mlp_start_vector) then runs the
+ * whole network in one fused kernel per 128 states, h1 rounded to BF16
+ * between the layers and tanh the hardware approximation. Training
+ * (sed_mlp_loss_grad, sed_mlp_train) runs each product as a tensor-core GEMM
+ * with h1, h2 and the backward activations stored in BF16 (the bias
+ * gradients sum them before the rounding). SIMT keeps every product on the
+ * CUDA cores with FP32 activations. */
 enum { SED_MLP_PATH_AUTO = 0, SED_MLP_PATH_SIMT = 1 };
 SED_API int sed_mlp_set_path(sed_mlp* mlp, int path);
 /* 1 if inference runs on the tensor cores, else 0. */

@@ -62,13 +62,22 @@ def forward(p, n, h, states, act_bf16=False):
     return x, h1, h2, out
 
 
-def loss_grad(p, n, h, states, t_abs, t_sign, sign_mask=0):
+def loss_grad(p, n, h, states, t_abs, t_sign, sign_mask=0, act_bf16=False):
     """Loss and gradient with respect to the FP32 parameters (the BF16
     rounding of the weights is treated as the identity in the backward pass,
-    as the library does)."""
+    as the library does).
+
+    act_bf16 follows the tensor-core training step instead of the CUDA-core
+    one: h1, h2 and the backward activations d2, d1 are rounded to BF16 where
+    the GEMMs read them (h1 and h2 as stored, d2 before dW2 and d1, d1
+    before dW1), while the bias gradients db2, db1 sum the unrounded d2, d1."""
     w = unpack(p, n, h)
-    W2, W3 = bf16(w["W2"]), bf16(w["W3"])
-    x, h1, h2, out = forward(p, n, h, states)
+    W1, W2, W3 = bf16(w["W1"]), bf16(w["W2"]), bf16(w["W3"])
+    x = spins(states, n)
+    r = (lambda a: bf16(a.astype(np.float32))) if act_bf16 else (lambda a: a)
+    h1 = r(np.tanh(x @ W1.T + w["b1"]))
+    h2 = r(np.tanh(h1 @ W2.T + w["b2"]))
+    out = h2 @ W3.T + w["b3"]
     N = len(states)
     a, s = out[:, 0], out[:, 1]
     y = np.abs(t_sign.astype(np.float64) - parity(states, sign_mask))
@@ -77,8 +86,8 @@ def loss_grad(p, n, h, states, t_abs, t_sign, sign_mask=0):
     dout = np.stack([2 * da / N, (1 / (1 + np.exp(-s)) - y) / N], axis=1)
     dW3, db3 = dout.T @ h2, dout.sum(0)
     d2 = (dout @ W3) * (1 - h2 * h2)
-    dW2, db2 = d2.T @ h1, d2.sum(0)
-    d1 = (d2 @ W2) * (1 - h1 * h1)
-    dW1, db1 = d1.T @ x, d1.sum(0)
+    dW2, db2 = r(d2).T @ h1, d2.sum(0)
+    d1 = (r(d2) @ W2) * (1 - h1 * h1)
+    dW1, db1 = r(d1).T @ x, d1.sum(0)
     g = np.concatenate([dW1.ravel(), db1, dW2.ravel(), db2, dW3.ravel(), db3])
     return loss, g

@@ -16,11 +16,15 @@
 // |c_r|^2 from ground states the solver computed at neighbouring couplings;
 // the start vector is v_r = prior(r) sign(s) exp(a) / n_r.
 //
-// Training GEMMs are SIMT tiles (64 x 64 outputs per 256-thread block,
-// 16-deep K steps through shared memory, 4 x 4 outputs per thread) with
-// arbitrary strides, so one kernel serves every product of the forward and
-// backward passes. Inference (forward and start vector) runs the whole
-// network on the tensor cores in one persistent kernel, k_mlp_forward_tc.
+// Two paths. Tensor cores (n_in <= 64, hidden 128, 256 or 512, the default):
+// training runs every product of the forward and backward passes through
+// the tcgen05 GEMM of tc_gemm.cu with BF16 activations (the weight-gradient
+// products read the activations transposed, through M-/N-major operand
+// descriptors), and inference runs the whole network in one persistent
+// kernel, k_mlp_forward_tc. CUDA cores (any shape, or SED_MLP_PATH_SIMT):
+// SIMT GEMM tiles (64 x 64 outputs per 256-thread block, 16-deep K steps
+// through shared memory, 4 x 4 outputs per thread) with arbitrary strides
+// and FP32 activations.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -31,6 +35,7 @@
 
 #include "sed_internal.hpp"
 #include "tc.cuh"
+#include "tc_gemm.cuh"
 #include "util.cuh"
 
 namespace sed {
@@ -155,9 +160,12 @@ __global__ void k_colsum(float const* __restrict__ g, int64_t rows, int cols, fl
   atomicAdd(db + j, s);
 }
 
+// Adam step on the FP32 master copy, refreshing the BF16 copy; with w1p set
+// also the tensor-core training's copy of W1 (the first n_w1 = hidden x
+// n_in parameters), rows padded to 64 inputs.
 __global__ void k_adam(float* __restrict__ p, float const* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, __nv_bfloat16* __restrict__ pb, int64_t n, float lr, float c1,
-                       float c2) {
+                       float c2, __nv_bfloat16* __restrict__ w1p, int n_in, int64_t n_w1) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
     float const gq = g[q];
     float const mq = 0.9f * m[q] + 0.1f * gq;
@@ -167,7 +175,198 @@ __global__ void k_adam(float* __restrict__ p, float const* __restrict__ g, float
     float const pq = p[q] - lr * (mq * c1) / (sqrtf(vq * c2) + 1e-8f);
     p[q] = pq;
     pb[q] = __float2bfloat16(pq);
+    if (w1p && q < n_w1) w1p[(q / n_in) * 64 + q % n_in] = __float2bfloat16(pq);
   }
+}
+
+// ------------------------------------------- tensor-core training step ---
+// One batch of rows [0, n): X (BF16 spins, 64 columns, zero past n_in) ->
+// h1 = bf16(tanh(X W1^T + b1)) -> h2 = bf16(tanh(h1 W2^T + b2)) on the
+// tensor cores (tc_gemm); k_head evaluates (a, s) = W3 h2 + b3, the loss and
+// g2 = bf16((dout W3) (1 - h2^2)); the tensor cores then give
+// g1 = bf16((g2 W2) (1 - h1^2)) with db1 in its epilogue, dW2 = g2^T h1 and
+// dW1 = g1^T X (K = the batch, read M-/N-major). The column sums db2, db1
+// add the unrounded values. Batches are drawn in the order of a keyed
+// permutation of the samples, made on the device once per epoch.
+
+// W1 (FP32, hidden x n_in) -> BF16 rows of 64, zero padded
+__global__ void k_w1_pad(float const* __restrict__ w1, int n_in, int hidden, __nv_bfloat16* __restrict__ w1p) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < hidden * 64; q += gridDim.x * blockDim.x) {
+    int const r = q / 64, c = q % 64;
+    w1p[q] = __float2bfloat16(c < n_in ? w1[r * n_in + c] : 0.0f);
+  }
+}
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {  // the "lowbias32" integer hash (C. Wellons)
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// perm[j] = pi(j) for j < n: a four-round Feistel network on 2 half bits
+// (the smallest even width covering n), keyed by key0..3, walked along its
+// cycles until the value falls below n; a bijection of [0, n).
+__global__ void k_perm(uint32_t n, int half, uint4 key, uint32_t* __restrict__ perm) {
+  uint32_t const mask = (1u << half) - 1u;
+  uint32_t const keys[4] = {key.x, key.y, key.z, key.w};
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    uint32_t x = j;
+    do {
+      uint32_t l = x >> half, r = x & mask;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        uint32_t const nr = l ^ (mix32(r ^ keys[k]) & mask);
+        l = r;
+        r = nr;
+      }
+      x = (l << half) | r;
+    } while (x >= n);
+    perm[j] = x;
+  }
+}
+
+// Batch rows r < rows from samples perm[b0 + r] (b0 + r without perm): the
+// X row (64 BF16 spins, zero past n_in; eight threads per row, 16 bytes
+// each) and the row's state and targets.
+__global__ void k_batch(uint64_t const* __restrict__ states, float const* __restrict__ t_abs,
+                        float const* __restrict__ t_sign, uint32_t const* __restrict__ perm, uint64_t b0,
+                        int64_t rows, int n_in, __nv_bfloat16* __restrict__ X, uint64_t* __restrict__ bst,
+                        float* __restrict__ bta, float* __restrict__ bts) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < rows * 8; q += (int64_t)gridDim.x * blockDim.x) {
+    int64_t const r = q >> 3;
+    int const c = (int)(q & 7);
+    uint64_t const idx = perm ? perm[b0 + r] : b0 + r;
+    uint64_t const s = states[idx];
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      int const j = 8 * c + 2 * k;
+      uint32_t const lo = j < n_in ? (((s >> j) & 1u) ? 0x3F80u : 0xBF80u) : 0u;
+      uint32_t const hi = j + 1 < n_in ? (((s >> (j + 1)) & 1u) ? 0x3F80u : 0xBF80u) : 0u;
+      w[k] = lo | (hi << 16);
+    }
+    reinterpret_cast<uint4*>(X + r * 64)[c] = make_uint4(w[0], w[1], w[2], w[3]);
+    if (c == 0) {
+      bst[r] = s;
+      bta[r] = t_abs[idx];
+      bts[r] = t_sign[idx];
+    }
+  }
+}
+
+// Output layer, loss and first backward step for rows [0, n): one warp per
+// row, lane l holding the 8-column chunks l and l + 32 of h2. Per row
+// (a, s) = W3 h2 + b3 (warp sums), the output gradient as in k_out_grad,
+// g2 = (dout W3) (1 - h2^2) written as BF16; the row sums of g2 (db2), of
+// dout_c h2 (dW3) and of dout (db3) go through shared memory into the
+// gradient; the loss partial of the block into loss_partial.
+constexpr int kHeadChunks = 2;  // 8-column chunks per lane: hidden <= 512
+__global__ void __launch_bounds__(256)
+    k_head(__nv_bfloat16 const* __restrict__ h2, int H, int64_t n, __nv_bfloat16 const* __restrict__ W3,
+           float const* __restrict__ b3, uint64_t const* __restrict__ bst, float const* __restrict__ bta,
+           float const* __restrict__ bts, uint64_t sign_mask, __nv_bfloat16* __restrict__ g2,
+           float* __restrict__ db2, float* __restrict__ dW3, float* __restrict__ db3,
+           double* __restrict__ loss_partial) {
+  extern __shared__ float sacc[];  // [3][H]: db2, dW3 row 0, dW3 row 1
+  __shared__ double red[32];
+  __shared__ float sd[2];
+  for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) sacc[c] = 0.0f;
+  if (threadIdx.x < 2) sd[threadIdx.x] = 0.0f;
+  __syncthreads();
+  int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, chunks = H / 8;
+  float w0[kHeadChunks][8], w1[kHeadChunks][8], ab[kHeadChunks][8], a0[kHeadChunks][8], a1[kHeadChunks][8];
+#pragma unroll
+  for (int q = 0; q < kHeadChunks; ++q) {
+    int const ch = lane + 32 * q;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      w0[q][j] = ch < chunks ? __bfloat162float(W3[8 * ch + j]) : 0.0f;
+      w1[q][j] = ch < chunks ? __bfloat162float(W3[H + 8 * ch + j]) : 0.0f;
+      ab[q][j] = a0[q][j] = a1[q][j] = 0.0f;
+    }
+  }
+  float const b30 = b3[0], b31 = b3[1], inv_n = 1.0f / (float)n;
+  float sd0 = 0.0f, sd1 = 0.0f;
+  double l = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; r < n; r += (int64_t)gridDim.x * (blockDim.x >> 5)) {
+    float h[kHeadChunks][8];
+    float pa = 0.0f, ps = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kHeadChunks; ++q) {
+      int const ch = lane + 32 * q;
+      uint4 u = make_uint4(0, 0, 0, 0);
+      if (ch < chunks) u = reinterpret_cast<uint4 const*>(h2 + r * H)[ch];
+      uint32_t const wv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        h[q][2 * k] = __uint_as_float(wv[k] << 16);
+        h[q][2 * k + 1] = __uint_as_float(wv[k] & 0xFFFF0000u);
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        pa = fmaf(w0[q][j], h[q][j], pa);
+        ps = fmaf(w1[q][j], h[q][j], ps);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      pa += __shfl_xor_sync(0xffffffffu, pa, o);
+      ps += __shfl_xor_sync(0xffffffffu, ps, o);
+    }
+    float const a = pa + b30, s = ps + b31;
+    float const da = a - bta[r];
+    float const y = fabsf(bts[r] - prior_flip(bst[r], sign_mask));
+    float const pr = 1.0f / (1.0f + expf(-s));
+    float const d0 = 2.0f * da * inv_n, d1 = (pr - y) * inv_n;
+    if (lane == 0) {
+      l += (double)da * da + (double)(fmaxf(s, 0.0f) - s * y + log1pf(expf(-fabsf(s))));
+      sd0 += d0;
+      sd1 += d1;
+    }
+#pragma unroll
+    for (int q = 0; q < kHeadChunks; ++q) {
+      int const ch = lane + 32 * q;
+      if (ch >= chunks) continue;
+      uint32_t pk[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float g[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          int const j = 2 * k + e;
+          g[e] = (d0 * w0[q][j] + d1 * w1[q][j]) * (1.0f - h[q][j] * h[q][j]);
+          ab[q][j] += g[e];
+          a0[q][j] = fmaf(d0, h[q][j], a0[q][j]);
+          a1[q][j] = fmaf(d1, h[q][j], a1[q][j]);
+        }
+        pk[k] = tc::pack_bf16x2(g[0], g[1]);
+      }
+      reinterpret_cast<uint4*>(g2 + r * H)[ch] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kHeadChunks; ++q) {
+    int const ch = lane + 32 * q;
+    if (ch >= chunks) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      atomicAdd(&sacc[8 * ch + j], ab[q][j]);
+      atomicAdd(&sacc[H + 8 * ch + j], a0[q][j]);
+      atomicAdd(&sacc[2 * H + 8 * ch + j], a1[q][j]);
+    }
+  }
+  if (lane == 0) {
+    atomicAdd(&sd[0], sd0);
+    atomicAdd(&sd[1], sd1);
+  }
+  double const tot = block_sum(l, red);  // contains a __syncthreads
+  if (threadIdx.x == 0) loss_partial[blockIdx.x] = tot;
+  __syncthreads();
+  for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) atomicAdd(c < H ? db2 + c : dW3 + (c - H), sacc[c]);
+  if (threadIdx.x < 2) atomicAdd(db3 + threadIdx.x, sd[threadIdx.x]);
 }
 
 __global__ void k_to_bf16(float const* __restrict__ p, __nv_bfloat16* __restrict__ pb, int64_t n) {
@@ -717,6 +916,13 @@ struct MlpData {
   bool img_valid = false;
   int path = 0;  // SED_MLP_PATH_*
   int n_sm = 0;  // multiprocessors of the device (grid of the persistent kernel)
+  // tensor-core training: one batch's BF16 activations (row-major), its
+  // states and targets, the padded BF16 copy of W1, an error flag, and the
+  // tensor maps over them (K-major "k" and M-/N-major "m" boxes)
+  DeviceBuffer tX, tH1, tH2, tG2, tG1, tW1p, tState, tAbs, tSign, t_error;
+  uint64_t t_cap = 0, t_rows = 0;
+  bool t_wmaps = false;
+  CUtensorMap mXk{}, mXm{}, mW1k{}, mH1k{}, mH1m{}, mW2k{}, mW2m{}, mG2k{}, mG2m{}, mG1m{};
   ~MlpData() {
     if (stream) cudaStreamDestroy(stream);
   }
@@ -870,6 +1076,134 @@ int stage(DeviceBuffer& buf, void const* src, size_t bytes, cudaStream_t s) {
   return LS_SUCCESS;
 }
 
+// Tensor-core training: buffers for batches of up to `rows` rows, tensor
+// maps for batches of exactly `rows` rows (rows past them read as zero), the
+// padded W1 copy refreshed from the FP32 master, the error flag cleared.
+int tc_train_prepare(MlpData& d, uint64_t rows) {
+  uint64_t const H = d.hidden;
+  if (rows > d.t_cap) {
+    d.t_cap = d.t_rows = 0;
+    for (DeviceBuffer* b : {&d.tH1, &d.tH2, &d.tG2, &d.tG1})
+      if (int st = b->allocate(rows * H * 2)) return st;
+    if (int st = d.tX.allocate(rows * 64 * 2)) return st;
+    if (int st = d.tState.allocate(rows * 8)) return st;
+    if (int st = d.tAbs.allocate(rows * 4)) return st;
+    if (int st = d.tSign.allocate(rows * 4)) return st;
+    d.t_cap = rows;
+  }
+  if (!d.loss_part.ptr)
+    if (int st = d.loss_part.allocate(152 * 16 * 8)) return st;
+  if (!d.t_wmaps) {
+    if (int st = d.tW1p.allocate(H * 64 * 2)) return st;
+    if (int st = d.t_error.allocate(16)) return st;
+    __nv_bfloat16 const* W2 = d.pb.as<__nv_bfloat16>() + d.oW2;
+    if (int st = tma_map_bf16(&d.mW1k, d.tW1p.ptr, H, 64, 64, 128)) return st;
+    if (int st = tma_map_bf16(&d.mW2k, W2, H, H, H, 128)) return st;
+    if (int st = tma_map_bf16(&d.mW2m, W2, H, H, H, 64)) return st;
+    d.t_wmaps = true;
+  }
+  if (rows != d.t_rows) {
+    d.t_rows = 0;
+    if (int st = tma_map_bf16(&d.mXk, d.tX.ptr, rows, 64, 64, 128)) return st;
+    if (int st = tma_map_bf16(&d.mXm, d.tX.ptr, rows, 64, 64, 64)) return st;
+    if (int st = tma_map_bf16(&d.mH1k, d.tH1.ptr, rows, H, H, 128)) return st;
+    if (int st = tma_map_bf16(&d.mH1m, d.tH1.ptr, rows, H, H, 64)) return st;
+    if (int st = tma_map_bf16(&d.mG2k, d.tG2.ptr, rows, H, H, 128)) return st;
+    if (int st = tma_map_bf16(&d.mG2m, d.tG2.ptr, rows, H, H, 64)) return st;
+    if (int st = tma_map_bf16(&d.mG1m, d.tG1.ptr, rows, H, H, 64)) return st;
+    d.t_rows = rows;
+  }
+  if (d.n_sm == 0) SED_TRY_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, d.device));
+  { k_w1_pad<<<blocks_for((int64_t)H * 64), 256, 0, d.stream>>>(d.p.as<float>() + d.oW1, (int)d.n_in, (int)H, d.tW1p.as<__nv_bfloat16>()); note_launches(1); }
+  SED_TRY_CUDA(cudaMemsetAsync(d.t_error.ptr, 0, 4, d.stream));
+  SED_TRY_CUDA(cudaGetLastError());
+  return LS_SUCCESS;
+}
+
+// K splits of a weight gradient: enough CTAs to cover the multiprocessors
+int tc_split(MlpData const& d, int tiles, int k_tiles) {
+  return std::max(1, std::min(k_tiles, (d.n_sm + tiles - 1) / tiles));
+}
+
+// Forward and backward pass of batch rows [0, n) (staged by k_batch): the
+// gradient into d.g, the loss (if requested) into *loss.
+int tc_train_step(MlpData& d, uint64_t n, double* loss) {
+  cudaStream_t s = d.stream;
+  int const H = (int)d.hidden, N = (int)n;
+  float* const G = d.g.as<float>();
+  float const* const P = d.p.as<float>();
+  SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, s));
+  TcGemmArgs base;
+  base.error = d.t_error.as<int>();
+  base.wait_ns = device_wait_ns(kTcWaitNs);
+  // h1 = bf16(tanh(X W1^T + b1)), h2 = bf16(tanh(h1 W2^T + b2))
+  TcGemmArgs f = base;
+  f.M = N;
+  f.N = H;
+  f.k_tiles = 1;
+  f.epilogue = kEpiTanh;
+  f.bias = P + d.ob1;
+  f.out_bf16 = d.tH1.as<__nv_bfloat16>();
+  f.ld_out = H;
+  if (int st = tc_gemm(s, d.mXk, d.mW1k, f, 128)) return st;
+  f.k_tiles = H / 64;
+  f.bias = P + d.ob2;
+  f.out_bf16 = d.tH2.as<__nv_bfloat16>();
+  if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, 128)) return st;
+  // output layer, loss, g2, db2, dW3, db3
+  unsigned const hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 127) / 128, 152 * 16));
+  { k_head<<<hb, 256, 3 * (size_t)H * 4, s>>>(d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, d.pb.as<__nv_bfloat16>() + d.oW3, P + d.ob3, d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>()); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  // g1 = bf16((g2 W2) (1 - h1^2)) and db1; W2 read N-major (element (i, o) at W2[o][i])
+  TcGemmArgs b = base;
+  b.M = N;
+  b.N = H;
+  b.k_tiles = H / 64;
+  b.b_mn = 1;
+  b.epilogue = kEpiBack;
+  b.aux = d.tH1.as<__nv_bfloat16>();
+  b.ld_aux = H;
+  b.colsum = G + d.ob1;
+  b.out_bf16 = d.tG1.as<__nv_bfloat16>();
+  b.ld_out = H;
+  if (int st = tc_gemm(s, d.mG2k, d.mW2m, b, 128)) return st;
+  // dW2 = g2^T h1 and dW1 = g1^T X: K = the batch, both operands read M-/N-major
+  TcGemmArgs w = base;
+  w.M = H;
+  w.N = H;
+  w.k_tiles = (N + 63) / 64;
+  w.a_mn = w.b_mn = 1;
+  w.epilogue = kEpiAdd;
+  w.out_f32 = G + d.oW2;
+  w.ld_f32 = H;
+  w.n_valid = H;
+  w.split = tc_split(d, (H / 128) * (H / 128), w.k_tiles);
+  if (int st = tc_gemm(s, d.mG2m, d.mH1m, w, 128)) return st;
+  w.N = 64;
+  w.out_f32 = G + d.oW1;
+  w.ld_f32 = d.n_in;
+  w.n_valid = (int)d.n_in;
+  w.split = tc_split(d, H / 128, w.k_tiles);
+  if (int st = tc_gemm(s, d.mG1m, d.mXm, w, 64)) return st;
+  if (loss) {
+    std::vector<double> lp(hb);
+    SED_TRY_CUDA(cudaMemcpyAsync(lp.data(), d.loss_part.ptr, hb * 8, cudaMemcpyDeviceToHost, s));
+    SED_TRY_CUDA(cudaStreamSynchronize(s));
+    double t = 0.0;
+    for (double q : lp) t += q;
+    *loss = t / (double)n;
+  }
+  return LS_SUCCESS;
+}
+
+int tc_check_error(MlpData& d) {
+  int err = 0;
+  SED_TRY_CUDA(cudaMemcpyAsync(&err, d.t_error.ptr, 4, cudaMemcpyDeviceToHost, d.stream));
+  SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
+  if (err) return fail(LS_DEVICE_TIMEOUT, "MLP tensor-core training: a wait on the tensor cores or a copy timed out");
+  return LS_SUCCESS;
+}
+
 }  // namespace
 }  // namespace sed
 
@@ -1016,8 +1350,15 @@ int sed_mlp_loss_grad(sed_mlp* m, uint64_t const* states, float const* t_abs, fl
   if (int st = stage(sb, states, n * 8, d.stream)) return st;
   if (int st = stage(ta, t_abs, n * 4, d.stream)) return st;
   if (int st = stage(ts, t_sign, n * 4, d.stream)) return st;
-  if (int st = forward(d, sb.as<uint64_t>(), n, true)) return st;
-  if (int st = backward(d, sb.as<uint64_t>(), n, ta.as<float>(), ts.as<float>(), loss)) return st;
+  if (tc_eligible(d)) {
+    if (int st = tc_train_prepare(d, n)) return st;
+    { k_batch<<<blocks_for((int64_t)n * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), nullptr, 0, (int64_t)n, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
+    if (int st = tc_train_step(d, n, loss)) return st;
+    if (int st = tc_check_error(d)) return st;
+  } else {
+    if (int st = forward(d, sb.as<uint64_t>(), n, true)) return st;
+    if (int st = backward(d, sb.as<uint64_t>(), n, ta.as<float>(), ts.as<float>(), loss)) return st;
+  }
   if (grads) SED_TRY_CUDA(cudaMemcpyAsync(grads, d.g.ptr, d.n_params * 4, cudaMemcpyDefault, d.stream));
   SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
   return LS_SUCCESS;
@@ -1031,8 +1372,49 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
   MlpData& d = m->d;
   ScopedDevice dev(d.device);
   if (int st = wait_for_caller({states, t_abs, t_sign})) return st;
-  // the data set is shuffled on the host once per epoch (an index permutation
-  // from mt19937_64(seed)) and uploaded; batches are contiguous slices of it
+  uint64_t const bsz = std::min<uint64_t>(batch, n);
+  uint64_t const nb = n / bsz;
+  double loss = 0.0;
+  auto adam = [&](__nv_bfloat16* w1p) -> int {
+    ++d.step;
+    float const c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)d.step)));
+    float const c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)d.step)));
+    { k_adam<<<blocks_for((int64_t)d.n_params), 256, 0, d.stream>>>(d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2, w1p, (int)d.n_in, (int64_t)d.hidden * d.n_in); note_launches(1); }
+    return LS_SUCCESS;
+  };
+  if (tc_eligible(d) && n < (1ull << 31)) {
+    // tensor cores: the samples stay on the device; each epoch draws its
+    // batches in the order of a keyed permutation (k_perm, keys from
+    // mt19937_64(seed)) made on the device
+    DeviceBuffer sb, ta, ts, perm;
+    if (int st = stage(sb, states, n * 8, d.stream)) return st;
+    if (int st = stage(ta, t_abs, n * 4, d.stream)) return st;
+    if (int st = stage(ts, t_sign, n * 4, d.stream)) return st;
+    if (int st = perm.allocate(n * 4)) return st;
+    if (int st = tc_train_prepare(d, bsz)) return st;
+    int half = 1;
+    while ((1ull << (2 * half)) < n) ++half;
+    std::mt19937_64 rng(seed);
+    for (unsigned ep = 0; ep < epochs; ++ep) {
+      uint64_t const k01 = rng(), k23 = rng();
+      uint4 const key = make_uint4((uint32_t)k01, (uint32_t)(k01 >> 32), (uint32_t)k23, (uint32_t)(k23 >> 32));
+      { k_perm<<<blocks_for((int64_t)n), 256, 0, d.stream>>>((uint32_t)n, half, key, perm.as<uint32_t>()); note_launches(1); }
+      for (uint64_t bi = 0; bi < nb; ++bi) {
+        { k_batch<<<blocks_for((int64_t)bsz * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), perm.as<uint32_t>(), bi * bsz, (int64_t)bsz, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
+        bool const last = ep + 1 == epochs && bi + 1 == nb;
+        if (int st = tc_train_step(d, bsz, last ? &loss : nullptr)) return st;
+        if (int st = adam(d.tW1p.as<__nv_bfloat16>())) return st;
+      }
+      SED_TRY_CUDA(cudaGetLastError());
+    }
+    d.img_valid = false;
+    if (int st = tc_check_error(d)) return st;
+    if (final_loss) *final_loss = loss;
+    return LS_SUCCESS;
+  }
+  // CUDA cores: the data set is shuffled on the host once per epoch (an index
+  // permutation from mt19937_64(seed)) and uploaded; batches are contiguous
+  // slices of it
   std::vector<uint64_t> hs(n);
   std::vector<float> ha(n), hg(n);
   SED_TRY_CUDA(cudaMemcpy(hs.data(), states, n * 8, cudaMemcpyDefault));
@@ -1047,9 +1429,6 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
   std::mt19937_64 rng(seed);
   std::vector<uint64_t> bs(n);
   std::vector<float> ba(n), bg(n);
-  uint64_t const bsz = std::min<uint64_t>(batch, n);
-  uint64_t const nb = n / bsz;
-  double loss = 0.0;
   for (unsigned ep = 0; ep < epochs; ++ep) {
     std::shuffle(order.begin(), order.end(), rng);
     for (uint64_t q = 0; q < n; ++q) {
@@ -1067,10 +1446,7 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
       if (int st = backward(d, sb.as<uint64_t>() + b0, bsz, ta.as<float>() + b0, ts.as<float>() + b0,
                             last ? &loss : nullptr))
         return st;
-      ++d.step;
-      float const c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)d.step)));
-      float const c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)d.step)));
-      { k_adam<<<blocks_for((int64_t)d.n_params), 256, 0, d.stream>>>(d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2); note_launches(1); }
+      if (int st = adam(nullptr)) return st;
     }
     d.img_valid = false;
     SED_TRY_CUDA(cudaGetLastError());

@@ -79,6 +79,22 @@ __device__ __forceinline__ void bulk_g2s(void* dst, void const* src, uint32_t by
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
 }
+// Tensor (TMA) copy of the 2-D box at element coordinates (x, y) of the
+// tensor map at `map` (a kernel parameter declared __grid_constant__) into
+// shared memory, completion signalled on `bar` as transaction bytes. Boxes
+// that reach past the tensor's edge are filled with zeros. x times the
+// element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(void* dst, void const* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_prefetch_map(void const* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
 // Makes this thread's generic-proxy writes to shared memory visible to the
 // async proxy (the tensor cores read operands through it).
 __device__ __forceinline__ void fence_proxy_async_smem() {
@@ -113,10 +129,25 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
          ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
+// Shared-memory matrix descriptor of an MN-major, 128-byte-swizzled operand
+// slice: each 128-byte row holds 64 consecutive M (or N) elements of one K
+// index, 8 rows (8 K indices) form a 1024-byte atom, and the atoms of 8
+// consecutive K indices follow each other at the stride byte offset 1024;
+// the next 64 M (or N) elements start `mn_stride` bytes further on (the
+// leading byte offset). A K = 16 slice spans two atoms (2048 bytes).
+__device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t saddr, uint32_t mn_stride) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((mn_stride >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
 // Instruction descriptor of kind::f16 with BF16 A and B, FP32 accumulator,
 // both operands K-major, shape M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+// The same with A (bit 15) and / or B (bit 16) MN-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_major(uint32_t M, uint32_t N, bool a_mn, bool b_mn) {
+  return idesc_bf16_f32(M, N) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16);
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.

@@ -82,39 +82,62 @@ def test_tensor_core_start_vector_matches_simt():
     np.testing.assert_allclose(np.abs(v_tc), np.abs(v_simt), rtol=2e-2, atol=1e-3 * np.abs(v_simt).max())
 
 
-@pytest.mark.parametrize("n,h,mask", [(16, 64, 0), (36, 512, lattices.square_sublattice_mask(6))])
-def test_gradients_match_oracle(n, h, mask):
+@pytest.mark.parametrize("n,h,mask,tc,N", [
+    (16, 64, 0, False, 1500), (36, 512, lattices.square_sublattice_mask(6), False, 1500),
+    (36, 512, lattices.square_sublattice_mask(6), True, 1500), (20, 128, 0, True, 1500),
+    (64, 256, 0b1011, True, 1500), (7, 128, 0b101, True, 77), (36, 512, 0, True, 4096)])
+def test_gradients_match_oracle(n, h, mask, tc, N):
+    """Loss and gradient of one batch. CUDA cores (FP32 activations) against
+    the FP64 oracle; tensor cores (the tcgen05 training step, BF16
+    activations, weight gradients through transposed operand reads, ragged
+    last row tiles) against the oracle with the same BF16 rounding points."""
+    from spined import _lib as L
     from spined.learned import Samples
-    rng = np.random.default_rng(7)
+    rng = np.random.default_rng(7 + N + h)
     net = _net(n, h, mask)
+    if not tc:
+        net.set_path(L.SED_MLP_PATH_SIMT)
+    assert net.uses_tensor_cores == tc
     p = net.get_params()
-    N = 1500
+    p[h * n:h * n + h] = rng.normal(scale=0.1, size=h)  # nonzero biases
+    net.set_params(p)
     s = Samples(_random_states(rng, n, N), rng.normal(size=N).astype(np.float32),
                 rng.integers(0, 2, size=N).astype(np.float32))
     loss, g = net.loss_grad(s)
-    want_loss, want_g = M.loss_grad(p, n, h, s.states, s.t_abs.astype(np.float64), s.t_sign, mask)
+    want_loss, want_g = M.loss_grad(p, n, h, s.states, s.t_abs.astype(np.float64), s.t_sign, mask, act_bf16=tc)
     assert loss == pytest.approx(want_loss, rel=1e-5)
-    # per-block tolerance: FP32 sums over N samples against FP64
+    # per-block tolerance: FP32 sums over N samples against FP64 (with BF16
+    # activations also a rare rounding flip of one activation, 2^-8 of it)
+    tol = 1e-3 if tc else 2e-4
     o = 0
     for name, k in [("W1", h * n), ("b1", h), ("W2", h * h), ("b2", h), ("W3", 2 * h), ("b3", 2)]:
         gg, ww = g[o:o + k], want_g[o:o + k]
-        np.testing.assert_allclose(gg, ww, rtol=0, atol=2e-4 * np.abs(ww).max() + 1e-9, err_msg=name)
+        np.testing.assert_allclose(gg, ww, rtol=0, atol=tol * np.abs(ww).max() + 1e-9, err_msg=name)
         o += k
+    if tc:  # the BF16 step is close to the FP32 one too
+        _, g32 = M.loss_grad(p, n, h, s.states, s.t_abs.astype(np.float64), s.t_sign, mask)
+        np.testing.assert_allclose(g, g32, rtol=0, atol=3e-2 * np.abs(g32).max())
 
 
-def test_training_lowers_the_loss():
+@pytest.mark.parametrize("h,tc", [(64, False), (128, True)])
+def test_training_lowers_the_loss(h, tc):
     from spined.learned import Samples
     rng = np.random.default_rng(11)
-    n, h, N = 16, 64, 1 << 14
+    n, N = 16, 1 << 14
     st = _random_states(rng, n, N)
     # a smooth target: log-amplitude = 0.1 * (number of up spins), sign = bit 0
     ones = np.array([bin(int(v)).count("1") for v in st], dtype=np.float32)
     s = Samples(st, 0.1 * ones, (st & np.uint64(1)).astype(np.float32))
     net = _net(n, h)
+    assert net.uses_tensor_cores == tc
     l0, _ = net.loss_grad(s)
-    l1 = net.train(s, epochs=20, batch=1024, lr=3e-3, seed=1)
+    l1 = net.train(s, epochs=20, batch=1000, lr=3e-3, seed=1)  # ragged: 16 batches of 1000, 384 samples unused
     l2, _ = net.loss_grad(s)
     assert l2 < 0.1 * l0, (l0, l1, l2)
+    # a second network, same seed: the same trajectory up to atomic-order rounding
+    net2 = _net(n, h)
+    l1b = net2.train(s, epochs=20, batch=1000, lr=3e-3, seed=1)
+    assert l1b == pytest.approx(l1, rel=0.05)
 
 
 def test_sampler_labels_and_frequencies(sed):
