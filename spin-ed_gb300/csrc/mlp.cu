@@ -264,6 +264,7 @@ __global__ void k_batch(uint64_t const* __restrict__ states, float const* __rest
 // dout_c h2 (dW3) and of dout (db3) go through shared memory into the
 // gradient; the loss partial of the block into loss_partial.
 constexpr int kHeadChunks = 2;  // 8-column chunks per lane: hidden <= 512
+constexpr int kHeadRows = 4;    // rows whose loads a warp issues together
 __global__ void __launch_bounds__(256)
     k_head(__nv_bfloat16 const* __restrict__ h2, int H, int64_t n, __nv_bfloat16 const* __restrict__ W3,
            float const* __restrict__ b3, uint64_t const* __restrict__ bst, float const* __restrict__ bta,
@@ -291,60 +292,81 @@ __global__ void __launch_bounds__(256)
   float const b30 = b3[0], b31 = b3[1], inv_n = 1.0f / (float)n;
   float sd0 = 0.0f, sd1 = 0.0f;
   double l = 0.0;
-  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; r < n; r += (int64_t)gridDim.x * (blockDim.x >> 5)) {
-    float h[kHeadChunks][8];
-    float pa = 0.0f, ps = 0.0f;
+  // warp w takes groups of kHeadRows consecutive rows; each group's loads are
+  // all issued before its arithmetic
+  int64_t const nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * kHeadRows; r0 < n; r0 += nw * kHeadRows) {
+    uint4 u[kHeadRows][kHeadChunks];
+    float ta[kHeadRows], ts[kHeadRows];
+    uint64_t sv[kHeadRows];
 #pragma unroll
-    for (int q = 0; q < kHeadChunks; ++q) {
-      int const ch = lane + 32 * q;
-      uint4 u = make_uint4(0, 0, 0, 0);
-      if (ch < chunks) u = reinterpret_cast<uint4 const*>(h2 + r * H)[ch];
-      uint32_t const wv[4] = {u.x, u.y, u.z, u.w};
+    for (int i = 0; i < kHeadRows; ++i) {
+      int64_t const r = r0 + i;
+      bool const row_ok = r < n;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        h[q][2 * k] = __uint_as_float(wv[k] << 16);
-        h[q][2 * k + 1] = __uint_as_float(wv[k] & 0xFFFF0000u);
+      for (int q = 0; q < kHeadChunks; ++q) {
+        int const ch = lane + 32 * q;
+        u[i][q] = (row_ok && ch < chunks) ? reinterpret_cast<uint4 const*>(h2 + r * H)[ch] : make_uint4(0, 0, 0, 0);
       }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        pa = fmaf(w0[q][j], h[q][j], pa);
-        ps = fmaf(w1[q][j], h[q][j], ps);
-      }
+      ta[i] = row_ok ? bta[r] : 0.0f;
+      ts[i] = row_ok ? bts[r] : 0.0f;
+      sv[i] = row_ok ? bst[r] : 0;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      pa += __shfl_xor_sync(0xffffffffu, pa, o);
-      ps += __shfl_xor_sync(0xffffffffu, ps, o);
-    }
-    float const a = pa + b30, s = ps + b31;
-    float const da = a - bta[r];
-    float const y = fabsf(bts[r] - prior_flip(bst[r], sign_mask));
-    float const pr = 1.0f / (1.0f + expf(-s));
-    float const d0 = 2.0f * da * inv_n, d1 = (pr - y) * inv_n;
-    if (lane == 0) {
-      l += (double)da * da + (double)(fmaxf(s, 0.0f) - s * y + log1pf(expf(-fabsf(s))));
-      sd0 += d0;
-      sd1 += d1;
-    }
+    for (int i = 0; i < kHeadRows; ++i) {
+      int64_t const r = r0 + i;
+      if (r >= n) break;  // warp-uniform
+      float h[kHeadChunks][8];
+      float pa = 0.0f, ps = 0.0f;
 #pragma unroll
-    for (int q = 0; q < kHeadChunks; ++q) {
-      int const ch = lane + 32 * q;
-      if (ch >= chunks) continue;
-      uint32_t pk[4];
+      for (int q = 0; q < kHeadChunks; ++q) {
+        uint32_t const wv[4] = {u[i][q].x, u[i][q].y, u[i][q].z, u[i][q].w};
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        float g[2];
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          int const j = 2 * k + e;
-          g[e] = (d0 * w0[q][j] + d1 * w1[q][j]) * (1.0f - h[q][j] * h[q][j]);
-          ab[q][j] += g[e];
-          a0[q][j] = fmaf(d0, h[q][j], a0[q][j]);
-          a1[q][j] = fmaf(d1, h[q][j], a1[q][j]);
+        for (int k = 0; k < 4; ++k) {
+          h[q][2 * k] = __uint_as_float(wv[k] << 16);
+          h[q][2 * k + 1] = __uint_as_float(wv[k] & 0xFFFF0000u);
         }
-        pk[k] = tc::pack_bf16x2(g[0], g[1]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          pa = fmaf(w0[q][j], h[q][j], pa);
+          ps = fmaf(w1[q][j], h[q][j], ps);
+        }
       }
-      reinterpret_cast<uint4*>(g2 + r * H)[ch] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        pa += __shfl_xor_sync(0xffffffffu, pa, o);
+        ps += __shfl_xor_sync(0xffffffffu, ps, o);
+      }
+      float const a = pa + b30, s = ps + b31;
+      float const da = a - ta[i];
+      float const y = fabsf(ts[i] - prior_flip(sv[i], sign_mask));
+      float const pr = 1.0f / (1.0f + expf(-s));
+      float const d0 = 2.0f * da * inv_n, d1 = (pr - y) * inv_n;
+      if (lane == 0) {
+        l += (double)da * da + (double)(fmaxf(s, 0.0f) - s * y + log1pf(expf(-fabsf(s))));
+        sd0 += d0;
+        sd1 += d1;
+      }
+#pragma unroll
+      for (int q = 0; q < kHeadChunks; ++q) {
+        int const ch = lane + 32 * q;
+        if (ch >= chunks) continue;
+        uint32_t pk[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float g[2];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            int const j = 2 * k + e;
+            g[e] = (d0 * w0[q][j] + d1 * w1[q][j]) * (1.0f - h[q][j] * h[q][j]);
+            ab[q][j] += g[e];
+            a0[q][j] = fmaf(d0, h[q][j], a0[q][j]);
+            a1[q][j] = fmaf(d1, h[q][j], a1[q][j]);
+          }
+          pk[k] = tc::pack_bf16x2(g[0], g[1]);
+        }
+        reinterpret_cast<uint4*>(g2 + r * H)[ch] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
     }
   }
 #pragma unroll
@@ -1151,7 +1173,7 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss) {
   f.out_bf16 = d.tH2.as<__nv_bfloat16>();
   if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, 128)) return st;
   // output layer, loss, g2, db2, dW3, db3
-  unsigned const hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 127) / 128, 152 * 16));
+  unsigned const hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 63) / 64, 152 * 16));  // <= 8 rows a warp
   { k_head<<<hb, 256, 3 * (size_t)H * 4, s>>>(d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, d.pb.as<__nv_bfloat16>() + d.oW3, P + d.ob3, d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>()); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   // g1 = bf16((g2 W2) (1 - h1^2)) and db1; W2 read N-major (element (i, o) at W2[o][i])

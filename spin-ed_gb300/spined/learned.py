@@ -112,6 +112,19 @@ class Mlp(_Handle):
                                             epochs, batch, lr, seed, C.byref(loss)))
         return loss.value
 
+    def train_decayed(self, s: Samples, epochs: int, batch: int = 4096, lr: float = 3e-3, seed: int = 0) -> float:
+        """Three phases of Adam with a falling learning rate: epochs/2 at lr,
+        epochs/4 at lr/3 and the rest at lr/15 (each phase reshuffles from
+        its own seed); returns the loss of the last batch."""
+        e1 = max(1, epochs // 2)
+        e2 = max(0, epochs // 4)
+        e3 = max(0, epochs - e1 - e2)
+        loss = self.train(s, epochs=e1, batch=batch, lr=lr, seed=seed)
+        for k, (e, f) in enumerate(((e2, 1 / 3), (e3, 1 / 15))):
+            if e:
+                loss = self.train(s, epochs=e, batch=batch, lr=lr * f, seed=seed + 1 + k)
+        return loss
+
     def start_vector(self, basis: Basis, out=None):
         """Start vector over the basis (numpy array, or fills a CUDA tensor)."""
         if out is None:

@@ -7,17 +7,17 @@ inversion, all characters +1) every point is solved three ways, all to
 
   random   the plain method: Philox start vector from seed 1234
   warm     the previous point's ground state
-  learned  the start-vector MLP (36 -> 512 -> 512 -> 2), trained on the
-           GPU on configurations sampled from |psi|^2 of the ground states of
-           the two previous points (2^19 per point; the same network is
-           fine-tuned point after point); its tensor-core inference is timed
-           with the solve
+  learned  the start-vector MLP (36 -> 256 -> 256 -> 2), trained on the
+           tensor cores on configurations sampled from |psi|^2 of the ground
+           states of the two previous points (2^19 per point; the same network
+           is fine-tuned point after point, 32 epochs with a falling learning
+           rate); its tensor-core inference is timed with the solve
 
 The first point has no earlier ground state, so it has no warm or learned
 run. The reference has no counterpart: SpinED starts PRIMME from its own
 random vector (src/SpinED.hs:385-394).
 
-    python -m spined.sweep [--precision fp64|mixed] [--epochs 8] [--out sweep.json]
+    python -m spined.sweep [--precision fp64|mixed] [--epochs 32] [--out sweep.json]
 """
 from __future__ import annotations
 
@@ -29,8 +29,8 @@ import time
 import numpy as np
 
 
-def run(L: int = 6, j2s=None, precision: str = "mixed", epochs: int = 8, per_point: int = 1 << 19,
-        hidden: int = 512, lr: float = 3e-3, log=print) -> list[dict]:
+def run(L: int = 6, j2s=None, precision: str = "mixed", epochs: int = 32, per_point: int = 1 << 19,
+        hidden: int = 256, lr: float = 3e-3, log=print) -> list[dict]:
     import torch
     from . import _lib as Lb
     from . import internal as I
@@ -89,7 +89,7 @@ def run(L: int = 6, j2s=None, precision: str = "mixed", epochs: int = 8, per_poi
             t_s, new = timed(lambda: sample(b.basis, prev, per_point, seed=100 + k, sign_mask=mask))
             window = (window + [new])[-2:]
             data = Samples.concat(window)
-            t_tr, loss = timed(lambda: net.train(data, epochs=epochs, batch=4096, lr=lr, seed=k))
+            t_tr, loss = timed(lambda: net.train_decayed(data, epochs=epochs, batch=4096, lr=lr, seed=100 * k))
             row["training"] = {"samples": len(data), "sample_s": t_s, "train_s": t_tr, "final_loss": loss}
         rows.append(row)
         log(json.dumps(row))
@@ -100,7 +100,7 @@ def run(L: int = 6, j2s=None, precision: str = "mixed", epochs: int = 8, per_poi
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--epochs", type=int, default=32)
     ap.add_argument("--side", type=int, default=6)
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
