@@ -1142,9 +1142,10 @@ int tc_train_prepare(MlpData& d, uint64_t rows) {
   return LS_SUCCESS;
 }
 
-// K splits of a weight gradient: enough CTAs to cover the multiprocessors
+// K splits of a weight gradient: as many CTAs as fit on the multiprocessors
+// in one wave (one 128-column CTA per multiprocessor)
 int tc_split(MlpData const& d, int tiles, int k_tiles) {
-  return std::max(1, std::min(k_tiles, (d.n_sm + tiles - 1) / tiles));
+  return std::max(1, std::min(k_tiles, d.n_sm / tiles));
 }
 
 // Forward and backward pass of batch rows [0, n) (staged by k_batch): the
