@@ -162,12 +162,16 @@ __global__ void k_colsum(float const* __restrict__ g, int64_t rows, int cols, fl
 
 // Adam step on the FP32 master copy, refreshing the BF16 copy; with w1p set
 // also the tensor-core training's copy of W1 (the first n_w1 = hidden x
-// n_in parameters), rows padded to 64 inputs.
-__global__ void k_adam(float* __restrict__ p, float const* __restrict__ g, float* __restrict__ m,
+// n_in parameters), rows padded to 64 inputs; with zero_g the gradient is
+// cleared after use.
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, __nv_bfloat16* __restrict__ pb, int64_t n, float lr, float c1,
-                       float c2, __nv_bfloat16* __restrict__ w1p, int n_in, int64_t n_w1) {
+                       float c2, __nv_bfloat16* __restrict__ w1p, int n_in, int64_t n_w1, bool zero_g) {
+  tc::grid_dependency_wait();
+  tc::launch_dependents();
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
     float const gq = g[q];
+    if (zero_g) g[q] = 0.0f;  // the next step's gradient accumulates from zero
     float const mq = 0.9f * m[q] + 0.1f * gq;
     float const vq = 0.999f * v[q] + 0.001f * gq * gq;
     m[q] = mq;
@@ -235,6 +239,8 @@ __global__ void k_batch(uint64_t const* __restrict__ states, float const* __rest
                         float const* __restrict__ t_sign, uint32_t const* __restrict__ perm, uint64_t b0,
                         int64_t rows, int n_in, __nv_bfloat16* __restrict__ X, uint64_t* __restrict__ bst,
                         float* __restrict__ bta, float* __restrict__ bts) {
+  tc::grid_dependency_wait();  // the previous step still reads X and the batch arrays
+  tc::launch_dependents();
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < rows * 8; q += (int64_t)gridDim.x * blockDim.x) {
     int64_t const r = q >> 3;
     int const c = (int)(q & 7);
@@ -277,6 +283,8 @@ __global__ void __launch_bounds__(256)
   for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) sacc[c] = 0.0f;
   if (threadIdx.x < 2) sd[threadIdx.x] = 0.0f;
   __syncthreads();
+  tc::grid_dependency_wait();
+  tc::launch_dependents();
   int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, chunks = H / 8;
   float w0[kHeadChunks][8], w1[kHeadChunks][8], ab[kHeadChunks][8], a0[kHeadChunks][8], a1[kHeadChunks][8];
 #pragma unroll
@@ -1149,13 +1157,15 @@ int tc_split(MlpData const& d, int tiles, int k_tiles) {
 }
 
 // Forward and backward pass of batch rows [0, n) (staged by k_batch): the
-// gradient into d.g, the loss (if requested) into *loss.
-int tc_train_step(MlpData& d, uint64_t n, double* loss) {
+// gradient added into d.g (cleared first with zero_grad), the loss (if
+// requested) into *loss. Every kernel of the step is launched with
+// programmatic stream serialisation.
+int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   cudaStream_t s = d.stream;
   int const H = (int)d.hidden, N = (int)n;
   float* const G = d.g.as<float>();
   float const* const P = d.p.as<float>();
-  SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, s));
+  if (zero_grad) SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, s));
   TcGemmArgs base;
   base.error = d.t_error.as<int>();
   base.wait_ns = device_wait_ns(kTcWaitNs);
@@ -1175,8 +1185,8 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss) {
   if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, 128)) return st;
   // output layer, loss, g2, db2, dW3, db3
   unsigned const hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 63) / 64, 152 * 16));  // <= 8 rows a warp
-  { k_head<<<hb, 256, 3 * (size_t)H * 4, s>>>(d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, d.pb.as<__nv_bfloat16>() + d.oW3, P + d.ob3, d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>()); note_launches(1); }
-  SED_TRY_CUDA(cudaGetLastError());
+  SED_TRY_CUDA(launch_pdl(k_head, dim3(hb), dim3(256), 3 * (size_t)H * 4, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>()));
+  note_launches(1);
   // g1 = bf16((g2 W2) (1 - h1^2)) and db1; W2 read N-major (element (i, o) at W2[o][i])
   TcGemmArgs b = base;
   b.M = N;
@@ -1376,7 +1386,7 @@ int sed_mlp_loss_grad(sed_mlp* m, uint64_t const* states, float const* t_abs, fl
   if (tc_eligible(d)) {
     if (int st = tc_train_prepare(d, n)) return st;
     { k_batch<<<blocks_for((int64_t)n * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), nullptr, 0, (int64_t)n, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
-    if (int st = tc_train_step(d, n, loss)) return st;
+    if (int st = tc_train_step(d, n, loss, true)) return st;
     if (int st = tc_check_error(d)) return st;
   } else {
     if (int st = forward(d, sb.as<uint64_t>(), n, true)) return st;
@@ -1402,7 +1412,13 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
     ++d.step;
     float const c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)d.step)));
     float const c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)d.step)));
-    { k_adam<<<blocks_for((int64_t)d.n_params), 256, 0, d.stream>>>(d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2, w1p, (int)d.n_in, (int64_t)d.hidden * d.n_in); note_launches(1); }
+    dim3 const grid(blocks_for((int64_t)d.n_params));
+    if (w1p) {  // tensor-core step: leaves the gradient cleared for the next one
+      SED_TRY_CUDA(launch_pdl(k_adam, grid, dim3(256), 0, d.stream, d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2, w1p, (int)d.n_in, (int64_t)d.hidden * d.n_in, true));
+    } else {
+      k_adam<<<grid, 256, 0, d.stream>>>(d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2, nullptr, (int)d.n_in, (int64_t)0, false);
+    }
+    note_launches(1);
     return LS_SUCCESS;
   };
   if (tc_eligible(d) && n < (1ull << 31)) {
@@ -1415,6 +1431,7 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
     if (int st = stage(ts, t_sign, n * 4, d.stream)) return st;
     if (int st = perm.allocate(n * 4)) return st;
     if (int st = tc_train_prepare(d, bsz)) return st;
+    SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, d.stream));  // then k_adam clears it each step
     int half = 1;
     while ((1ull << (2 * half)) < n) ++half;
     std::mt19937_64 rng(seed);
@@ -1423,9 +1440,10 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
       uint4 const key = make_uint4((uint32_t)k01, (uint32_t)(k01 >> 32), (uint32_t)k23, (uint32_t)(k23 >> 32));
       { k_perm<<<blocks_for((int64_t)n), 256, 0, d.stream>>>((uint32_t)n, half, key, perm.as<uint32_t>()); note_launches(1); }
       for (uint64_t bi = 0; bi < nb; ++bi) {
-        { k_batch<<<blocks_for((int64_t)bsz * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), perm.as<uint32_t>(), bi * bsz, (int64_t)bsz, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
+        SED_TRY_CUDA(launch_pdl(k_batch, dim3(blocks_for((int64_t)bsz * 8)), dim3(256), 0, d.stream, (uint64_t const*)sb.as<uint64_t>(), (float const*)ta.as<float>(), (float const*)ts.as<float>(), (uint32_t const*)perm.as<uint32_t>(), bi * bsz, (int64_t)bsz, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()));
+        note_launches(1);
         bool const last = ep + 1 == epochs && bi + 1 == nb;
-        if (int st = tc_train_step(d, bsz, last ? &loss : nullptr)) return st;
+        if (int st = tc_train_step(d, bsz, last ? &loss : nullptr, false)) return st;
         if (int st = adam(d.tW1p.as<__nv_bfloat16>())) return st;
       }
       SED_TRY_CUDA(cudaGetLastError());

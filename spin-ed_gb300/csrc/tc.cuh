@@ -231,6 +231,15 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, uint32_t const (&r)[16
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// Programmatic dependent launch. A kernel launched with the programmatic
+// stream serialisation attribute may start while the kernel before it in
+// the stream is still running; grid_dependency_wait blocks until that kernel
+// has completed and its writes are visible (a no-op without the attribute),
+// so nothing before it may touch memory the previous kernels write or read.
+// launch_dependents lets the next such kernel start early.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // Hardware tanh approximation (MUFU.TANH; max relative error about 2^-11).
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;

@@ -100,6 +100,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   __syncthreads();
   tc::fence_after_sync();
   uint32_t const tmem = tmem_slot;
+  // everything above is private to the CTA; the operands and outputs belong
+  // to the kernels before and after this one
+  tc::grid_dependency_wait();
+  tc::launch_dependents();
 
   if (warp == 4) {
     // ---- TMA warp: slab i goes to stage i % S once the MMAs of slab i - S
@@ -275,9 +279,8 @@ int launch(cudaStream_t s, CUtensorMap const& a, CUtensorMap const& b, TcGemmArg
     configured.fetch_or(bit);
   }
   dim3 const grid((unsigned)(args.N / BN), (unsigned)((args.M + 127) / 128), (unsigned)args.split);
-  k_tc_gemm<BN><<<grid, kGemmThreads, GemmShape<BN>::smem, s>>>(a, b, args);
+  SED_TRY_CUDA(launch_pdl(k_tc_gemm<BN>, grid, dim3(kGemmThreads), GemmShape<BN>::smem, s, a, b, args));
   note_launches(1);
-  SED_TRY_CUDA(cudaGetLastError());
   return LS_SUCCESS;
 }
 

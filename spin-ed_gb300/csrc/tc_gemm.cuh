@@ -8,6 +8,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <utility>
 
 #include "sed_internal.hpp"
 
@@ -44,9 +45,30 @@ struct TcGemmArgs {
   uint64_t wait_ns = 0;
 };
 
-// Launches the GEMM on `s`. The map of an operand stored K-major must have
-// boxes of 64 x 128 rows (A) or 64 x tile-width rows (B); an M- or N-major
-// operand's map has boxes of 64 x 64 rows. tile_n: 64 or 128.
+// Launches kernel k on stream s with programmatic stream serialisation: it
+// may start while the previous kernel of the stream finishes, and must call
+// tc::grid_dependency_wait before it touches memory that kernel (or any
+// earlier one) writes or reads.
+template <class... Params, class... Args>
+cudaError_t launch_pdl(void (*k)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
+// Launches the GEMM on `s` (programmatic stream serialisation: the CTAs set
+// up their barriers and tensor memory while the previous kernel finishes).
+// The map of an operand stored K-major must have boxes of 64 x 128 rows (A)
+// or 64 x tile-width rows (B); an M- or N-major operand's map has boxes of
+// 64 x 64 rows. tile_n: 64 or 128.
 int tc_gemm(cudaStream_t s, CUtensorMap const& a, CUtensorMap const& b, TcGemmArgs const& args, int tile_n);
 
 }  // namespace sed
