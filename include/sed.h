@@ -413,6 +413,19 @@ SED_API int sed_mlp_sample(ls_spin_basis const* basis, double const* psi, uint64
  * Pass it to sed_eigh as SED_START_GIVEN. */
 SED_API int sed_mlp_start_vector(sed_mlp* mlp, ls_spin_basis const* basis, double* out);
 
+/* Patch network: the same three layers applied to the `patch` spins around
+ * each of the n_sites sites (patch_sites[i * patch + j] = the j-th site of
+ * site i's patch) and summed over the sites,
+ *   (a, s) = W3 sum_i tanh(W2 tanh(W1 x_i + b1) + b2) + b3,
+ * with the parameter layout of sed_mlp_create for n_inputs = patch. The
+ * parameters do not depend on the lattice: sed_mlp_set_patch_sites binds the
+ * network to another lattice with the same patch shape (for example one
+ * trained on a 4x4 torus to a 6x6 torus). patch <= 64, hidden 64, 128 or 256,
+ * n_sites <= 64; training and inference run on the tensor cores only. */
+SED_API int sed_mlp_create_patch(sed_mlp** out, unsigned n_sites, unsigned patch, uint16_t const* patch_sites,
+                                 unsigned hidden, uint64_t sign_mask, uint64_t seed);
+SED_API int sed_mlp_set_patch_sites(sed_mlp* mlp, unsigned n_sites, uint16_t const* patch_sites, uint64_t sign_mask);
+
 /* Path of every pass. AUTO uses the tensor cores (tcgen05, BF16 operands,
  * FP32 accumulation in tensor memory) when n_inputs <= 64 and hidden is 128,
  * 256 or 512. Inference (sed_mlp_forward, sed_mlp_start_vector) then runs the

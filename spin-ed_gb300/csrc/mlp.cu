@@ -263,14 +263,199 @@ __global__ void k_batch(uint64_t const* __restrict__ states, float const* __rest
   }
 }
 
+constexpr int kHeadChunks = 2;  // 8-column chunks per lane: hidden <= 512
+constexpr int kHeadRows = 4;    // rows whose loads a warp issues together
+
+// Patch network (sed_mlp_create_patch): X row b N + i holds the P spins of
+// site i's patch (patch[i][0..P)) of sample b, zero past P; eight threads
+// per row, 16 bytes each; thread (row b N, chunk 0) also copies sample b's
+// state and targets (t_abs / t_sign may be null: inference).
+__global__ void k_batch_patch(uint64_t const* __restrict__ states, float const* __restrict__ t_abs,
+                              float const* __restrict__ t_sign, uint32_t const* __restrict__ perm, uint64_t b0,
+                              int64_t samples, int n_sites, int P, uint16_t const* __restrict__ patch,
+                              __nv_bfloat16* __restrict__ X, uint64_t* __restrict__ bst, float* __restrict__ bta,
+                              float* __restrict__ bts) {
+  tc::grid_dependency_wait();
+  tc::launch_dependents();
+  int64_t const rows = samples * n_sites;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < rows * 8; q += (int64_t)gridDim.x * blockDim.x) {
+    int64_t const r = q >> 3;
+    int const c = (int)(q & 7);
+    int64_t const b = r / n_sites;
+    int const site = (int)(r - b * n_sites);
+    uint64_t const idx = perm ? perm[b0 + b] : b0 + b;
+    uint64_t const s = states[idx];
+    uint16_t const* const ps = patch + (int64_t)site * P;
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      int const j = 8 * c + 2 * k;
+      uint32_t const lo = j < P ? (((s >> ps[j]) & 1u) ? 0x3F80u : 0xBF80u) : 0u;
+      uint32_t const hi = j + 1 < P ? (((s >> ps[j + 1]) & 1u) ? 0x3F80u : 0xBF80u) : 0u;
+      w[k] = lo | (hi << 16);
+    }
+    reinterpret_cast<uint4*>(X + r * 64)[c] = make_uint4(w[0], w[1], w[2], w[3]);
+    if (site == 0 && c == 0) {
+      bst[b] = s;
+      if (t_abs) bta[b] = t_abs[idx];
+      if (t_sign) bts[b] = t_sign[idx];
+    }
+  }
+}
+
+// Patch network output layer for samples [0, n), one warp per sample over
+// its n_sites rows of h2 (rows b N .. b N + N - 1; lane l holds the 8-column
+// chunks l and l + 32): hs = sum over the sites of h2, (a, s) = W3 hs + b3.
+// With `out` set only (a, s) are written (inference). Otherwise the output
+// gradient as in k_head, g2 = (dout W3) (1 - h2^2) for every site row (BF16),
+// and the sums db2 (unrounded g2), dW3 = dout^T hs, db3 and the loss partial.
+__global__ void __launch_bounds__(256)
+    k_head_patch(__nv_bfloat16 const* __restrict__ h2, int H, int n_sites, int64_t n,
+                 __nv_bfloat16 const* __restrict__ W3, float const* __restrict__ b3,
+                 uint64_t const* __restrict__ bst, float const* __restrict__ bta, float const* __restrict__ bts,
+                 uint64_t sign_mask, __nv_bfloat16* __restrict__ g2, float* __restrict__ db2,
+                 float* __restrict__ dW3, float* __restrict__ db3, double* __restrict__ loss_partial,
+                 float* __restrict__ out) {
+  extern __shared__ float sacc[];  // [3][H]
+  __shared__ double red[32];
+  __shared__ float sd[2];
+  bool const train = out == nullptr;
+  if (train) {
+    for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) sacc[c] = 0.0f;
+    if (threadIdx.x < 2) sd[threadIdx.x] = 0.0f;
+  }
+  __syncthreads();
+  tc::grid_dependency_wait();
+  tc::launch_dependents();
+  int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, chunks = H / 8;
+  float w0[kHeadChunks][8], w1[kHeadChunks][8], ab[kHeadChunks][8], a0[kHeadChunks][8], a1[kHeadChunks][8];
+#pragma unroll
+  for (int q = 0; q < kHeadChunks; ++q) {
+    int const ch = lane + 32 * q;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      w0[q][j] = ch < chunks ? __bfloat162float(W3[8 * ch + j]) : 0.0f;
+      w1[q][j] = ch < chunks ? __bfloat162float(W3[H + 8 * ch + j]) : 0.0f;
+      ab[q][j] = a0[q][j] = a1[q][j] = 0.0f;
+    }
+  }
+  float const b30 = b3[0], b31 = b3[1], inv_n = 1.0f / (float)n;
+  float sd0 = 0.0f, sd1 = 0.0f;
+  double l = 0.0;
+  auto load_row = [&](int64_t row, float (&h)[kHeadChunks][8]) {
+#pragma unroll
+    for (int q = 0; q < kHeadChunks; ++q) {
+      int const ch = lane + 32 * q;
+      uint4 const u = ch < chunks ? reinterpret_cast<uint4 const*>(h2 + row * H)[ch] : make_uint4(0, 0, 0, 0);
+      uint32_t const wv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        h[q][2 * k] = __uint_as_float(wv[k] << 16);
+        h[q][2 * k + 1] = __uint_as_float(wv[k] & 0xFFFF0000u);
+      }
+    }
+  };
+  int64_t const nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; b < n; b += nw) {
+    float hs[kHeadChunks][8] = {};
+    int64_t const r0 = b * n_sites;
+    for (int i = 0; i < n_sites; ++i) {
+      float h[kHeadChunks][8];
+      load_row(r0 + i, h);
+#pragma unroll
+      for (int q = 0; q < kHeadChunks; ++q)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) hs[q][j] += h[q][j];
+    }
+    float pa = 0.0f, ps = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kHeadChunks; ++q)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        pa = fmaf(w0[q][j], hs[q][j], pa);
+        ps = fmaf(w1[q][j], hs[q][j], ps);
+      }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      pa += __shfl_xor_sync(0xffffffffu, pa, o);
+      ps += __shfl_xor_sync(0xffffffffu, ps, o);
+    }
+    float const a = pa + b30, s = ps + b31;
+    if (!train) {
+      if (lane == 0) {
+        out[2 * b] = a;
+        out[2 * b + 1] = s;
+      }
+      continue;
+    }
+    float const da = a - bta[b];
+    float const y = fabsf(bts[b] - prior_flip(bst[b], sign_mask));
+    float const pr = 1.0f / (1.0f + expf(-s));
+    float const d0 = 2.0f * da * inv_n, d1 = (pr - y) * inv_n;
+    if (lane == 0) {
+      l += (double)da * da + (double)(fmaxf(s, 0.0f) - s * y + log1pf(expf(-fabsf(s))));
+      sd0 += d0;
+      sd1 += d1;
+    }
+#pragma unroll
+    for (int q = 0; q < kHeadChunks; ++q)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        a0[q][j] = fmaf(d0, hs[q][j], a0[q][j]);
+        a1[q][j] = fmaf(d1, hs[q][j], a1[q][j]);
+      }
+    for (int i = 0; i < n_sites; ++i) {
+      float h[kHeadChunks][8];
+      load_row(r0 + i, h);
+#pragma unroll
+      for (int q = 0; q < kHeadChunks; ++q) {
+        int const ch = lane + 32 * q;
+        if (ch >= chunks) continue;
+        uint32_t pk[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float g[2];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            int const j = 2 * k + e;
+            g[e] = (d0 * w0[q][j] + d1 * w1[q][j]) * (1.0f - h[q][j] * h[q][j]);
+            ab[q][j] += g[e];
+          }
+          pk[k] = tc::pack_bf16x2(g[0], g[1]);
+        }
+        reinterpret_cast<uint4*>(g2 + (r0 + i) * H)[ch] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+  }
+  if (!train) return;
+#pragma unroll
+  for (int q = 0; q < kHeadChunks; ++q) {
+    int const ch = lane + 32 * q;
+    if (ch >= chunks) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      atomicAdd(&sacc[8 * ch + j], ab[q][j]);
+      atomicAdd(&sacc[H + 8 * ch + j], a0[q][j]);
+      atomicAdd(&sacc[2 * H + 8 * ch + j], a1[q][j]);
+    }
+  }
+  if (lane == 0) {
+    atomicAdd(&sd[0], sd0);
+    atomicAdd(&sd[1], sd1);
+  }
+  double const tot = block_sum(l, red);
+  if (threadIdx.x == 0) loss_partial[blockIdx.x] = tot;
+  __syncthreads();
+  for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) atomicAdd(c < H ? db2 + c : dW3 + (c - H), sacc[c]);
+  if (threadIdx.x < 2) atomicAdd(db3 + threadIdx.x, sd[threadIdx.x]);
+}
+
 // Output layer, loss and first backward step for rows [0, n): one warp per
 // row, lane l holding the 8-column chunks l and l + 32 of h2. Per row
 // (a, s) = W3 h2 + b3 (warp sums), the output gradient as in k_out_grad,
 // g2 = (dout W3) (1 - h2^2) written as BF16; the row sums of g2 (db2), of
 // dout_c h2 (dW3) and of dout (db3) go through shared memory into the
 // gradient; the loss partial of the block into loss_partial.
-constexpr int kHeadChunks = 2;  // 8-column chunks per lane: hidden <= 512
-constexpr int kHeadRows = 4;    // rows whose loads a warp issues together
 __global__ void __launch_bounds__(256)
     k_head(__nv_bfloat16 const* __restrict__ h2, int H, int64_t n, __nv_bfloat16 const* __restrict__ W3,
            float const* __restrict__ b3, uint64_t const* __restrict__ bst, float const* __restrict__ bta,
@@ -950,8 +1135,12 @@ struct MlpData {
   // states and targets, the padded BF16 copy of W1, an error flag, and the
   // tensor maps over them (K-major "k" and M-/N-major "m" boxes)
   DeviceBuffer tX, tH1, tH2, tG2, tG1, tW1p, tState, tAbs, tSign, t_error;
-  uint64_t t_cap = 0, t_rows = 0;
+  uint64_t t_cap = 0, t_cap_samples = 0, t_rows = 0;
   bool t_wmaps = false;
+  // patch network (n_sites > 0): the n_in = P sites of each site's patch,
+  // [n_sites][P] on the device; one activation row per (sample, site)
+  unsigned n_sites = 0;
+  DeviceBuffer patch_dev;
   CUtensorMap mXk{}, mXm{}, mW1k{}, mH1k{}, mH1m{}, mW2k{}, mW2m{}, mG2k{}, mG2m{}, mG1m{};
   ~MlpData() {
     if (stream) cudaStreamDestroy(stream);
@@ -1043,6 +1232,7 @@ int backward(MlpData& d, uint64_t const* states, uint64_t n, float const* t_abs,
 }
 
 bool tc_eligible(MlpData const& d) {
+  if (d.n_sites) return true;  // patch networks run on the tensor cores only (checked at creation)
   return d.path != SED_MLP_PATH_SIMT && d.n_in <= 64 && (d.hidden == 128 || d.hidden == 256 || d.hidden == 512);
 }
 
@@ -1106,20 +1296,32 @@ int stage(DeviceBuffer& buf, void const* src, size_t bytes, cudaStream_t s) {
   return LS_SUCCESS;
 }
 
-// Tensor-core training: buffers for batches of up to `rows` rows, tensor
-// maps for batches of exactly `rows` rows (rows past them read as zero), the
-// padded W1 copy refreshed from the FP32 master, the error flag cleared.
-int tc_train_prepare(MlpData& d, uint64_t rows) {
-  uint64_t const H = d.hidden;
+// Activation rows of a batch: one per sample, or one per (sample, site) for
+// a patch network.
+uint64_t tc_rows(MlpData const& d, uint64_t samples) { return samples * (d.n_sites ? d.n_sites : 1u); }
+// Output tile width of the hidden-layer GEMMs.
+int tc_tile(MlpData const& d) { return d.hidden >= 128 ? 128 : 64; }
+
+// Tensor-core training: buffers for batches of up to `samples` samples,
+// tensor maps for batches of exactly `samples` (rows past them read as
+// zero); with `reset` also the padded W1 copy refreshed from the FP32 master
+// and the error flag cleared.
+int tc_train_prepare(MlpData& d, uint64_t samples, bool reset = true) {
+  uint64_t const H = d.hidden, rows = tc_rows(d, samples);
+  uint32_t const tn = (uint32_t)tc_tile(d);
   if (rows > d.t_cap) {
     d.t_cap = d.t_rows = 0;
     for (DeviceBuffer* b : {&d.tH1, &d.tH2, &d.tG2, &d.tG1})
       if (int st = b->allocate(rows * H * 2)) return st;
     if (int st = d.tX.allocate(rows * 64 * 2)) return st;
-    if (int st = d.tState.allocate(rows * 8)) return st;
-    if (int st = d.tAbs.allocate(rows * 4)) return st;
-    if (int st = d.tSign.allocate(rows * 4)) return st;
     d.t_cap = rows;
+  }
+  if (samples > d.t_cap_samples) {
+    d.t_cap_samples = 0;
+    if (int st = d.tState.allocate(samples * 8)) return st;
+    if (int st = d.tAbs.allocate(samples * 4)) return st;
+    if (int st = d.tSign.allocate(samples * 4)) return st;
+    d.t_cap_samples = samples;
   }
   if (!d.loss_part.ptr)
     if (int st = d.loss_part.allocate(152 * 16 * 8)) return st;
@@ -1127,8 +1329,8 @@ int tc_train_prepare(MlpData& d, uint64_t rows) {
     if (int st = d.tW1p.allocate(H * 64 * 2)) return st;
     if (int st = d.t_error.allocate(16)) return st;
     __nv_bfloat16 const* W2 = d.pb.as<__nv_bfloat16>() + d.oW2;
-    if (int st = tma_map_bf16(&d.mW1k, d.tW1p.ptr, H, 64, 64, 128)) return st;
-    if (int st = tma_map_bf16(&d.mW2k, W2, H, H, H, 128)) return st;
+    if (int st = tma_map_bf16(&d.mW1k, d.tW1p.ptr, H, 64, 64, tn)) return st;
+    if (int st = tma_map_bf16(&d.mW2k, W2, H, H, H, tn)) return st;
     if (int st = tma_map_bf16(&d.mW2m, W2, H, H, H, 64)) return st;
     d.t_wmaps = true;
   }
@@ -1144,9 +1346,11 @@ int tc_train_prepare(MlpData& d, uint64_t rows) {
     d.t_rows = rows;
   }
   if (d.n_sm == 0) SED_TRY_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, d.device));
-  { k_w1_pad<<<blocks_for((int64_t)H * 64), 256, 0, d.stream>>>(d.p.as<float>() + d.oW1, (int)d.n_in, (int)H, d.tW1p.as<__nv_bfloat16>()); note_launches(1); }
-  SED_TRY_CUDA(cudaMemsetAsync(d.t_error.ptr, 0, 4, d.stream));
-  SED_TRY_CUDA(cudaGetLastError());
+  if (reset) {
+    { k_w1_pad<<<blocks_for((int64_t)H * 64), 256, 0, d.stream>>>(d.p.as<float>() + d.oW1, (int)d.n_in, (int)H, d.tW1p.as<__nv_bfloat16>()); note_launches(1); }
+    SED_TRY_CUDA(cudaMemsetAsync(d.t_error.ptr, 0, 4, d.stream));
+    SED_TRY_CUDA(cudaGetLastError());
+  }
   return LS_SUCCESS;
 }
 
@@ -1162,7 +1366,7 @@ int tc_split(MlpData const& d, int tiles, int k_tiles) {
 // programmatic stream serialisation.
 int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   cudaStream_t s = d.stream;
-  int const H = (int)d.hidden, N = (int)n;
+  int const H = (int)d.hidden, N = (int)tc_rows(d, n), tn = tc_tile(d);
   float* const G = d.g.as<float>();
   float const* const P = d.p.as<float>();
   if (zero_grad) SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, s));
@@ -1178,14 +1382,20 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   f.bias = P + d.ob1;
   f.out_bf16 = d.tH1.as<__nv_bfloat16>();
   f.ld_out = H;
-  if (int st = tc_gemm(s, d.mXk, d.mW1k, f, 128)) return st;
+  if (int st = tc_gemm(s, d.mXk, d.mW1k, f, tn)) return st;
   f.k_tiles = H / 64;
   f.bias = P + d.ob2;
   f.out_bf16 = d.tH2.as<__nv_bfloat16>();
-  if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, 128)) return st;
+  if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, tn)) return st;
   // output layer, loss, g2, db2, dW3, db3
-  unsigned const hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 63) / 64, 152 * 16));  // <= 8 rows a warp
-  SED_TRY_CUDA(launch_pdl(k_head, dim3(hb), dim3(256), 3 * (size_t)H * 4, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>()));
+  unsigned hb;
+  if (d.n_sites) {  // one warp per sample
+    hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 7) / 8, 152 * 16));
+    SED_TRY_CUDA(launch_pdl(k_head_patch, dim3(hb), dim3(256), 3 * (size_t)H * 4, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int)d.n_sites, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>(), (float*)nullptr));
+  } else {
+    hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 63) / 64, 152 * 16));  // <= 8 rows a warp
+    SED_TRY_CUDA(launch_pdl(k_head, dim3(hb), dim3(256), 3 * (size_t)H * 4, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>()));
+  }
   note_launches(1);
   // g1 = bf16((g2 W2) (1 - h1^2)) and db1; W2 read N-major (element (i, o) at W2[o][i])
   TcGemmArgs b = base;
@@ -1199,7 +1409,7 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   b.colsum = G + d.ob1;
   b.out_bf16 = d.tG1.as<__nv_bfloat16>();
   b.ld_out = H;
-  if (int st = tc_gemm(s, d.mG2k, d.mW2m, b, 128)) return st;
+  if (int st = tc_gemm(s, d.mG2k, d.mW2m, b, tn)) return st;
   // dW2 = g2^T h1 and dW1 = g1^T X: K = the batch, both operands read M-/N-major
   TcGemmArgs w = base;
   w.M = H;
@@ -1210,13 +1420,14 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   w.out_f32 = G + d.oW2;
   w.ld_f32 = H;
   w.n_valid = H;
-  w.split = tc_split(d, (H / 128) * (H / 128), w.k_tiles);
-  if (int st = tc_gemm(s, d.mG2m, d.mH1m, w, 128)) return st;
+  int const m_tiles = (H + 127) / 128;
+  w.split = tc_split(d, m_tiles * (H / tn), w.k_tiles);
+  if (int st = tc_gemm(s, d.mG2m, d.mH1m, w, tn)) return st;
   w.N = 64;
   w.out_f32 = G + d.oW1;
   w.ld_f32 = d.n_in;
   w.n_valid = (int)d.n_in;
-  w.split = tc_split(d, H / 128, w.k_tiles);
+  w.split = tc_split(d, m_tiles, w.k_tiles);
   if (int st = tc_gemm(s, d.mG1m, d.mXm, w, 64)) return st;
   if (loss) {
     std::vector<double> lp(hb);
@@ -1235,6 +1446,42 @@ int tc_check_error(MlpData& d) {
   SED_TRY_CUDA(cudaStreamSynchronize(d.stream));
   if (err) return fail(LS_DEVICE_TIMEOUT, "MLP tensor-core training: a wait on the tensor cores or a copy timed out");
   return LS_SUCCESS;
+}
+
+// Patch network inference: (a, s) for states[0..n) (device) into out[2 n]
+// (device), in chunks of about 2^21 activation rows through the training
+// step's forward GEMMs and k_head_patch.
+int forward_patch(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
+  if (n == 0) return LS_SUCCESS;
+  cudaStream_t s = d.stream;
+  int const H = (int)d.hidden, tn = tc_tile(d);
+  uint64_t const chunk = std::max<uint64_t>(1, ((uint64_t)1 << 21) / d.n_sites);
+  for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
+    uint64_t const nb = std::min(chunk, n - b0);
+    if (int st = tc_train_prepare(d, nb, b0 == 0)) return st;
+    int64_t const rows = (int64_t)tc_rows(d, nb);
+    SED_TRY_CUDA(launch_pdl(k_batch_patch, dim3(blocks_for(rows * 8)), dim3(256), 0, s, states, (float const*)nullptr, (float const*)nullptr, (uint32_t const*)nullptr, b0, (int64_t)nb, (int)d.n_sites, (int)d.n_in, (uint16_t const*)d.patch_dev.as<uint16_t>(), d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()));
+    note_launches(1);
+    TcGemmArgs f;
+    f.error = d.t_error.as<int>();
+    f.wait_ns = device_wait_ns(kTcWaitNs);
+    f.M = (int)rows;
+    f.N = H;
+    f.k_tiles = 1;
+    f.epilogue = kEpiTanh;
+    f.bias = d.p.as<float>() + d.ob1;
+    f.out_bf16 = d.tH1.as<__nv_bfloat16>();
+    f.ld_out = H;
+    if (int st = tc_gemm(s, d.mXk, d.mW1k, f, tn)) return st;
+    f.k_tiles = H / 64;
+    f.bias = d.p.as<float>() + d.ob2;
+    f.out_bf16 = d.tH2.as<__nv_bfloat16>();
+    if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, tn)) return st;
+    unsigned const hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((nb + 7) / 8, 152 * 16));
+    SED_TRY_CUDA(launch_pdl(k_head_patch, dim3(hb), dim3(256), 0, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int)d.n_sites, (int64_t)nb, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), (float const*)(d.p.as<float>() + d.ob3), (uint64_t const*)nullptr, (float const*)nullptr, (float const*)nullptr, d.sign_mask, (__nv_bfloat16*)nullptr, (float*)nullptr, (float*)nullptr, (float*)nullptr, (double*)nullptr, out + 2 * b0));
+    note_launches(1);
+  }
+  return tc_check_error(d);
 }
 
 }  // namespace
@@ -1310,6 +1557,46 @@ int sed_mlp_create(sed_mlp** out, unsigned n_inputs, unsigned hidden, uint64_t s
   return LS_SUCCESS;
 }
 
+int sed_mlp_set_patch_sites(sed_mlp* m, unsigned n_sites, uint16_t const* patch_sites, uint64_t sign_mask) {
+  if (!m || !patch_sites || n_sites == 0) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_patch_sites: bad argument");
+  MlpData& d = m->d;
+  if (!d.n_sites) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_patch_sites: not a patch network");
+  if (n_sites > 64) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_patch_sites: at most 64 sites");
+  if (n_sites < 64 && (sign_mask >> n_sites) != 0)
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_patch_sites: sign_mask has bits beyond n_sites");
+  for (uint64_t q = 0; q < (uint64_t)n_sites * d.n_in; ++q)
+    if (patch_sites[q] >= n_sites) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_patch_sites: site out of range");
+  ScopedDevice dev(d.device);
+  DeviceBuffer buf;
+  if (int st = buf.allocate((size_t)n_sites * d.n_in * 2)) return st;
+  SED_TRY_CUDA(cudaMemcpy(buf.ptr, patch_sites, (size_t)n_sites * d.n_in * 2, cudaMemcpyHostToDevice));
+  SED_TRY_CUDA(cudaStreamSynchronize(d.stream));  // no pass of the old geometry is in flight
+  d.patch_dev = std::move(buf);
+  d.n_sites = n_sites;
+  d.sign_mask = sign_mask;
+  d.t_rows = 0;  // activation rows per sample changed: new tensor maps
+  return LS_SUCCESS;
+}
+
+int sed_mlp_create_patch(sed_mlp** out, unsigned n_sites, unsigned patch, uint16_t const* patch_sites,
+                         unsigned hidden, uint64_t sign_mask, uint64_t seed) {
+  if (!out) return fail(LS_INVALID_ARGUMENT, "sed_mlp_create_patch: NULL argument");
+  *out = nullptr;
+  if (patch == 0 || patch > 64 || (hidden != 64 && hidden != 128 && hidden != 256))
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_create_patch: patch must be 1..64 and hidden 64, 128 or 256");
+  if (n_sites == 0 || n_sites > 64 || !patch_sites)
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_create_patch: n_sites must be 1..64 with a patch table");
+  sed_mlp* m = nullptr;
+  if (int st = sed_mlp_create(&m, patch, hidden, 0, seed)) return st;
+  m->d.n_sites = 1;  // marks the patch network for the check below
+  if (int st = sed_mlp_set_patch_sites(m, n_sites, patch_sites, sign_mask)) {
+    sed_mlp_destroy(m);
+    return st;
+  }
+  *out = m;
+  return LS_SUCCESS;
+}
+
 void sed_mlp_destroy(sed_mlp* m) {
   if (!m) return;
   ScopedDevice dev(m->d.device);
@@ -1322,6 +1609,8 @@ int sed_mlp_set_path(sed_mlp* m, int path) {
   if (!m) return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_path: NULL argument");
   if (path != SED_MLP_PATH_AUTO && path != SED_MLP_PATH_SIMT)
     return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_path: unknown path");
+  if (m->d.n_sites && path == SED_MLP_PATH_SIMT)
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_set_path: a patch network runs on the tensor cores only");
   m->d.path = path;
   return LS_SUCCESS;
 }
@@ -1360,7 +1649,10 @@ int sed_mlp_forward(sed_mlp* m, uint64_t const* states, uint64_t n, float* out) 
   for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
     uint64_t const nb = std::min(chunk, n - b0);
     SED_TRY_CUDA(cudaMemcpyAsync(sbuf.ptr, states + b0, nb * 8, cudaMemcpyDefault, d.stream));
-    if (tc_path) {
+    if (d.n_sites) {
+      if (int st = ensure_batch(d, nb, false)) return st;
+      if (int st = forward_patch(d, sbuf.as<uint64_t>(), nb, d.out.as<float>())) return st;
+    } else if (tc_path) {
       if (int st = ensure_batch(d, nb, false)) return st;
       if (int st = forward_tc(d, sbuf.as<uint64_t>(), nb, d.out.as<float>())) return st;
     } else if (int st = forward(d, sbuf.as<uint64_t>(), nb, false)) {
@@ -1385,7 +1677,11 @@ int sed_mlp_loss_grad(sed_mlp* m, uint64_t const* states, float const* t_abs, fl
   if (int st = stage(ts, t_sign, n * 4, d.stream)) return st;
   if (tc_eligible(d)) {
     if (int st = tc_train_prepare(d, n)) return st;
-    { k_batch<<<blocks_for((int64_t)n * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), nullptr, 0, (int64_t)n, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
+    if (d.n_sites) {
+      { k_batch_patch<<<blocks_for((int64_t)tc_rows(d, n) * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), nullptr, 0, (int64_t)n, (int)d.n_sites, (int)d.n_in, d.patch_dev.as<uint16_t>(), d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
+    } else {
+      { k_batch<<<blocks_for((int64_t)n * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), nullptr, 0, (int64_t)n, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
+    }
     if (int st = tc_train_step(d, n, loss, true)) return st;
     if (int st = tc_check_error(d)) return st;
   } else {
@@ -1421,6 +1717,8 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
     note_launches(1);
     return LS_SUCCESS;
   };
+  if (d.n_sites && n >= (1ull << 31))
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_train: a patch network trains on at most 2^31 - 1 samples");
   if (tc_eligible(d) && n < (1ull << 31)) {
     // tensor cores: the samples stay on the device; each epoch draws its
     // batches in the order of a keyed permutation (k_perm, keys from
@@ -1440,7 +1738,10 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
       uint4 const key = make_uint4((uint32_t)k01, (uint32_t)(k01 >> 32), (uint32_t)k23, (uint32_t)(k23 >> 32));
       { k_perm<<<blocks_for((int64_t)n), 256, 0, d.stream>>>((uint32_t)n, half, key, perm.as<uint32_t>()); note_launches(1); }
       for (uint64_t bi = 0; bi < nb; ++bi) {
-        SED_TRY_CUDA(launch_pdl(k_batch, dim3(blocks_for((int64_t)bsz * 8)), dim3(256), 0, d.stream, (uint64_t const*)sb.as<uint64_t>(), (float const*)ta.as<float>(), (float const*)ts.as<float>(), (uint32_t const*)perm.as<uint32_t>(), bi * bsz, (int64_t)bsz, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()));
+        if (d.n_sites)
+          SED_TRY_CUDA(launch_pdl(k_batch_patch, dim3(blocks_for((int64_t)tc_rows(d, bsz) * 8)), dim3(256), 0, d.stream, (uint64_t const*)sb.as<uint64_t>(), (float const*)ta.as<float>(), (float const*)ts.as<float>(), (uint32_t const*)perm.as<uint32_t>(), bi * bsz, (int64_t)bsz, (int)d.n_sites, (int)d.n_in, (uint16_t const*)d.patch_dev.as<uint16_t>(), d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()));
+        else
+          SED_TRY_CUDA(launch_pdl(k_batch, dim3(blocks_for((int64_t)bsz * 8)), dim3(256), 0, d.stream, (uint64_t const*)sb.as<uint64_t>(), (float const*)ta.as<float>(), (float const*)ts.as<float>(), (uint32_t const*)perm.as<uint32_t>(), bi * bsz, (int64_t)bsz, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()));
         note_launches(1);
         bool const last = ep + 1 == epochs && bi + 1 == nb;
         if (int st = tc_train_step(d, bsz, last ? &loss : nullptr, false)) return st;
@@ -1558,7 +1859,9 @@ int sed_mlp_start_vector(sed_mlp* m, ls_spin_basis const* basis, double* out) {
   MlpData& d = m->d;
   BasisData& b = *basis->d;
   if (!b.built) return fail(LS_CACHE_NOT_BUILT, "basis has not been built (call ls_build)");
-  if (b.n != d.n_in) return fail(LS_DIMENSION_MISMATCH, "sed_mlp_start_vector: network inputs != number of spins");
+  if (d.n_sites ? b.n != d.n_sites : b.n != d.n_in)
+    return fail(LS_DIMENSION_MISMATCH, d.n_sites ? "sed_mlp_start_vector: patch table sites != number of spins"
+                                                 : "sed_mlp_start_vector: network inputs != number of spins");
   if (b.D == 0) return LS_SUCCESS;
   ScopedDevice dev(d.device);
   if (int st = wait_for_caller({out})) return st;
@@ -1566,7 +1869,9 @@ int sed_mlp_start_vector(sed_mlp* m, ls_spin_basis const* basis, double* out) {
   DeviceBuffer amp, part, vout;
   if (int st = amp.allocate(D * 8)) return st;  // (a, s) pairs
   if (int st = part.allocate(152 * 16 * 4)) return st;
-  if (tc_eligible(d)) {
+  if (d.n_sites) {
+    if (int st = forward_patch(d, b.reps.as<uint64_t>(), D, amp.as<float>())) return st;
+  } else if (tc_eligible(d)) {
     if (int st = forward_tc(d, b.reps.as<uint64_t>(), D, amp.as<float>())) return st;
   } else {
     for (uint64_t b0 = 0; b0 < D; b0 += chunk) {

@@ -149,6 +149,8 @@ SIGNATURES = [
     ("sed_mlp_sample", _I, [_P, _P, _U64, _U64, _U64, _P, _P, _P]),
     ("sed_mlp_start_vector", _I, [_P, _P, _P]),
     ("sed_mlp_set_path", _I, [_P, _I]),
+    ("sed_mlp_create_patch", _I, [C.POINTER(_P), _U, _U, _P, _U, _U64, _U64]),
+    ("sed_mlp_set_patch_sites", _I, [_P, _U, _P, _U64]),
     ("sed_release_workspace", None, []),
     ("sed_set_batched_launch", None, [C.c_uint, C.c_uint]),
     ("sed_rotate_vectors", _I, [_P, _U64, C.c_uint32, _P, C.c_uint32, _U64, _I, _P]),

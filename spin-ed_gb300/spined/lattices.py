@@ -133,3 +133,14 @@ def square_sublattice_mask(L: int) -> int:
 def chain_sublattice_mask(n: int) -> int:
     """Even sites of a ring of even length n."""
     return sum(1 << i for i in range(0, n, 2))
+
+
+def square_patches(L: int, radius: int = 1) -> np.ndarray:
+    """(L*L, (2 radius + 1)^2) patch table of the L x L torus: row i lists the
+    sites of the square window around site i, offsets (dx, dy) in row-major
+    order, so every site's patch has the same shape on any L (the input of
+    the size-independent patch network)."""
+    idx = lambda x, y: (y % L) * L + (x % L)
+    offs = [(dx, dy) for dy in range(-radius, radius + 1) for dx in range(-radius, radius + 1)]
+    return np.array([[idx(x + dx, y + dy) for dx, dy in offs] for y in range(L) for x in range(L)], dtype=np.uint16)
+

@@ -131,3 +131,24 @@ class Mlp(_Handle):
             out = np.zeros(get_number_states(basis), np.float64)
         check_status(L.load().sed_mlp_start_vector(self.ptr, basis.ptr, _ptr(out)))
         return out
+
+
+class PatchMlp(Mlp):
+    """Size-independent network (sed_mlp_create_patch): the MLP applied to
+    every site's patch of spins and summed over the sites. `patches` is an
+    (n_sites, P) integer array of site indices; `rebind` moves the trained
+    network to another lattice with the same patch shape."""
+
+    def __init__(self, patches, hidden: int = 128, sign_mask: int = 0, seed: int = 0):
+        t = np.ascontiguousarray(patches, dtype=np.uint16)
+        n, P = t.shape
+        _Handle.__init__(self, _mk(L.load().sed_mlp_create_patch, n, P, C.c_void_p(t.ctypes.data), hidden,
+                                   sign_mask, seed))
+        self.n_inputs, self.hidden, self.sign_mask, self.n_sites = P, hidden, sign_mask, n
+
+    def rebind(self, patches, sign_mask: int = 0) -> None:
+        t = np.ascontiguousarray(patches, dtype=np.uint16)
+        assert t.shape[1] == self.n_inputs, "the patch shape must stay the same"
+        check_status(L.load().sed_mlp_set_patch_sites(self.ptr, t.shape[0], C.c_void_p(t.ctypes.data), sign_mask))
+        self.n_sites, self.sign_mask = t.shape[0], sign_mask
+

@@ -58,3 +58,38 @@ def test_spins_and_parity():
     st = np.array([0b0110, 0b1111, 0], dtype=np.uint64)
     np.testing.assert_array_equal(M.spins(st, 4)[0], [-1, 1, 1, -1])
     np.testing.assert_array_equal(M.parity(st, 0b0011), [1, 0, 0])
+
+
+@pytest.mark.parametrize("mask", [0, 0b0110])
+def test_patch_gradient_matches_finite_differences(mask):
+    """The patch network (per-site MLP summed over sites): analytic gradient
+    against central differences, and the same parameters on two lattice sizes."""
+    rng = np.random.default_rng(9)
+    h, P = 5, 3
+    patches = np.array([[i, (i + 1) % 4, (i + 3) % 4] for i in range(4)])  # ring of 4, neighbours
+    size = h * P + h + h * h + h + 2 * h + 2
+    p = (rng.integers(-96, 96, size=size) / 64).astype(np.float32)
+    st = rng.integers(0, 16, size=21).astype(np.uint64)
+    ta = rng.normal(size=21)
+    ts = rng.integers(0, 2, size=21).astype(np.float32)
+    loss, g = M.patch_loss_grad(p, h, st, patches, ta, ts, mask)
+
+    def f(q):
+        w = _unpack64(q, P, h)
+        x = M.patch_spins(st, patches)
+        h1 = np.tanh(x @ w["W1"].T + w["b1"])
+        h2 = np.tanh(h1 @ w["W2"].T + w["b2"])
+        o = h2.sum(axis=1) @ w["W3"].T + w["b3"]
+        y = np.abs(ts - M.parity(st, mask))
+        a, s = o[:, 0], o[:, 1]
+        return np.mean((a - ta) ** 2 + np.maximum(s, 0) - s * y + np.log1p(np.exp(-np.abs(s))))
+
+    q = p.astype(np.float64)
+    assert loss == pytest.approx(f(q), rel=1e-14)
+    eps = 1e-6
+    fd = np.array([(f(q + eps * e) - f(q - eps * e)) / (2 * eps) for e in np.eye(len(q))])
+    np.testing.assert_allclose(g, fd, atol=1e-8, rtol=1e-6)
+    # translation invariance: rotating every state of the ring leaves the outputs unchanged
+    rot = ((st << np.uint64(1)) | (st >> np.uint64(3))) & np.uint64(15)
+    np.testing.assert_allclose(M.patch_forward(p, h, rot, patches)[3], M.patch_forward(p, h, st, patches)[3],
+                               rtol=1e-12)

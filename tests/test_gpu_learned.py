@@ -201,3 +201,93 @@ def test_learned_start_beats_random_start(sed):
     assert learned.eigenvalues[0] == pytest.approx(rand.eigenvalues[0], rel=1e-10)
     assert learned.residuals[0] <= 1e-8
     assert learned.iterations < rand.iterations, (learned.iterations, rand.iterations)
+
+
+# ------------------------------------------------------------ patch network
+def _patch_net(L, h, mask=0, seed=3):
+    from spined.learned import PatchMlp
+    return PatchMlp(lattices.square_patches(L), h, sign_mask=mask, seed=seed)
+
+
+def _patch_states(rng, L, N):
+    n = L * L
+    return rng.integers(0, 2 ** min(n, 63), size=N, dtype=np.uint64)
+
+
+@pytest.mark.parametrize("L,h,count", [(4, 64, 1000), (6, 128, 777), (6, 256, 4099), (4, 128, 5)])
+def test_patch_forward_matches_oracle(L, h, count):
+    """Patch network inference (the training step's forward GEMMs and the
+    per-sample sum over sites) against the oracle with BF16 h1, h2; and the
+    sum over sites makes it invariant under translations of the torus."""
+    rng = np.random.default_rng(L * 100 + h)
+    net = _patch_net(L, h, seed=count)
+    assert net.uses_tensor_cores
+    p = net.get_params()
+    P = 9
+    p[h * P:h * P + h] = rng.normal(scale=0.1, size=h)
+    net.set_params(p)
+    st = _patch_states(rng, L, count)
+    got = net.forward(st)
+    want = M.patch_forward(p, h, st, lattices.square_patches(L), act_bf16=True)[3]
+    scale = max(1.0, np.abs(want).max())
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-3 * scale)
+    # translate every state by one site along x (site (x, y) -> (x + 1, y))
+    perm = np.array([(y * L + (x + 1) % L) for y in range(L) for x in range(L)])
+    bits = (st[:, None] >> np.arange(L * L, dtype=np.uint64)[None, :]) & np.uint64(1)
+    moved = np.zeros_like(st)
+    for i in range(L * L):
+        moved |= bits[:, i] << np.uint64(perm[i])
+    np.testing.assert_allclose(net.forward(moved), got, rtol=0, atol=1e-4 * scale)
+
+
+@pytest.mark.parametrize("L,h,mask,N", [(4, 64, 0, 300), (6, 128, lattices.square_sublattice_mask(6), 77),
+                                        (6, 64, 0, 1024)])
+def test_patch_gradients_match_oracle(L, h, mask, N):
+    from spined.learned import Samples
+    rng = np.random.default_rng(L + h + N)
+    net = _patch_net(L, h, mask)
+    p = net.get_params()
+    P = 9
+    p[h * P:h * P + h] = rng.normal(scale=0.1, size=h)
+    net.set_params(p)
+    s = Samples(_patch_states(rng, L, N), rng.normal(size=N).astype(np.float32),
+                rng.integers(0, 2, size=N).astype(np.float32))
+    loss, g = net.loss_grad(s)
+    want_loss, want_g = M.patch_loss_grad(p, h, s.states, lattices.square_patches(L), s.t_abs.astype(np.float64),
+                                          s.t_sign, mask, act_bf16=True)
+    assert loss == pytest.approx(want_loss, rel=1e-5)
+    o = 0
+    for name, k in [("W1", h * P), ("b1", h), ("W2", h * h), ("b2", h), ("W3", 2 * h), ("b3", 2)]:
+        gg, ww = g[o:o + k], want_g[o:o + k]
+        np.testing.assert_allclose(gg, ww, rtol=0, atol=1e-3 * np.abs(ww).max() + 1e-9, err_msg=name)
+        o += k
+
+
+def test_patch_network_transfers_between_lattices():
+    """Trained on 4x4 states, the same parameters evaluate a 6x6 lattice
+    after rebind, matching the oracle there; a target that is a sum of local
+    terms is learned on one size and predicted on the other."""
+    from spined import _lib as L
+    from spined.learned import Samples
+    rng = np.random.default_rng(17)
+    net = _patch_net(4, 64, seed=2)
+    with pytest.raises(Exception):
+        net.set_path(L.SED_MLP_PATH_SIMT)  # patch networks run on the tensor cores only
+
+    def target(states, n):  # 0.1 x (number of up spins), an extensive local quantity
+        return np.array([0.1 * bin(int(v)).count("1") for v in states], dtype=np.float32)
+
+    st4 = _patch_states(rng, 4, 1 << 14)
+    s4 = Samples(st4, target(st4, 16), (st4 & np.uint64(1)).astype(np.float32))
+    l0, _ = net.loss_grad(s4)
+    net.train(s4, epochs=20, batch=1024, lr=3e-3, seed=1)
+    l1, _ = net.loss_grad(s4)
+    assert l1 < 0.05 * l0, (l0, l1)
+    net.rebind(lattices.square_patches(6))
+    st6 = _patch_states(rng, 6, 2000)
+    got = net.forward(st6)
+    want = M.patch_forward(net.get_params(), 64, st6, lattices.square_patches(6), act_bf16=True)[3]
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-3 * max(1.0, np.abs(want).max()))
+    # the extensive target transfers: 36 sites predicted from 16-site training
+    err = got[:, 0] - target(st6, 36)
+    assert np.sqrt(np.mean(err * err)) < 0.1, np.sqrt(np.mean(err * err))
