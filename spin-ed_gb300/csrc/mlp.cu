@@ -737,9 +737,14 @@ struct MlpTcArgs {
   float const* b2;
   __nv_bfloat16 const* W3;  // [2][hidden]
   float const* b3;
-  float* out;  // [n][2]
+  float* out;  // [n][2]; for a patch network [n / n_sites][2], zeroed before the launch
   int* error;
   uint64_t wait_ns;  // bound on every mbarrier wait
+  // patch network: n = samples x n_sites rows, row b n_sites + i is site i's
+  // patch of states[b] (patch[i * n_in + j] = the site of input j), and the
+  // rows' outputs add into out[b] (b3 once, with site 0)
+  uint16_t const* patch = nullptr;
+  int n_sites = 0;
 };
 
 // dynamic shared memory: the X tile, b1, b2, W3 (FP32), two buffers of
@@ -760,10 +765,20 @@ __device__ __forceinline__ void epi_sync() {  // the 512 epilogue threads only
   asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32) : "memory");
 }
 
-// State of row t % 128 of `tile` (0 past n), read by epilogue thread t.
+// Input word of row t % 128 of `tile` (0 past n), read by epilogue thread
+// t: the state itself, or for a patch network the row's patch gathered into
+// bits 0 .. n_in - 1.
 __device__ __forceinline__ uint64_t tc_state(MlpTcArgs const& p, int64_t tile, int t) {
   int64_t const xrow = tile * kTcRows + (t & 127);
-  return xrow < p.n ? p.states[xrow] : 0;
+  if (xrow >= p.n) return 0;
+  if (!p.n_sites) return p.states[xrow];
+  int64_t const b = xrow / p.n_sites;
+  int const site = (int)(xrow - b * p.n_sites);
+  uint64_t const s = p.states[b];
+  uint16_t const* const ps = p.patch + (int64_t)site * p.n_in;
+  uint64_t x = 0;
+  for (int j = 0; j < p.n_in; ++j) x |= ((s >> __ldg(ps + j)) & 1ull) << j;
+  return x;
 }
 
 // X tile row t % 128 from its state s: input j -> BF16 +1 / -1, zero for
@@ -998,13 +1013,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(MlpTcArgs p) {
     auto write_out = [&](int64_t tile, float const* sp) {
       if (t < kTcRows) {
         int64_t const row = tile * kTcRows + t;
-        float sa = b3a, ss = b3s;
+        int64_t const b = p.n_sites ? row / p.n_sites : row;
+        bool const first = !p.n_sites || row == b * p.n_sites;  // the row that carries b3
+        float sa = first ? b3a : 0.0f, ss = first ? b3s : 0.0f;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           sa += sp[(i * kTcRows + t) * 2];
           ss += sp[(i * kTcRows + t) * 2 + 1];
         }
-        if (ok && row < p.n) reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
+        if (ok && row < p.n) {
+          if (p.n_sites) {
+            atomicAdd(p.out + 2 * b, sa);
+            atomicAdd(p.out + 2 * b + 1, ss);
+          } else {
+            reinterpret_cast<float2*>(p.out)[row] = make_float2(sa, ss);
+          }
+        }
       }
     };
     // After a failed wait a warp skips the remaining work but still passes
@@ -1231,6 +1255,11 @@ int backward(MlpData& d, uint64_t const* states, uint64_t n, float const* t_abs,
   return LS_SUCCESS;
 }
 
+// The fused inference kernel's shapes.
+bool fused_shape(MlpData const& d) {
+  return d.n_in <= 64 && (d.hidden == 128 || d.hidden == 256 || d.hidden == 512);
+}
+
 bool tc_eligible(MlpData const& d) {
   if (d.n_sites) return true;  // patch networks run on the tensor cores only (checked at creation)
   return d.path != SED_MLP_PATH_SIMT && d.n_in <= 64 && (d.hidden == 128 || d.hidden == 256 || d.hidden == 512);
@@ -1255,9 +1284,13 @@ int forward_tc(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
   size_t const smem = tc_smem_bytes(H);
   SED_TRY_CUDA(cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SED_TRY_CUDA(cudaMemsetAsync(d.tc_error.ptr, 0, 4, s));
+  uint64_t const rows = d.n_sites ? n * d.n_sites : n;
+  if (d.n_sites) SED_TRY_CUDA(cudaMemsetAsync(out, 0, n * 8, s));  // the site rows add into it
   MlpTcArgs a;
   a.states = states;
-  a.n = (int64_t)n;
+  a.n = (int64_t)rows;
+  a.patch = d.n_sites ? d.patch_dev.as<uint16_t>() : nullptr;
+  a.n_sites = (int)d.n_sites;
   a.n_in = (int)d.n_in;
   a.hidden = H;
   a.stages = tc_stages(H);
@@ -1271,7 +1304,7 @@ int forward_tc(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
   a.error = d.tc_error.as<int>();
   a.wait_ns = device_wait_ns(kTcWaitNs);
   if (d.n_sm == 0) SED_TRY_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, d.device));
-  uint64_t const tiles = (n + kTcRows - 1) / kTcRows;
+  uint64_t const tiles = (rows + kTcRows - 1) / kTcRows;
   unsigned const grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)d.n_sm);  // persistent: one CTA per SM
   { k_mlp_forward_tc<<<grid, kTcThreads, smem, s>>>(a); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
@@ -1448,9 +1481,10 @@ int tc_check_error(MlpData& d) {
   return LS_SUCCESS;
 }
 
-// Patch network inference: (a, s) for states[0..n) (device) into out[2 n]
-// (device), in chunks of about 2^21 activation rows through the training
-// step's forward GEMMs and k_head_patch.
+// Patch network inference for hidden sizes the fused kernel does not take
+// (64): (a, s) for states[0..n) (device) into out[2 n] (device), in chunks
+// of about 2^21 activation rows through the training step's forward GEMMs
+// and k_head_patch. Larger networks run in k_mlp_forward_tc.
 int forward_patch(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
   if (n == 0) return LS_SUCCESS;
   cudaStream_t s = d.stream;
@@ -1649,7 +1683,7 @@ int sed_mlp_forward(sed_mlp* m, uint64_t const* states, uint64_t n, float* out) 
   for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
     uint64_t const nb = std::min(chunk, n - b0);
     SED_TRY_CUDA(cudaMemcpyAsync(sbuf.ptr, states + b0, nb * 8, cudaMemcpyDefault, d.stream));
-    if (d.n_sites) {
+    if (d.n_sites && !fused_shape(d)) {
       if (int st = ensure_batch(d, nb, false)) return st;
       if (int st = forward_patch(d, sbuf.as<uint64_t>(), nb, d.out.as<float>())) return st;
     } else if (tc_path) {
@@ -1869,7 +1903,7 @@ int sed_mlp_start_vector(sed_mlp* m, ls_spin_basis const* basis, double* out) {
   DeviceBuffer amp, part, vout;
   if (int st = amp.allocate(D * 8)) return st;  // (a, s) pairs
   if (int st = part.allocate(152 * 16 * 4)) return st;
-  if (d.n_sites) {
+  if (d.n_sites && !fused_shape(d)) {
     if (int st = forward_patch(d, b.reps.as<uint64_t>(), D, amp.as<float>())) return st;
   } else if (tc_eligible(d)) {
     if (int st = forward_tc(d, b.reps.as<uint64_t>(), D, amp.as<float>())) return st;

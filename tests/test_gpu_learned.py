@@ -216,9 +216,12 @@ def _patch_states(rng, L, N):
 
 @pytest.mark.parametrize("L,h,count", [(4, 64, 1000), (6, 128, 777), (6, 256, 4099), (4, 128, 5)])
 def test_patch_forward_matches_oracle(L, h, count):
-    """Patch network inference (the training step's forward GEMMs and the
-    per-sample sum over sites) against the oracle with BF16 h1, h2; and the
-    sum over sites makes it invariant under translations of the torus."""
+    """Patch network inference against the oracle with BF16 activations:
+    hidden 128 and 256 in the fused tensor-core kernel (site rows gathered
+    from the patch table, outputs added per sample; hardware tanh, h2 kept in
+    FP32: 4e-3 of the output scale), hidden 64 through the training step's
+    forward GEMMs (1e-3). The sum over sites makes it invariant under
+    translations of the torus."""
     rng = np.random.default_rng(L * 100 + h)
     net = _patch_net(L, h, seed=count)
     assert net.uses_tensor_cores
@@ -230,7 +233,7 @@ def test_patch_forward_matches_oracle(L, h, count):
     got = net.forward(st)
     want = M.patch_forward(p, h, st, lattices.square_patches(L), act_bf16=True)[3]
     scale = max(1.0, np.abs(want).max())
-    np.testing.assert_allclose(got, want, rtol=0, atol=1e-3 * scale)
+    np.testing.assert_allclose(got, want, rtol=0, atol=(4e-3 if h >= 128 else 1e-3) * scale)
     # translate every state by one site along x (site (x, y) -> (x + 1, y))
     perm = np.array([(y * L + (x + 1) % L) for y in range(L) for x in range(L)])
     bits = (st[:, None] >> np.arange(L * L, dtype=np.uint64)[None, :]) & np.uint64(1)
@@ -289,6 +292,8 @@ def test_patch_network_transfers_between_lattices():
     got = net.forward(st6)
     want = M.patch_forward(net.get_params(), 64, st6, lattices.square_patches(6), act_bf16=True)[3]
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-3 * max(1.0, np.abs(want).max()))
-    # the extensive target transfers: 36 sites predicted from 16-site training
+    # the extensive target transfers (36 sites predicted from 16-site training) up to a constant: the split of a
+    # constant between the per-site outputs and b3 is not fixed by one lattice size, and a constant shift of the
+    # log-amplitude does not change a normalised start vector
     err = got[:, 0] - target(st6, 36)
-    assert np.sqrt(np.mean(err * err)) < 0.1, np.sqrt(np.mean(err * err))
+    assert np.std(err) < 0.2 * np.std(target(st6, 36)), (np.std(err), np.mean(err))
