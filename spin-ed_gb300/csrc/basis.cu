@@ -306,6 +306,13 @@ int basis_build_index(BasisData& b, cudaStream_t stream) {
 
 namespace {
 
+int ensure_plan_checked(BasisData& b) {
+  if (b.plan_checked) return LS_SUCCESS;
+  if (int st = check_plan(b.plan)) return st;
+  b.plan_checked = true;
+  return LS_SUCCESS;
+}
+
 int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
   if (b.device < 0 || !b.plan_buf.ptr)
     if (int st = current_device(&b.device)) return st;
@@ -324,6 +331,7 @@ int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
   b.weights.reset();
   b.prefix.reset();
   if (given) {
+    if (int st = ensure_plan_checked(b)) return st;
     b.D = given_size;
     if (int st = b.reps.allocate(std::max<uint64_t>(1, given_size) * 8)) return st;
     if (int st = b.weights.allocate(std::max<uint64_t>(1, given_size) * 4)) return st;
@@ -417,6 +425,11 @@ int build_impl(BasisData& b, uint64_t const* given, uint64_t given_size) {
       { k_mark<uint32_t><<<grid, kThreads, 0, stream>>>(P, b.binom.as<uint64_t>(), b.n, b.hw, space,
                                                        n_words, bitmap.as<uint32_t>(), sbeg, spre, n_seg); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
+    // the plan's host self-check runs while the scan runs on the device
+    if (int st = ensure_plan_checked(b)) {
+      cudaStreamSynchronize(stream);
+      return st;
+    }
     if (n_tiles) {
       { k_tile_counts<<<(unsigned)n_tiles, kThreads, 0, stream>>>(bitmap.as<uint32_t>(), n_words,
                                                                 tiles.as<uint64_t>()); note_launches(1); }
@@ -490,7 +503,7 @@ int ls_create_spin_basis(ls_spin_basis** ptr, ls_group const* group, unsigned nu
     d->hw = hamming_weight;
     d->inv = spin_inversion;
     d->group = group->d;
-    if (int st = build_plan(d->group, number_spins, spin_inversion, d->plan)) return st;
+    if (int st = build_plan(d->group, number_spins, spin_inversion, d->plan, false)) return st;
     d->device = -1;  // bound to the current device by ls_build
     auto* b = new ls_spin_basis;
     b->d = std::move(d);
@@ -584,8 +597,12 @@ uint64_t const* sed_basis_device_states(ls_spin_basis const* basis) {
 int sed_basis_state_info(ls_spin_basis const* basis, uint64_t bits, uint64_t* representative,
                          unsigned* phase, unsigned* modulus) {
   if (!basis || !representative) return fail(LS_INVALID_ARGUMENT, "sed_basis_state_info: NULL argument");
-  BasisData const& b = *basis->d;
+  BasisData& b = *basis->d;
   if (b.n < 64 && (bits >> b.n)) return fail(LS_INVALID_STATE, "state has bits above number_spins");
+  {
+    std::lock_guard<std::mutex> lock(b.mu);
+    if (int st = ensure_plan_checked(b)) return st;
+  }
   PlanView const P = b.plan.view();
   uint64_t rep;
   uint32_t ph;

@@ -132,7 +132,11 @@ struct SymPlanHost {
   PlanView view() const;
 };
 
-int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymPlanHost& out);
+// self_check: also run check_plan (otherwise the caller runs it before the
+// plan's first use; ls_build overlaps it with the basis scan).
+int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymPlanHost& out,
+               bool self_check = true);
+int check_plan(SymPlanHost const& plan);
 
 // ---------------------------------------------------------------- basis ---
 struct BasisData {
@@ -142,6 +146,7 @@ struct BasisData {
   int inv = 0;
   GroupData group;
   SymPlanHost plan;
+  bool plan_checked = false;  // check_plan has passed (run by the first ls_build or host lookup)
   // device copy of the plan arrays (one allocation) and the view onto it
   DeviceBuffer plan_buf;
   PlanView plan_dev{};

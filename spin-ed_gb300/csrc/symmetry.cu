@@ -142,7 +142,60 @@ bool shift_terms(std::vector<uint8_t> const& p, unsigned width, unsigned max_ter
 
 }  // namespace
 
-int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymPlanHost& out) {
+// Self-check of the structured plan (cyclic-product walk, row and line
+// tables) against the plan's explicit element list on 256 random words and
+// their representatives (about 3 ms on the host).
+int check_plan(SymPlanHost const& out) {
+  unsigned const width = out.n_bits <= 32 ? 32u : 64u;
+  if (out.cyc) {
+    PlanView vx = out.view();
+    PlanView ve = vx;
+    ve.cyc = 0;
+    ve.rows = 0;
+    uint64_t rng = 0x9E3779B97F4A7C15ull;
+    for (int t = 0; t < 256; ++t) {  // 256 random words and their representatives (about 3 ms)
+      rng ^= rng << 13;
+      rng ^= rng >> 7;
+      rng ^= rng << 17;
+      uint64_t const x = rng & out.mask;
+      bool same;
+      if (width == 32) {
+        auto c1 = canonicalize<uint32_t>((uint32_t)x, vx), c2 = canonicalize<uint32_t>((uint32_t)x, ve);
+        uint32_t const w1 = representative_weight<uint32_t>((uint32_t)x, vx);
+        uint32_t const w2 = representative_weight<uint32_t>((uint32_t)x, ve);
+        same = c1.rep == c2.rep && w1 == w2 &&
+               (representative_weight<uint32_t>(c2.rep, ve) == 0 || c1.phase == c2.phase);
+        uint32_t const r = c2.rep;  // the representative itself: weights must agree too
+        same = same && representative_weight<uint32_t>(r, vx) == representative_weight<uint32_t>(r, ve);
+      } else {
+        auto c1 = canonicalize<uint64_t>(x, vx), c2 = canonicalize<uint64_t>(x, ve);
+        uint32_t const w1 = representative_weight<uint64_t>(x, vx);
+        uint32_t const w2 = representative_weight<uint64_t>(x, ve);
+        same = c1.rep == c2.rep && w1 == w2 &&
+               (representative_weight<uint64_t>(c2.rep, ve) == 0 || c1.phase == c2.phase);
+        uint64_t const r = c2.rep;
+        same = same && representative_weight<uint64_t>(r, vx) == representative_weight<uint64_t>(r, ve);
+      }
+      if (!same) return fail(LS_SYSTEM_ERROR, "structured subgroup walk disagrees with the explicit list");
+      if (out.line_fast) {  // the line-table test of the row path against the explicit list
+        RowTab const TL{out.row_min.data(), out.row_set.data(), out.line_row.data(),
+                        out.line_cols ? out.line_col.data() : nullptr};
+        uint64_t const r = canonicalize<uint64_t>(x, ve).rep;
+        bool const lines_same =
+            width == 32
+                ? representative_weight<uint32_t>((uint32_t)x, vx, TL) == representative_weight<uint32_t>((uint32_t)x, ve) &&
+                      representative_weight<uint32_t>((uint32_t)r, vx, TL) ==
+                          representative_weight<uint32_t>((uint32_t)r, ve)
+                : representative_weight<uint64_t>(x, vx, TL) == representative_weight<uint64_t>(x, ve) &&
+                      representative_weight<uint64_t>(r, vx, TL) == representative_weight<uint64_t>(r, ve);
+        if (!lines_same) return fail(LS_SYSTEM_ERROR, "line tables disagree with the explicit list");
+      }
+    }
+  }
+  return LS_SUCCESS;
+}
+
+int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymPlanHost& out, bool self_check) {
   unsigned const width = n_bits <= 32 ? 32u : 64u;
   out = SymPlanHost{};
   out.n_bits = n_bits;
@@ -590,51 +643,8 @@ int build_plan(GroupData const& group, unsigned n_bits, int spin_inversion, SymP
       if (!ok) out.rows = 0;
     }
   }
-  if (out.cyc) {
-    PlanView vx = out.view();
-    PlanView ve = vx;
-    ve.cyc = 0;
-    ve.rows = 0;
-    uint64_t rng = 0x9E3779B97F4A7C15ull;
-    for (int t = 0; t < 256; ++t) {  // 256 random words and their representatives (about 3 ms)
-      rng ^= rng << 13;
-      rng ^= rng >> 7;
-      rng ^= rng << 17;
-      uint64_t const x = rng & out.mask;
-      bool same;
-      if (width == 32) {
-        auto c1 = canonicalize<uint32_t>((uint32_t)x, vx), c2 = canonicalize<uint32_t>((uint32_t)x, ve);
-        uint32_t const w1 = representative_weight<uint32_t>((uint32_t)x, vx);
-        uint32_t const w2 = representative_weight<uint32_t>((uint32_t)x, ve);
-        same = c1.rep == c2.rep && w1 == w2 &&
-               (representative_weight<uint32_t>(c2.rep, ve) == 0 || c1.phase == c2.phase);
-        uint32_t const r = c2.rep;  // the representative itself: weights must agree too
-        same = same && representative_weight<uint32_t>(r, vx) == representative_weight<uint32_t>(r, ve);
-      } else {
-        auto c1 = canonicalize<uint64_t>(x, vx), c2 = canonicalize<uint64_t>(x, ve);
-        uint32_t const w1 = representative_weight<uint64_t>(x, vx);
-        uint32_t const w2 = representative_weight<uint64_t>(x, ve);
-        same = c1.rep == c2.rep && w1 == w2 &&
-               (representative_weight<uint64_t>(c2.rep, ve) == 0 || c1.phase == c2.phase);
-        uint64_t const r = c2.rep;
-        same = same && representative_weight<uint64_t>(r, vx) == representative_weight<uint64_t>(r, ve);
-      }
-      if (!same) return fail(LS_SYSTEM_ERROR, "structured subgroup walk disagrees with the explicit list");
-      if (out.line_fast) {  // the line-table test of the row path against the explicit list
-        RowTab const TL{out.row_min.data(), out.row_set.data(), out.line_row.data(),
-                        out.line_cols ? out.line_col.data() : nullptr};
-        uint64_t const r = canonicalize<uint64_t>(x, ve).rep;
-        bool const lines_same =
-            width == 32
-                ? representative_weight<uint32_t>((uint32_t)x, vx, TL) == representative_weight<uint32_t>((uint32_t)x, ve) &&
-                      representative_weight<uint32_t>((uint32_t)r, vx, TL) ==
-                          representative_weight<uint32_t>((uint32_t)r, ve)
-                : representative_weight<uint64_t>(x, vx, TL) == representative_weight<uint64_t>(x, ve) &&
-                      representative_weight<uint64_t>(r, vx, TL) == representative_weight<uint64_t>(r, ve);
-        if (!lines_same) return fail(LS_SYSTEM_ERROR, "line tables disagree with the explicit list");
-      }
-    }
-  }
+  if (self_check)
+    if (int st = check_plan(out)) return st;
   if (logging_enabled())
     log_line("symmetry plan: |G| = %u (x%u inversion), |H| = %u (cyclic product: %u, rows: %u of %u bits, "
              "mode %u), cosets = %u, stages = %u, terms = %u, line tables: %u (columns: %u)",
