@@ -388,7 +388,8 @@ SED_API int sed_mlp_set_params(sed_mlp* mlp, float const* in);
 SED_API int sed_mlp_forward(sed_mlp* mlp, uint64_t const* states, uint64_t n, float* out);
 /* Loss L = mean_i [(a_i - t_abs_i)^2 + BCE(s_i, y_i)], y_i = [t_sign_i (1 if
  * psi_i > 0, else 0) agrees with the prior], and dL/dparams (same layout as
- * the parameters; grads may be NULL). At most 2^20 samples. */
+ * the parameters; grads may be NULL). At most 2^20 samples (a patch network:
+ * at most 8 388 480 / n_sites). */
 SED_API int sed_mlp_loss_grad(sed_mlp* mlp, uint64_t const* states, float const* t_abs, float const* t_sign,
                               uint64_t n, double* loss, float* grads);
 /* Adam (0.9, 0.999, 1e-8) on mini-batches of `batch` samples, reshuffled

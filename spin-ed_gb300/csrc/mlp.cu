@@ -1329,6 +1329,10 @@ int stage(DeviceBuffer& buf, void const* src, size_t bytes, cudaStream_t s) {
   return LS_SUCCESS;
 }
 
+// Activation rows of one tensor-core pass at most (the GEMM grid's rows of
+// 128-row tiles).
+constexpr uint64_t kTcMaxRows = 65535ull * 128;
+
 // Activation rows of a batch: one per sample, or one per (sample, site) for
 // a patch network.
 uint64_t tc_rows(MlpData const& d, uint64_t samples) { return samples * (d.n_sites ? d.n_sites : 1u); }
@@ -1710,6 +1714,9 @@ int sed_mlp_loss_grad(sed_mlp* m, uint64_t const* states, float const* t_abs, fl
   if (int st = stage(ta, t_abs, n * 4, d.stream)) return st;
   if (int st = stage(ts, t_sign, n * 4, d.stream)) return st;
   if (tc_eligible(d)) {
+    if (tc_rows(d, n) > kTcMaxRows)
+      return fail(LS_INVALID_ARGUMENT, "sed_mlp_loss_grad: a patch network takes at most " +
+                                           std::to_string(kTcMaxRows / d.n_sites) + " samples per call");
     if (int st = tc_train_prepare(d, n)) return st;
     if (d.n_sites) {
       { k_batch_patch<<<blocks_for((int64_t)tc_rows(d, n) * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), nullptr, 0, (int64_t)n, (int)d.n_sites, (int)d.n_in, d.patch_dev.as<uint16_t>(), d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
@@ -1753,6 +1760,8 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
   };
   if (d.n_sites && n >= (1ull << 31))
     return fail(LS_INVALID_ARGUMENT, "sed_mlp_train: a patch network trains on at most 2^31 - 1 samples");
+  if (d.n_sites && tc_rows(d, std::min<uint64_t>(batch, n)) > kTcMaxRows)
+    return fail(LS_INVALID_ARGUMENT, "sed_mlp_train: batch x sites exceeds " + std::to_string(kTcMaxRows) + " rows");
   if (tc_eligible(d) && n < (1ull << 31)) {
     // tensor cores: the samples stay on the device; each epoch draws its
     // batches in the order of a keyed permutation (k_perm, keys from
