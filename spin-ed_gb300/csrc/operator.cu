@@ -1199,6 +1199,30 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
   DeviceBuffer elements;
   if (int st = sf.slice_ptr.allocate((n_slices + 1) * 8)) return st;
   if (int st = elements.allocate((n_slices + 1) * 8)) return st;
+  unsigned const grid = (unsigned)((n_slices * 32 + kBlock - 1) / kBlock);
+  if (n_slices) {
+    { k_count<<<grid, kBlock, 0, stream>>>(b.reps.as<uint64_t>(), D, op.terms_dev, n_slices,
+                                         sf.slice_ptr.as<uint64_t>(), elements.as<uint64_t>()); note_launches(1); }
+    SED_TRY_CUDA(cudaGetLastError());
+  }
+  { k_scan_u64<<<1, 1024, 0, stream>>>(sf.slice_ptr.as<uint64_t>(), n_slices); note_launches(1); }
+  { k_scan_u64<<<1, 1024, 0, stream>>>(elements.as<uint64_t>(), n_slices); note_launches(1); }
+  SED_TRY_CUDA(cudaGetLastError());
+  uint64_t n_entries = 0, n_elements = 0;
+  SED_TRY_CUDA(cudaMemcpyAsync(&n_entries, sf.slice_ptr.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
+  SED_TRY_CUDA(cudaMemcpyAsync(&n_elements, elements.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
+  SED_TRY_CUDA(cudaStreamSynchronize(stream));
+  size_t free_b = 0, total_b = 0;
+  SED_TRY_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  uint64_t const need = n_entries * (packed ? 4 : 6) + D * (op.is_real ? 9 : 17);
+  if (need > free_b)
+    return fail(LS_OUT_OF_MEMORY, "stream form needs " + std::to_string(need) + " bytes, " +
+                                      std::to_string(free_b) + " free");
+  if (int st = sf.entries.allocate(std::max<uint64_t>(1, n_entries) * 4)) return st;
+  if (!packed)
+    if (int st = sf.values.allocate(std::max<uint64_t>(1, n_entries) * 2)) return st;
+  if (int st = sf.diag.allocate(std::max<uint64_t>(1, D) * (op.is_real ? 8 : 16))) return st;
+  if (int st = sf.row_class.allocate(std::max<uint64_t>(1, D))) return st;
   // orbit-table path: real characters, a weight class small enough to tabulate
   uint64_t space = 0;
   bool use_table = false;
@@ -1228,37 +1252,19 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     }
     size_t fr = 0, tt = 0;
     SED_TRY_CUDA(cudaMemGetInfo(&fr, &tt));
-    use_table = space > 0 && space * 4 <= fr / 5 * 2;  // decided before the stream form's allocation
+    use_table = space > 0 && space * 4 <= fr / 5 * 2;
   }
-  // The orbit table depends only on the basis: it is built on a side stream
-  // while the main stream counts the rows and the stream form is allocated.
-  DeviceBuffer table;
-  struct TableGuard {
-    DeviceBuffer& b;
-    ~TableGuard() { krylov_give(b); }
-  } table_guard{table};
-  DeviceBuffer err, seg_buf, rank_buf;
-  std::vector<uint64_t> R;  // the rank table's host copy, alive while its upload may be in flight
-  RowIndex RI{nullptr, 0, 0};
-  uint32_t n_chunks = 0, wp1 = 0, rank_words = 0;
-  size_t dsmem = (size_t)64 * 33 * 8;
-  struct SideGuard {  // declared last, destroyed first: the side stream is idle before its buffers go
-    cudaStream_t s = nullptr;
-    cudaEvent_t e = nullptr;
-    ~SideGuard() {
-      if (s) {
-        cudaStreamSynchronize(s);
-        cudaStreamDestroy(s);
-      }
-      if (e) cudaEventDestroy(e);
-    }
-  } side;
   if (use_table) {
+    DeviceBuffer table;
+    struct TableGuard {
+      DeviceBuffer& b;
+      ~TableGuard() { krylov_give(b); }
+    } table_guard{table};
+    DeviceBuffer err;
     if (int st = err.allocate(16)) return st;
     if (int st = krylov_take(space * 4, table)) return st;
-    SED_TRY_CUDA(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
-    SED_TRY_CUDA(cudaEventCreateWithFlags(&side.e, cudaEventDisableTiming));
-    cudaStream_t const stream = side.s;  // the table's work below runs on the side stream
+    DeviceBuffer seg_buf;
+    RowIndex RI{nullptr, 0, 0};
     if (!seg_off.empty()) {
       if (int st = seg_buf.allocate(seg_off.size() * 8)) return st;
       SED_TRY_CUDA(cudaMemcpyAsync(seg_buf.ptr, seg_off.data(), seg_off.size() * 8, cudaMemcpyHostToDevice, stream));
@@ -1268,12 +1274,14 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
     SED_TRY_CUDA(cudaMemsetAsync(table.ptr, 0xFF, space * 4, stream));
     SED_TRY_CUDA(cudaMemsetAsync(err.ptr, 0, 16, stream));
     // chunked rank table (6-bit chunks) when it fits in 96 KB of shared memory
+    uint32_t n_chunks = 0, wp1 = 0, rank_words = 0;
+    DeviceBuffer rank_buf;
     if (b.hw >= 0) {
       n_chunks = (b.n + 5) / 6;
       wp1 = (uint32_t)b.hw + 1;
       uint64_t const words = (uint64_t)n_chunks * wp1 * 64;
       if (words * 8 <= 96 * 1024) {
-        R.assign(words, 0);
+        std::vector<uint64_t> R(words, 0);
         for (uint32_t c = 0; c < n_chunks; ++c)
           for (uint32_t m = 0; m < wp1; ++m)
             for (uint32_t v = 0; v < 64; ++v) {
@@ -1289,10 +1297,11 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
             }
         if (int st = rank_buf.allocate(words * 8)) return st;
         SED_TRY_CUDA(cudaMemcpyAsync(rank_buf.ptr, R.data(), words * 8, cudaMemcpyHostToDevice, stream));
+        SED_TRY_CUDA(cudaStreamSynchronize(stream));
         rank_words = (uint32_t)words;
       }
     }
-    dsmem = rank_words ? (size_t)rank_words * 8 : (size_t)64 * 33 * 8;
+    size_t const dsmem = rank_words ? (size_t)rank_words * 8 : (size_t)64 * 33 * 8;
     bool const wide = b.plan.n_bits > 32;
     uint64_t const threads = D * b.plan.n_cosets;
     unsigned const sgrid = (unsigned)((threads + 255) / 256);
@@ -1305,43 +1314,6 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
       { k_orbit_scatter<uint32_t><<<sgrid, 256, dsmem, stream>>>(b.plan_dev, b.reps.as<uint64_t>(), D, b.hw, b.binom.as<uint64_t>(), table.as<uint32_t>(), space, err.as<int>(), rtab, rank_words, n_chunks, wp1, RI); note_launches(1); }
     }
     SED_TRY_CUDA(cudaGetLastError());
-    SED_TRY_CUDA(cudaEventRecord(side.e, side.s));
-  }
-  unsigned const grid = (unsigned)((n_slices * 32 + kBlock - 1) / kBlock);
-  if (n_slices) {
-    { k_count<<<grid, kBlock, 0, stream>>>(b.reps.as<uint64_t>(), D, op.terms_dev, n_slices,
-                                         sf.slice_ptr.as<uint64_t>(), elements.as<uint64_t>()); note_launches(1); }
-    SED_TRY_CUDA(cudaGetLastError());
-  }
-  { k_scan_u64<<<1, 1024, 0, stream>>>(sf.slice_ptr.as<uint64_t>(), n_slices); note_launches(1); }
-  { k_scan_u64<<<1, 1024, 0, stream>>>(elements.as<uint64_t>(), n_slices); note_launches(1); }
-  SED_TRY_CUDA(cudaGetLastError());
-  uint64_t n_entries = 0, n_elements = 0;
-  SED_TRY_CUDA(cudaMemcpyAsync(&n_entries, sf.slice_ptr.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
-  SED_TRY_CUDA(cudaMemcpyAsync(&n_elements, elements.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
-  SED_TRY_CUDA(cudaStreamSynchronize(stream));
-  size_t free_b = 0, total_b = 0;
-  SED_TRY_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  uint64_t const need = n_entries * (packed ? 4 : 6) + D * (op.is_real ? 9 : 17);
-  if (need > free_b && use_table) {
-    // the table was taken first: free it and record by canonicalisation
-    SED_TRY_CUDA(cudaStreamSynchronize(side.s));
-    table.reset();
-    use_table = false;
-    SED_TRY_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  }
-  if (need > free_b)
-    return fail(LS_OUT_OF_MEMORY, "stream form needs " + std::to_string(need) + " bytes, " +
-                                      std::to_string(free_b) + " free");
-  if (int st = sf.entries.allocate(std::max<uint64_t>(1, n_entries) * 4)) return st;
-  if (!packed)
-    if (int st = sf.values.allocate(std::max<uint64_t>(1, n_entries) * 2)) return st;
-  if (int st = sf.diag.allocate(std::max<uint64_t>(1, D) * (op.is_real ? 8 : 16))) return st;
-  if (int st = sf.row_class.allocate(std::max<uint64_t>(1, D))) return st;
-  if (use_table) {
-    SED_TRY_CUDA(cudaStreamWaitEvent(stream, side.e, 0));
-    bool const wide = b.plan.n_bits > 32;
-    uint64_t const* rtab = rank_words ? rank_buf.as<uint64_t>() : nullptr;
     IndexView const I = b.index_view();
     unsigned const rgrid = (unsigned)((n_slices * 32 + 255) / 256);
     auto rec = [&](auto w_tag, auto real_tag) {
