@@ -215,8 +215,11 @@ __device__ bool chol4(double const* G, double* R) {
 }
 
 // In place X <- X R^{-1} on own rows (X = [D][4]); y R = x by forward
-// substitution.
+// substitution, dividing by the diagonal through its reciprocals (four FP64
+// divisions per CTA instead of four per row: a division is a long sequence
+// on GB300's narrow FP64 pipe).
 __device__ void apply_rinv(Ctx& x, double* X, double const* R) {
+  double const inv[4] = {1.0 / R[0], 1.0 / R[5], 1.0 / R[10], 1.0 / R[15]};
   for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
     Row4 const v = *reinterpret_cast<Row4 const*>(X + r * 4);
     double const a[4] = {v.x, v.y, v.z, v.w};
@@ -226,7 +229,7 @@ __device__ void apply_rinv(Ctx& x, double* X, double const* R) {
       double s = a[j];
 #pragma unroll
       for (int k = 0; k < j; ++k) s -= y[k] * R[k * 4 + j];
-      y[j] = s / R[j * 4 + j];
+      y[j] = s * inv[j];
     }
     *reinterpret_cast<Row4*>(X + r * 4) = mk4(y[0], y[1], y[2], y[3]);
   }
@@ -322,53 +325,6 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
   }
 }
 
-// ----------------------------------------------------- fixed-point CGS ---
-// GB300's FP64 pipe (1.75 FMA per clock per SM) bounds the Gram-Schmidt
-// loops, while its integer pipe is tens of times wider. The projections
-// therefore run in exact fixed point on the integer pipe: every entry of a
-// stored block V (orthonormal, |v| <= 1) becomes round(v 2^kFixV), every entry
-// of column t of X round(x 2^(kFixV - E_t)) with |x| < 2^E_t on this CTA's
-// rows, and the products (< 2^100) are summed exactly in 128-bit integers
-// (up to 2^24 rows per CTA); each sum is rounded to FP64 once. The update
-// X -= V C converts C the same way per column and subtracts the exactly
-// summed correction, rounded once, from each entry. The results match the
-// FP64 loops to a few units in the last place of the largest term, and do
-// not depend on the order of the sums.
-constexpr int kFixV = 50;
-constexpr uint64_t kFixMaxRows = 1ull << 24;
-
-// round(d 2^k) (|d| 2^k < 2^62, d finite) with integer operations only.
-__device__ __forceinline__ long long fx_scale(double d, int k) {
-  unsigned long long const b = (unsigned long long)__double_as_longlong(d);
-  int const e = (int)((b >> 52) & 0x7FF);
-  unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  if (e) m |= 1ull << 52;
-  int const sh = (e ? e : 1) - 1075 + k;
-  long long r;
-  if (sh >= 0)
-    r = (long long)(m << sh);
-  else if (sh > -64)
-    r = (long long)((m + (1ull << (-sh - 1))) >> (-sh));
-  else
-    r = 0;
-  return (b >> 63) ? -r : r;
-}
-
-// a 2^-k in FP64 for a 128-bit integer a (two roundings: the high and low
-// halves are exact in FP64 only up to 53 bits each, so the result is within
-// an ulp or two of a 2^-k).
-__device__ __forceinline__ double fx_to_double(__int128 a, int k) {
-  long long const hi = (long long)(a >> 64);
-  unsigned long long const lo = (unsigned long long)a;
-  double const v = fma((double)hi, 0x1p64, (double)lo);
-  return ldexp(v, -k);
-}
-
-// Biased exponent field of |d| (0x7FF: NaN or infinity).
-__device__ __forceinline__ uint32_t fx_expo(double d) {
-  return (uint32_t)(((unsigned long long)__double_as_longlong(d) >> 52) & 0x7FF);
-}
-
 // X -= sum_{i<nb} V_i C_i (two passes of classical Gram-Schmidt). C (shared,
 // nb * 16, row-major a*4+c per block, may be null) receives the summed
 // coefficients; norms2 (shared, may be null) the squared column norms of X
@@ -382,66 +338,19 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
   if (C)
     for (int k = threadIdx.x; k < K; k += blockDim.x) C[k] = 0.0;
   __syncthreads();
-  __shared__ int ex_s[4];
-  __shared__ long long cfix[16 * (kMaxBlocks + 1)];
-  __shared__ int cexp[4];
   for (int pass = 0; pass < 2; ++pass) {
     uint32_t const i0 = pass == 0 ? first : 0u;
-    // exponent bound of each column of X on this CTA's rows (0x7FF: not
-    // finite, then the FP64 loops run)
-    if (threadIdx.x < 4) ex_s[threadIdx.x] = 0;
-    __syncthreads();
-    {
-      uint32_t em[4] = {0, 0, 0, 0};
-      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-        Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
-        em[0] = max(em[0], fx_expo(w.x));
-        em[1] = max(em[1], fx_expo(w.y));
-        em[2] = max(em[2], fx_expo(w.z));
-        em[3] = max(em[3], fx_expo(w.w));
-      }
-#pragma unroll
-      for (int t = 0; t < 4; ++t) atomicMax(&ex_s[t], (int)em[t]);
-    }
-    __syncthreads();
-    bool const fixp = (x.r1 - x.r0) <= kFixMaxRows && ex_s[0] < 0x7FF && ex_s[1] < 0x7FF && ex_s[2] < 0x7FF &&
-                      ex_s[3] < 0x7FF;
-    int kx[4];  // x scale: |x| < 2^(e - 1022), so x 2^(kFixV - e + 1022) < 2^kFixV
-#pragma unroll
-    for (int t = 0; t < 4; ++t) kx[t] = kFixV - (max(ex_s[t], 1) - 1022);
     for (uint32_t i = i0; i < nb; ++i) {
       double p[16] = {};
       double const* Vi = V + (uint64_t)i * D * 4;
-      if (fixp) {
-        __int128 q[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) q[k] = 0;
-        for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-          Row4 const a = *reinterpret_cast<Row4 const*>(Vi + r * 4);
-          Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
-          long long const av[4] = {fx_scale(a.x, kFixV), fx_scale(a.y, kFixV), fx_scale(a.z, kFixV),
-                                   fx_scale(a.w, kFixV)};
-          long long const wv[4] = {fx_scale(w.x, kx[0]), fx_scale(w.y, kx[1]), fx_scale(w.z, kx[2]),
-                                   fx_scale(w.w, kx[3])};
-#pragma unroll
-          for (int s = 0; s < 4; ++s)
-#pragma unroll
-            for (int t = 0; t < 4; ++t) q[s * 4 + t] += (__int128)av[s] * wv[t];
-        }
+      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+        Row4 const a = *reinterpret_cast<Row4 const*>(Vi + r * 4);
+        Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
+        double const av[4] = {a.x, a.y, a.z, a.w}, wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
         for (int s = 0; s < 4; ++s)
 #pragma unroll
-          for (int t = 0; t < 4; ++t) p[s * 4 + t] = fx_to_double(q[s * 4 + t], kFixV + kx[t]);
-      } else {
-        for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-          Row4 const a = *reinterpret_cast<Row4 const*>(Vi + r * 4);
-          Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
-          double const av[4] = {a.x, a.y, a.z, a.w}, wv[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-          for (int s = 0; s < 4; ++s)
-#pragma unroll
-            for (int t = 0; t < 4; ++t) p[s * 4 + t] = fma(av[s], wv[t], p[s * 4 + t]);
-        }
+          for (int t = 0; t < 4; ++t) p[s * 4 + t] = fma(av[s], wv[t], p[s * 4 + t]);
       }
       cta_sum<16>(p, x.red, x.tmp + 16 * i);
     }
@@ -465,55 +374,17 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
       for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) C[k] += tot[k];
     if (Kp > K && threadIdx.x < 4) norms2[threadIdx.x] = tot[K + threadIdx.x];
     // X -= sum_i V_i tot_i
-    bool fixu = fixp;
-    if (fixu) {  // C per column: |c| < 2^(e - 1022) over this pass's blocks
-      if (threadIdx.x < 4) {
-        uint32_t em = 0;
-        for (int k = 16 * (int)i0 + (int)threadIdx.x; k < K; k += 4) em = max(em, fx_expo(tot[k]));
-        cexp[threadIdx.x] = (int)em;
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      Row4 w = *reinterpret_cast<Row4 const*>(X + r * 4);
+      for (uint32_t i = i0; i < nb; ++i) {
+        Row4 const a = *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4);
+        double const* c = tot + 16 * i;
+        w.x -= a.x * c[0] + a.y * c[4] + a.z * c[8] + a.w * c[12];
+        w.y -= a.x * c[1] + a.y * c[5] + a.z * c[9] + a.w * c[13];
+        w.z -= a.x * c[2] + a.y * c[6] + a.z * c[10] + a.w * c[14];
+        w.w -= a.x * c[3] + a.y * c[7] + a.z * c[11] + a.w * c[15];
       }
-      __syncthreads();
-      fixu = cexp[0] < 0x7FF && cexp[1] < 0x7FF && cexp[2] < 0x7FF && cexp[3] < 0x7FF;
-      for (int k = 16 * (int)i0 + (int)threadIdx.x; k < K; k += blockDim.x)
-        cfix[k] = fixu ? fx_scale(tot[k], kFixV - (max(cexp[k & 3], 1) - 1022)) : 0;
-      __syncthreads();
-    }
-    if (fixu) {
-      int kc[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) kc[t] = kFixV + kFixV - (max(cexp[t], 1) - 1022);
-      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-        __int128 acc[4] = {0, 0, 0, 0};
-        for (uint32_t i = i0; i < nb; ++i) {
-          Row4 const a = *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4);
-          long long const av[4] = {fx_scale(a.x, kFixV), fx_scale(a.y, kFixV), fx_scale(a.z, kFixV),
-                                   fx_scale(a.w, kFixV)};
-          long long const* c = cfix + 16 * i;
-#pragma unroll
-          for (int s = 0; s < 4; ++s)
-#pragma unroll
-            for (int t = 0; t < 4; ++t) acc[t] += (__int128)av[s] * c[s * 4 + t];
-        }
-        Row4 w = *reinterpret_cast<Row4 const*>(X + r * 4);
-        w.x -= fx_to_double(acc[0], kc[0]);
-        w.y -= fx_to_double(acc[1], kc[1]);
-        w.z -= fx_to_double(acc[2], kc[2]);
-        w.w -= fx_to_double(acc[3], kc[3]);
-        *reinterpret_cast<Row4*>(X + r * 4) = w;
-      }
-    } else {
-      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-        Row4 w = *reinterpret_cast<Row4 const*>(X + r * 4);
-        for (uint32_t i = i0; i < nb; ++i) {
-          Row4 const a = *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4);
-          double const* c = tot + 16 * i;
-          w.x -= a.x * c[0] + a.y * c[4] + a.z * c[8] + a.w * c[12];
-          w.y -= a.x * c[1] + a.y * c[5] + a.z * c[9] + a.w * c[13];
-          w.z -= a.x * c[2] + a.y * c[6] + a.z * c[10] + a.w * c[14];
-          w.w -= a.x * c[3] + a.y * c[7] + a.z * c[11] + a.w * c[15];
-        }
-        *reinterpret_cast<Row4*>(X + r * 4) = w;
-      }
+      *reinterpret_cast<Row4*>(X + r * 4) = w;
     }
     __syncthreads();
   }
