@@ -261,7 +261,9 @@ def forms_arm(stream):
     learned start (MLP 36-256-256-2 trained on the tensor cores for 96
     epochs, falling learning rate, on 2^20 configurations sampled from the
     J2 = 0.05 ground state; its training is reported apart, its tensor-core
-    inference is inside the timed solve)."""
+    inference is inside the timed solve); and the size-independent patch
+    network trained on the 4x4 lattice's ground states only, bound to the
+    6x6 lattice (FP64 solve from its start vector)."""
     import torch
     from spined import internal as I, lattices, _lib as L
     from spined.learned import Mlp, Samples, sample
@@ -329,8 +331,35 @@ def forms_arm(stream):
     out["training"] = {"sample_s": t_s, "train_s": t_tr, "samples": len(data), "epochs": LEARNED_EPOCHS,
                        "hidden": LEARNED_HIDDEN, "schedule": "lr 3e-3, then 1e-3 from epoch/2, 2e-4 from 3 epoch/4",
                        "final_loss": loss, "tensor_cores": net.uses_tensor_cores}
+    # size-independent patch network trained on the 4x4 lattice only, bound to the 6x6 one
+    from spined.learned import PatchMlp
+    b4 = build_model(lattices.heisenberg_square(4))
+    D4 = I.get_number_states(b4.basis)
+    v4 = torch.empty(D4, dtype=torch.float64, device="cuda")
+    parts = []
+    for k, j2 in enumerate((0.0, 0.05)):
+        mm = lattices.heisenberg_square(4, j2=j2)
+        op4 = I.mk_operator(b4.basis, [I.mk_interaction(mat, st) for mat, st in mm.terms])
+        I.eigh(op4, tol=1e-10, out=v4, seed=1234)
+        parts.append(sample(b4.basis, v4, 1 << 19, seed=10 + k, sign_mask=lattices.square_sublattice_mask(4)))
+        del op4
+    data4 = Samples.concat(parts)
+    pnet = PatchMlp(lattices.square_patches(4), 128, sign_mask=lattices.square_sublattice_mask(4), seed=5)
+    t_tr4, loss4 = timed(lambda: pnet.train_decayed(data4, epochs=32, batch=4096, lr=3e-3, seed=3))
+    pnet.rebind(lattices.square_patches(6), mask)
+
+    def run_patch():
+        pnet.start_vector(b.basis, out=start)
+        return I.eigh(op0, tol=1e-8, out=v, start=start)
+    timed(run_patch)  # first use: tensor maps, images
+    t, r = timed(run_patch)
+    t_inf, _ = timed(lambda: pnet.start_vector(b.basis, out=start))
+    rec("learned_patch_4x4_fp64", t, r, {
+        "inference_s": t_inf, "overlap": abs(torch.dot(start / torch.linalg.norm(start), psi0).item()),
+        "training": {"lattice": "4x4 (D=%d), J2 = 0 and 0.05 ground states" % D4, "samples": len(data4),
+                     "epochs": 32, "hidden": 128, "patch": "3x3", "train_s": t_tr4, "final_loss": loss4}})
     base = out["plain_fp64"]["seconds"]
-    for k in ("mixed_random", "warm_fp64", "warm_mixed", "learned_fp64", "learned_mixed"):
+    for k in ("mixed_random", "warm_fp64", "warm_mixed", "learned_fp64", "learned_mixed", "learned_patch_4x4_fp64"):
         out[k]["vs_plain_fp64"] = out[k]["seconds"] / base
         out[k]["eigenvalue_rel_err"] = abs(out[k]["E0"] - e_ref) / abs(e_ref)
     return out
