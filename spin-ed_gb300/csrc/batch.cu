@@ -289,6 +289,8 @@ __device__ bool block_qr(Ctx& x, double* X, double* Rtot, bool& ok) {
   return true;
 }
 
+constexpr int kBlockSpmvU = 4;  // slots whose gathers a lane issues together
+
 // W = H X on own rows (X, W: [D][4]); gathers of X go through L2.
 __device__ void block_spmv(Ctx& x, double const* X, double* W) {
   StreamView const& S = x.c.S;
@@ -301,17 +303,35 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
     uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     uint32_t const* ent = S.entries + base + lane;
-    for (uint32_t e = 0; e < width; ++e) {
-      uint32_t const v = __ldcs(ent + (uint64_t)e * 32);
-      if (v != kNull) {
-        uint32_t const col = v & col_mask;
-        uint32_t const code = packed ? (v >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)e * 32);
-        double const t = __ldg(table + code);
-        Row4 const xv = ldcg4(X + (uint64_t)col * 4);
-        a0 = fma(t, xv.x, a0);
-        a1 = fma(t, xv.y, a1);
-        a2 = fma(t, xv.z, a2);
-        a3 = fma(t, xv.w, a3);
+    // kBlockSpmvU slots per step: their entry loads, then their gathers, then
+    // the FMAs in slot order (the same order as one slot at a time), so
+    // several gathers are in flight per lane
+    for (uint32_t e0 = 0; e0 < width; e0 += kBlockSpmvU) {
+      uint32_t v[kBlockSpmvU];
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u) v[u] = e0 + u < width ? __ldcs(ent + (uint64_t)(e0 + u) * 32) : kNull;
+      double t[kBlockSpmvU];
+      Row4 xv[kBlockSpmvU];
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u) {
+        if (v[u] != kNull) {
+          uint32_t const col = v[u] & col_mask;
+          uint32_t const code =
+              packed ? (v[u] >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)(e0 + u) * 32);
+          t[u] = __ldg(table + code);
+          xv[u] = ldcg4(X + (uint64_t)col * 4);
+        } else {
+          t[u] = 0.0;
+          xv[u] = mk4(0.0, 0.0, 0.0, 0.0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u) {
+        if (v[u] == kNull) continue;
+        a0 = fma(t[u], xv[u].x, a0);
+        a1 = fma(t[u], xv[u].y, a1);
+        a2 = fma(t[u], xv[u].z, a2);
+        a3 = fma(t[u], xv[u].w, a3);
       }
     }
     uint64_t const i = s * 32 + lane;
