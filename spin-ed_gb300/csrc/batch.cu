@@ -363,26 +363,7 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
     for (uint32_t i = i0; i < nb; ++i) {
       double p[16] = {};
       double const* Vi = V + (uint64_t)i * D * 4;
-      // two of the thread's rows per step (loads of both first), products in
-      // row order as one row at a time
-      uint64_t r = x.r0 + threadIdx.x;
-      for (; r + blockDim.x < x.r1; r += 2 * (uint64_t)blockDim.x) {
-        Row4 const a0 = *reinterpret_cast<Row4 const*>(Vi + r * 4);
-        Row4 const w0 = *reinterpret_cast<Row4 const*>(X + r * 4);
-        Row4 const a1 = *reinterpret_cast<Row4 const*>(Vi + (r + blockDim.x) * 4);
-        Row4 const w1 = *reinterpret_cast<Row4 const*>(X + (r + blockDim.x) * 4);
-        double const av0[4] = {a0.x, a0.y, a0.z, a0.w}, wv0[4] = {w0.x, w0.y, w0.z, w0.w};
-        double const av1[4] = {a1.x, a1.y, a1.z, a1.w}, wv1[4] = {w1.x, w1.y, w1.z, w1.w};
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-#pragma unroll
-          for (int t = 0; t < 4; ++t) p[s * 4 + t] = fma(av0[s], wv0[t], p[s * 4 + t]);
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-#pragma unroll
-          for (int t = 0; t < 4; ++t) p[s * 4 + t] = fma(av1[s], wv1[t], p[s * 4 + t]);
-      }
-      for (; r < x.r1; r += blockDim.x) {
+      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
         Row4 const a = *reinterpret_cast<Row4 const*>(Vi + r * 4);
         Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
         double const av[4] = {a.x, a.y, a.z, a.w}, wv[4] = {w.x, w.y, w.z, w.w};
@@ -412,23 +393,17 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
     if (C)
       for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) C[k] += tot[k];
     if (Kp > K && threadIdx.x < 4) norms2[threadIdx.x] = tot[K + threadIdx.x];
-    // X -= sum_i V_i tot_i (two blocks' rows loaded per step, applied in block order)
-    auto sub = [&](Row4& w, Row4 const& a, double const* c) {
-      w.x -= a.x * c[0] + a.y * c[4] + a.z * c[8] + a.w * c[12];
-      w.y -= a.x * c[1] + a.y * c[5] + a.z * c[9] + a.w * c[13];
-      w.z -= a.x * c[2] + a.y * c[6] + a.z * c[10] + a.w * c[14];
-      w.w -= a.x * c[3] + a.y * c[7] + a.z * c[11] + a.w * c[15];
-    };
+    // X -= sum_i V_i tot_i
     for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
       Row4 w = *reinterpret_cast<Row4 const*>(X + r * 4);
-      uint32_t i = i0;
-      for (; i + 1 < nb; i += 2) {
+      for (uint32_t i = i0; i < nb; ++i) {
         Row4 const a = *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4);
-        Row4 const b = *reinterpret_cast<Row4 const*>(V + (uint64_t)(i + 1) * D * 4 + r * 4);
-        sub(w, a, tot + 16 * i);
-        sub(w, b, tot + 16 * (i + 1));
+        double const* c = tot + 16 * i;
+        w.x -= a.x * c[0] + a.y * c[4] + a.z * c[8] + a.w * c[12];
+        w.y -= a.x * c[1] + a.y * c[5] + a.z * c[9] + a.w * c[13];
+        w.z -= a.x * c[2] + a.y * c[6] + a.z * c[10] + a.w * c[14];
+        w.w -= a.x * c[3] + a.y * c[7] + a.z * c[11] + a.w * c[15];
       }
-      if (i < nb) sub(w, *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4), tot + 16 * i);
       *reinterpret_cast<Row4*>(X + r * 4) = w;
     }
     __syncthreads();
