@@ -266,6 +266,91 @@ __global__ void k_batch(uint64_t const* __restrict__ states, float const* __rest
 constexpr int kHeadChunks = 2;  // 8-column chunks per lane: hidden <= 512
 constexpr int kHeadRows = 4;    // rows whose loads a warp issues together
 
+// This block's sums of (db2, dW3 row 0, dW3 row 1, db3) into
+// part[blockIdx.x][3H + 2]: each warp puts its lanes' columns (and lane 0's
+// db3 terms) in shared memory, then the warps' values are added in warp
+// order, so the result does not depend on timing (no atomics).
+__device__ __forceinline__ void head_block_partial(float const (&ab)[kHeadChunks][8], float const (&a0)[kHeadChunks][8],
+                                                   float const (&a1)[kHeadChunks][8], float sd0, float sd1, int H,
+                                                   float* smem, float* __restrict__ part) {
+  int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, chunks = H / 8, W = 3 * H + 2;
+  int const nw = blockDim.x >> 5;
+  float* const mine = smem + warp * W;
+#pragma unroll
+  for (int q = 0; q < kHeadChunks; ++q) {
+    int const ch = lane + 32 * q;
+    if (ch >= chunks) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      mine[8 * ch + j] = ab[q][j];
+      mine[H + 8 * ch + j] = a0[q][j];
+      mine[2 * H + 8 * ch + j] = a1[q][j];
+    }
+  }
+  if (lane == 0) {
+    mine[3 * H] = sd0;
+    mine[3 * H + 1] = sd1;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < W; c += blockDim.x) {
+    float t = 0.0f;
+    for (int w = 0; w < nw; ++w) t += smem[w * W + c];
+    part[(int64_t)blockIdx.x * W + c] = t;
+  }
+}
+
+// The step's gradient from its partial sums, each added in a fixed order:
+// W1 and W2 from the K-split slabs of their GEMMs (s1, s2 slabs), b2, W3 and
+// b3 from the output-layer blocks' rows (nhb rows of 3H + 2); b1 is left to
+// k_grad_b1.
+__global__ void k_grad_rest(float* __restrict__ g, int n_in, int H, float const* __restrict__ w1part, int s1,
+                            float const* __restrict__ w2part, int s2, float const* __restrict__ hpart, int nhb) {
+  tc::grid_dependency_wait();
+  tc::launch_dependents();
+  int64_t const nW1 = (int64_t)H * n_in, ob1 = nW1, oW2 = ob1 + H, ob2 = oW2 + (int64_t)H * H, oW3 = ob2 + H,
+                ob3 = oW3 + 2 * H, n = ob3 + 2;
+  int const W = 3 * H + 2;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    if (q >= ob1 && q < oW2) continue;  // b1: k_grad_b1
+    float t = 0.0f;
+    if (q < nW1) {
+      for (int z = 0; z < s1; ++z) t += w1part[(int64_t)z * nW1 + q];
+    } else if (q < ob2) {
+      int64_t const e = q - oW2;
+      for (int z = 0; z < s2; ++z) t += w2part[(int64_t)z * H * H + e];
+    } else {
+      int const c = q < oW3 ? (int)(q - ob2) : q < ob3 ? H + (int)(q - oW3) : 3 * H + (int)(q - ob3);
+      for (int b = 0; b < nhb; ++b) t += hpart[(int64_t)b * W + c];
+    }
+    g[q] = t;
+  }
+}
+
+// b1[i] = the sum over the np partial column sums part[p][i] of the g1 GEMM's
+// epilogue; one block per column, strided partial sums added in a fixed
+// tree order.
+__global__ void __launch_bounds__(256) k_grad_b1(float* __restrict__ b1, float const* __restrict__ part, int np,
+                                                 int H) {
+  __shared__ float red[8];
+  tc::grid_dependency_wait();
+  tc::launch_dependents();
+  int const i = blockIdx.x;
+  float t = 0.0f;
+  for (int p = threadIdx.x; p < np; p += blockDim.x) t += part[(int64_t)p * H + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float u = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) u += red[w];
+    b1[i] = u;
+  }
+}
+
+// Shared memory of the output-layer kernels: one row of partial sums per warp.
+size_t head_smem_bytes(int H) { return (size_t)8 * (3 * H + 2) * 4; }
+
 // Patch network (sed_mlp_create_patch): X row b N + i holds the P spins of
 // site i's patch (patch[i][0..P)) of sample b, zero past P; eight threads
 // per row, 16 bytes each; thread (row b N, chunk 0) also copies sample b's
@@ -308,23 +393,17 @@ __global__ void k_batch_patch(uint64_t const* __restrict__ states, float const* 
 // chunks l and l + 32): hs = sum over the sites of h2, (a, s) = W3 hs + b3.
 // With `out` set only (a, s) are written (inference). Otherwise the output
 // gradient as in k_head, g2 = (dout W3) (1 - h2^2) for every site row (BF16),
-// and the sums db2 (unrounded g2), dW3 = dout^T hs, db3 and the loss partial.
+// the block's partial sums of db2 (unrounded g2), dW3 = dout^T hs and db3
+// (head_block_partial) and its loss partial.
 __global__ void __launch_bounds__(256)
     k_head_patch(__nv_bfloat16 const* __restrict__ h2, int H, int n_sites, int64_t n,
                  __nv_bfloat16 const* __restrict__ W3, float const* __restrict__ b3,
                  uint64_t const* __restrict__ bst, float const* __restrict__ bta, float const* __restrict__ bts,
-                 uint64_t sign_mask, __nv_bfloat16* __restrict__ g2, float* __restrict__ db2,
-                 float* __restrict__ dW3, float* __restrict__ db3, double* __restrict__ loss_partial,
-                 float* __restrict__ out) {
-  extern __shared__ float sacc[];  // [3][H]
+                 uint64_t sign_mask, __nv_bfloat16* __restrict__ g2, float* __restrict__ part,
+                 double* __restrict__ loss_partial, float* __restrict__ out) {
+  extern __shared__ float sacc[];  // [warps][3H + 2] (training only)
   __shared__ double red[32];
-  __shared__ float sd[2];
   bool const train = out == nullptr;
-  if (train) {
-    for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) sacc[c] = 0.0f;
-    if (threadIdx.x < 2) sd[threadIdx.x] = 0.0f;
-  }
-  __syncthreads();
   tc::grid_dependency_wait();
   tc::launch_dependents();
   int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, chunks = H / 8;
@@ -428,46 +507,24 @@ __global__ void __launch_bounds__(256)
     }
   }
   if (!train) return;
-#pragma unroll
-  for (int q = 0; q < kHeadChunks; ++q) {
-    int const ch = lane + 32 * q;
-    if (ch >= chunks) continue;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      atomicAdd(&sacc[8 * ch + j], ab[q][j]);
-      atomicAdd(&sacc[H + 8 * ch + j], a0[q][j]);
-      atomicAdd(&sacc[2 * H + 8 * ch + j], a1[q][j]);
-    }
-  }
-  if (lane == 0) {
-    atomicAdd(&sd[0], sd0);
-    atomicAdd(&sd[1], sd1);
-  }
   double const tot = block_sum(l, red);
   if (threadIdx.x == 0) loss_partial[blockIdx.x] = tot;
-  __syncthreads();
-  for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) atomicAdd(c < H ? db2 + c : dW3 + (c - H), sacc[c]);
-  if (threadIdx.x < 2) atomicAdd(db3 + threadIdx.x, sd[threadIdx.x]);
+  head_block_partial(ab, a0, a1, sd0, sd1, H, sacc, part);
 }
 
 // Output layer, loss and first backward step for rows [0, n): one warp per
 // row, lane l holding the 8-column chunks l and l + 32 of h2. Per row
 // (a, s) = W3 h2 + b3 (warp sums), the output gradient as in k_out_grad,
-// g2 = (dout W3) (1 - h2^2) written as BF16; the row sums of g2 (db2), of
-// dout_c h2 (dW3) and of dout (db3) go through shared memory into the
-// gradient; the loss partial of the block into loss_partial.
+// g2 = (dout W3) (1 - h2^2) written as BF16; the block's partial sums of g2
+// (db2), of dout_c h2 (dW3) and of dout (db3) into part (head_block_partial);
+// the loss partial of the block into loss_partial.
 __global__ void __launch_bounds__(256)
     k_head(__nv_bfloat16 const* __restrict__ h2, int H, int64_t n, __nv_bfloat16 const* __restrict__ W3,
            float const* __restrict__ b3, uint64_t const* __restrict__ bst, float const* __restrict__ bta,
            float const* __restrict__ bts, uint64_t sign_mask, __nv_bfloat16* __restrict__ g2,
-           float* __restrict__ db2, float* __restrict__ dW3, float* __restrict__ db3,
-           double* __restrict__ loss_partial) {
-  extern __shared__ float sacc[];  // [3][H]: db2, dW3 row 0, dW3 row 1
+           float* __restrict__ part, double* __restrict__ loss_partial) {
+  extern __shared__ float sacc[];  // [warps][3H + 2]
   __shared__ double red[32];
-  __shared__ float sd[2];
-  for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) sacc[c] = 0.0f;
-  if (threadIdx.x < 2) sd[threadIdx.x] = 0.0f;
-  __syncthreads();
   tc::grid_dependency_wait();
   tc::launch_dependents();
   int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, chunks = H / 8;
@@ -562,26 +619,9 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
-#pragma unroll
-  for (int q = 0; q < kHeadChunks; ++q) {
-    int const ch = lane + 32 * q;
-    if (ch >= chunks) continue;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      atomicAdd(&sacc[8 * ch + j], ab[q][j]);
-      atomicAdd(&sacc[H + 8 * ch + j], a0[q][j]);
-      atomicAdd(&sacc[2 * H + 8 * ch + j], a1[q][j]);
-    }
-  }
-  if (lane == 0) {
-    atomicAdd(&sd[0], sd0);
-    atomicAdd(&sd[1], sd1);
-  }
   double const tot = block_sum(l, red);  // contains a __syncthreads
   if (threadIdx.x == 0) loss_partial[blockIdx.x] = tot;
-  __syncthreads();
-  for (int c = threadIdx.x; c < 3 * H; c += blockDim.x) atomicAdd(c < H ? db2 + c : dW3 + (c - H), sacc[c]);
-  if (threadIdx.x < 2) atomicAdd(db3 + threadIdx.x, sd[threadIdx.x]);
+  head_block_partial(ab, a0, a1, sd0, sd1, H, sacc, part);
 }
 
 __global__ void k_to_bf16(float const* __restrict__ p, __nv_bfloat16* __restrict__ pb, int64_t n) {
@@ -1159,6 +1199,10 @@ struct MlpData {
   // states and targets, the padded BF16 copy of W1, an error flag, and the
   // tensor maps over them (K-major "k" and M-/N-major "m" boxes)
   DeviceBuffer tX, tH1, tH2, tG2, tG1, tW1p, tState, tAbs, tSign, t_error;
+  // partial sums of the gradient, reduced in a fixed order (k_grad_rest,
+  // k_grad_b1): the K-split slabs of dW1 and dW2, the column sums of g1 per
+  // (128-row tile, warp), the output-layer blocks' rows
+  DeviceBuffer pW1, pW2, pB1, pHead;
   uint64_t t_cap = 0, t_cap_samples = 0, t_rows = 0;
   bool t_wmaps = false;
   // patch network (n_sites > 0): the n_in = P sites of each site's patch,
@@ -1339,6 +1383,29 @@ uint64_t tc_rows(MlpData const& d, uint64_t samples) { return samples * (d.n_sit
 // Output tile width of the hidden-layer GEMMs.
 int tc_tile(MlpData const& d) { return d.hidden >= 128 ? 128 : 64; }
 
+// K splits of a weight gradient: as many CTAs as fit on the multiprocessors
+// in one wave (one 128-column CTA per multiprocessor)
+int tc_split(MlpData const& d, int tiles, int k_tiles) {
+  return std::max(1, std::min(k_tiles, d.n_sm / tiles));
+}
+
+// Launch geometry of one training step on n samples (n_sm must be known).
+struct TcShape {
+  int rows, k_tiles, s2, s1, m_tiles, hb;
+};
+TcShape tc_shape(MlpData const& d, uint64_t n) {
+  TcShape t;
+  int const H = (int)d.hidden, tn = tc_tile(d), mh = (H + 127) / 128;
+  t.rows = (int)tc_rows(d, n);
+  t.k_tiles = (t.rows + 63) / 64;
+  t.s2 = tc_split(d, mh * (H / tn), t.k_tiles);
+  t.s1 = tc_split(d, mh, t.k_tiles);
+  t.m_tiles = (t.rows + 127) / 128;
+  uint64_t const per_block = d.n_sites ? 8 : 64;  // samples per output-layer block
+  t.hb = (int)std::max<uint64_t>(1, std::min<uint64_t>((n + per_block - 1) / per_block, 152 * 16));
+  return t;
+}
+
 // Tensor-core training: buffers for batches of up to `samples` samples,
 // tensor maps for batches of exactly `samples` (rows past them read as
 // zero); with `reset` also the padded W1 copy refreshed from the FP32 master
@@ -1383,6 +1450,17 @@ int tc_train_prepare(MlpData& d, uint64_t samples, bool reset = true) {
     d.t_rows = rows;
   }
   if (d.n_sm == 0) SED_TRY_CUDA(cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, d.device));
+  {  // partial-sum buffers of a step on this many samples
+    TcShape const sh = tc_shape(d, samples);
+    auto need = [](DeviceBuffer& b, size_t bytes) { return b.bytes >= bytes ? LS_SUCCESS : b.allocate(bytes); };
+    if (int st = need(d.pW1, (size_t)sh.s1 * H * d.n_in * 4)) return st;
+    if (int st = need(d.pW2, (size_t)sh.s2 * H * H * 4)) return st;
+    if (int st = need(d.pB1, (size_t)sh.m_tiles * 4 * H * 4)) return st;
+    if (int st = need(d.pHead, (size_t)sh.hb * (3 * H + 2) * 4)) return st;
+    SED_TRY_CUDA(cudaFuncSetAttribute(k_head, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)head_smem_bytes((int)H)));
+    SED_TRY_CUDA(cudaFuncSetAttribute(k_head_patch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)head_smem_bytes((int)H)));
+  }
   if (reset) {
     { k_w1_pad<<<blocks_for((int64_t)H * 64), 256, 0, d.stream>>>(d.p.as<float>() + d.oW1, (int)d.n_in, (int)H, d.tW1p.as<__nv_bfloat16>()); note_launches(1); }
     SED_TRY_CUDA(cudaMemsetAsync(d.t_error.ptr, 0, 4, d.stream));
@@ -1391,22 +1469,17 @@ int tc_train_prepare(MlpData& d, uint64_t samples, bool reset = true) {
   return LS_SUCCESS;
 }
 
-// K splits of a weight gradient: as many CTAs as fit on the multiprocessors
-// in one wave (one 128-column CTA per multiprocessor)
-int tc_split(MlpData const& d, int tiles, int k_tiles) {
-  return std::max(1, std::min(k_tiles, d.n_sm / tiles));
-}
-
 // Forward and backward pass of batch rows [0, n) (staged by k_batch): the
-// gradient added into d.g (cleared first with zero_grad), the loss (if
-// requested) into *loss. Every kernel of the step is launched with
-// programmatic stream serialisation.
-int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
+// gradient into d.g, the loss (if requested) into *loss. Every kernel of the
+// step is launched with programmatic stream serialisation. The gradient's
+// sums go through partial-sum buffers reduced in a fixed order, so a step
+// gives the same bits every time.
+int tc_train_step(MlpData& d, uint64_t n, double* loss) {
   cudaStream_t s = d.stream;
-  int const H = (int)d.hidden, N = (int)tc_rows(d, n), tn = tc_tile(d);
+  TcShape const sh = tc_shape(d, n);
+  int const H = (int)d.hidden, N = sh.rows, tn = tc_tile(d);
   float* const G = d.g.as<float>();
   float const* const P = d.p.as<float>();
-  if (zero_grad) SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, s));
   TcGemmArgs base;
   base.error = d.t_error.as<int>();
   base.wait_ns = device_wait_ns(kTcWaitNs);
@@ -1425,13 +1498,12 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   f.out_bf16 = d.tH2.as<__nv_bfloat16>();
   if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, tn)) return st;
   // output layer, loss, g2, db2, dW3, db3
-  unsigned hb;
+  unsigned const hb = (unsigned)sh.hb;
+  size_t const hsm = head_smem_bytes(H);
   if (d.n_sites) {  // one warp per sample
-    hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 7) / 8, 152 * 16));
-    SED_TRY_CUDA(launch_pdl(k_head_patch, dim3(hb), dim3(256), 3 * (size_t)H * 4, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int)d.n_sites, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>(), (float*)nullptr));
-  } else {
-    hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 63) / 64, 152 * 16));  // <= 8 rows a warp
-    SED_TRY_CUDA(launch_pdl(k_head, dim3(hb), dim3(256), 3 * (size_t)H * 4, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), G + d.ob2, G + d.oW3, G + d.ob3, d.loss_part.as<double>()));
+    SED_TRY_CUDA(launch_pdl(k_head_patch, dim3(hb), dim3(256), hsm, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int)d.n_sites, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), d.pHead.as<float>(), d.loss_part.as<double>(), (float*)nullptr));
+  } else {  // <= 8 rows a warp
+    SED_TRY_CUDA(launch_pdl(k_head, dim3(hb), dim3(256), hsm, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int64_t)n, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), P + d.ob3, (uint64_t const*)d.tState.as<uint64_t>(), (float const*)d.tAbs.as<float>(), (float const*)d.tSign.as<float>(), d.sign_mask, d.tG2.as<__nv_bfloat16>(), d.pHead.as<float>(), d.loss_part.as<double>()));
   }
   note_launches(1);
   // g1 = bf16((g2 W2) (1 - h1^2)) and db1; W2 read N-major (element (i, o) at W2[o][i])
@@ -1443,7 +1515,7 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   b.epilogue = kEpiBack;
   b.aux = d.tH1.as<__nv_bfloat16>();
   b.ld_aux = H;
-  b.colsum = G + d.ob1;
+  b.colsum = d.pB1.as<float>();
   b.out_bf16 = d.tG1.as<__nv_bfloat16>();
   b.ld_out = H;
   if (int st = tc_gemm(s, d.mG2k, d.mW2m, b, tn)) return st;
@@ -1454,18 +1526,21 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss, bool zero_grad) {
   w.k_tiles = (N + 63) / 64;
   w.a_mn = w.b_mn = 1;
   w.epilogue = kEpiAdd;
-  w.out_f32 = G + d.oW2;
+  w.out_f32 = d.pW2.as<float>();
   w.ld_f32 = H;
   w.n_valid = H;
-  int const m_tiles = (H + 127) / 128;
-  w.split = tc_split(d, m_tiles * (H / tn), w.k_tiles);
+  w.split = sh.s2;
   if (int st = tc_gemm(s, d.mG2m, d.mH1m, w, tn)) return st;
   w.N = 64;
-  w.out_f32 = G + d.oW1;
+  w.out_f32 = d.pW1.as<float>();
   w.ld_f32 = d.n_in;
   w.n_valid = (int)d.n_in;
-  w.split = tc_split(d, m_tiles, w.k_tiles);
+  w.split = sh.s1;
   if (int st = tc_gemm(s, d.mG1m, d.mXm, w, 64)) return st;
+  // the gradient, each entry added in a fixed order
+  SED_TRY_CUDA(launch_pdl(k_grad_b1, dim3(H), dim3(256), 0, s, G + d.ob1, (float const*)d.pB1.as<float>(), sh.m_tiles * 4, H));
+  SED_TRY_CUDA(launch_pdl(k_grad_rest, dim3(blocks_for((int64_t)d.n_params)), dim3(256), 0, s, G, (int)d.n_in, H, (float const*)d.pW1.as<float>(), sh.s1, (float const*)d.pW2.as<float>(), sh.s2, (float const*)d.pHead.as<float>(), (int)hb));
+  note_launches(2);
   if (loss) {
     std::vector<double> lp(hb);
     SED_TRY_CUDA(cudaMemcpyAsync(lp.data(), d.loss_part.ptr, hb * 8, cudaMemcpyDeviceToHost, s));
@@ -1516,7 +1591,7 @@ int forward_patch(MlpData& d, uint64_t const* states, uint64_t n, float* out) {
     f.out_bf16 = d.tH2.as<__nv_bfloat16>();
     if (int st = tc_gemm(s, d.mH1k, d.mW2k, f, tn)) return st;
     unsigned const hb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((nb + 7) / 8, 152 * 16));
-    SED_TRY_CUDA(launch_pdl(k_head_patch, dim3(hb), dim3(256), 0, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int)d.n_sites, (int64_t)nb, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), (float const*)(d.p.as<float>() + d.ob3), (uint64_t const*)nullptr, (float const*)nullptr, (float const*)nullptr, d.sign_mask, (__nv_bfloat16*)nullptr, (float*)nullptr, (float*)nullptr, (float*)nullptr, (double*)nullptr, out + 2 * b0));
+    SED_TRY_CUDA(launch_pdl(k_head_patch, dim3(hb), dim3(256), 0, s, (__nv_bfloat16 const*)d.tH2.as<__nv_bfloat16>(), H, (int)d.n_sites, (int64_t)nb, (__nv_bfloat16 const*)(d.pb.as<__nv_bfloat16>() + d.oW3), (float const*)(d.p.as<float>() + d.ob3), (uint64_t const*)nullptr, (float const*)nullptr, (float const*)nullptr, d.sign_mask, (__nv_bfloat16*)nullptr, (float*)nullptr, (double*)nullptr, out + 2 * b0));
     note_launches(1);
   }
   return tc_check_error(d);
@@ -1723,7 +1798,7 @@ int sed_mlp_loss_grad(sed_mlp* m, uint64_t const* states, float const* t_abs, fl
     } else {
       { k_batch<<<blocks_for((int64_t)n * 8), 256, 0, d.stream>>>(sb.as<uint64_t>(), ta.as<float>(), ts.as<float>(), nullptr, 0, (int64_t)n, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()); note_launches(1); }
     }
-    if (int st = tc_train_step(d, n, loss, true)) return st;
+    if (int st = tc_train_step(d, n, loss)) return st;
     if (int st = tc_check_error(d)) return st;
   } else {
     if (int st = forward(d, sb.as<uint64_t>(), n, true)) return st;
@@ -1750,8 +1825,8 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
     float const c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)d.step)));
     float const c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)d.step)));
     dim3 const grid(blocks_for((int64_t)d.n_params));
-    if (w1p) {  // tensor-core step: leaves the gradient cleared for the next one
-      SED_TRY_CUDA(launch_pdl(k_adam, grid, dim3(256), 0, d.stream, d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2, w1p, (int)d.n_in, (int64_t)d.hidden * d.n_in, true));
+    if (w1p) {  // tensor-core step (it rewrites the whole gradient)
+      SED_TRY_CUDA(launch_pdl(k_adam, grid, dim3(256), 0, d.stream, d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2, w1p, (int)d.n_in, (int64_t)d.hidden * d.n_in, false));
     } else {
       k_adam<<<grid, 256, 0, d.stream>>>(d.p.as<float>(), d.g.as<float>(), d.m.as<float>(), d.v.as<float>(), d.pb.as<__nv_bfloat16>(), (int64_t)d.n_params, lr, c1, c2, nullptr, (int)d.n_in, (int64_t)0, false);
     }
@@ -1772,7 +1847,6 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
     if (int st = stage(ts, t_sign, n * 4, d.stream)) return st;
     if (int st = perm.allocate(n * 4)) return st;
     if (int st = tc_train_prepare(d, bsz)) return st;
-    SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, d.stream));  // then k_adam clears it each step
     int half = 1;
     while ((1ull << (2 * half)) < n) ++half;
     std::mt19937_64 rng(seed);
@@ -1787,7 +1861,7 @@ int sed_mlp_train(sed_mlp* m, uint64_t const* states, float const* t_abs, float 
           SED_TRY_CUDA(launch_pdl(k_batch, dim3(blocks_for((int64_t)bsz * 8)), dim3(256), 0, d.stream, (uint64_t const*)sb.as<uint64_t>(), (float const*)ta.as<float>(), (float const*)ts.as<float>(), (uint32_t const*)perm.as<uint32_t>(), bi * bsz, (int64_t)bsz, (int)d.n_in, d.tX.as<__nv_bfloat16>(), d.tState.as<uint64_t>(), d.tAbs.as<float>(), d.tSign.as<float>()));
         note_launches(1);
         bool const last = ep + 1 == epochs && bi + 1 == nb;
-        if (int st = tc_train_step(d, bsz, last ? &loss : nullptr, false)) return st;
+        if (int st = tc_train_step(d, bsz, last ? &loss : nullptr)) return st;
         if (int st = adam(d.tW1p.as<__nv_bfloat16>())) return st;
       }
       SED_TRY_CUDA(cudaGetLastError());

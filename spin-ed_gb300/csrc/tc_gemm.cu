@@ -2,7 +2,7 @@
 // training step of the learned start vector (mlp.cu).
 //
 // One CTA computes a 128 x BN tile of D = A B^T over its share of K (the K
-// splits of a weight gradient add into one FP32 output). Warp-specialised:
+// splits of a weight gradient are written as separate slabs). Warp-specialised:
 // warp 4 streams 64-deep K slabs of A and B through a 4-stage ring with TMA,
 // warp 5 issues the MMAs (M = 128, N = BN, K = 16) into BN tensor-memory
 // columns, warps 0-3 wait for the last MMA and run the epilogue, thread t on
@@ -227,17 +227,17 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             for (int j = 0; j < 32; ++j) v[j] = 0.0f;
           }
           float const s = warp_column_sums(v, lane);
-          atomicAdd(p.colsum + n + lane, s);
-        } else if (live) {  // kEpiAdd
-          float* const dst = p.out_f32 + (int64_t)m * p.ld_f32 + n;
+          p.colsum[((int64_t)blockIdx.y * 4 + warp) * p.N + n + lane] = s;  // partial per (m-tile, warp)
+        } else if (live) {  // kEpiAdd: this split's slab, reduced in a fixed order afterwards
+          float* const dst = p.out_f32 + ((int64_t)blockIdx.z * p.M + m) * p.ld_f32 + n;
           if (vec_add && n + 32 <= p.n_valid) {
 #pragma unroll
             for (int q = 0; q < 8; ++q)
-              atomicAdd(reinterpret_cast<float4*>(dst) + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+              reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
           } else {
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-              if (n + j < p.n_valid) atomicAdd(dst + j, v[j]);
+              if (n + j < p.n_valid) dst[j] = v[j];
           }
         }
       }

@@ -21,8 +21,8 @@ int tma_map_bf16(CUtensorMap* out, void const* base, uint64_t rows, uint64_t col
 
 enum TcEpilogue : int {
   kEpiTanh = 0,  // out_bf16[m][n] = bf16(tanh(acc + bias[n]))
-  kEpiBack = 1,  // v = acc (1 - aux[m][n]^2); out_bf16[m][n] = bf16(v); colsum[n] += sum over m of v
-  kEpiAdd = 2,   // out_f32[m][n] += acc for n < n_valid (atomic: several K splits add into one output)
+  kEpiBack = 1,  // v = acc (1 - aux[m][n]^2); out_bf16[m][n] = bf16(v); column sums of v (see colsum)
+  kEpiAdd = 2,   // out_f32[z][m][n] = acc for n < n_valid, z = the K split (one slab of M x ld_f32 per split)
 };
 
 struct TcGemmArgs {
@@ -37,7 +37,7 @@ struct TcGemmArgs {
   int64_t ld_out = 0;
   __nv_bfloat16 const* aux = nullptr;
   int64_t ld_aux = 0;
-  float* colsum = nullptr;
+  float* colsum = nullptr;  // kEpiBack: colsum[(m-tile * 4 + warp) * N + n] = the sum over the warp's 32 rows
   float* out_f32 = nullptr;
   int64_t ld_f32 = 0;
   int n_valid = 0;
