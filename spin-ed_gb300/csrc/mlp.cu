@@ -150,16 +150,6 @@ __global__ void k_tanh_back(float const* __restrict__ h, float* __restrict__ g, 
     g[q] *= 1.0f - h[q] * h[q];
 }
 
-// db[j] += sum over rows b = blockIdx.y (mod gridDim.y) of g[b][j]; db must
-// be zeroed first.
-__global__ void k_colsum(float const* __restrict__ g, int64_t rows, int cols, float* __restrict__ db) {
-  int const j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= cols) return;
-  float s = 0.0f;
-  for (int64_t b = blockIdx.y; b < rows; b += gridDim.y) s += g[b * cols + j];
-  atomicAdd(db + j, s);
-}
-
 // Adam step on the FP32 master copy, refreshing the BF16 copy; with w1p set
 // also the tensor-core training's copy of W1 (the first n_w1 = hidden x
 // n_in parameters), rows padded to 64 inputs; with zero_g the gradient is
@@ -302,7 +292,7 @@ __device__ __forceinline__ void head_block_partial(float const (&ab)[kHeadChunks
 // The step's gradient from its partial sums, each added in a fixed order:
 // W1 and W2 from the K-split slabs of their GEMMs (s1, s2 slabs), b2, W3 and
 // b3 from the output-layer blocks' rows (nhb rows of 3H + 2); b1 is left to
-// k_grad_b1.
+// k_column_sums.
 __global__ void k_grad_rest(float* __restrict__ g, int n_in, int H, float const* __restrict__ w1part, int s1,
                             float const* __restrict__ w2part, int s2, float const* __restrict__ hpart, int nhb) {
   tc::grid_dependency_wait();
@@ -311,7 +301,7 @@ __global__ void k_grad_rest(float* __restrict__ g, int n_in, int H, float const*
                 ob3 = oW3 + 2 * H, n = ob3 + 2;
   int const W = 3 * H + 2;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    if (q >= ob1 && q < oW2) continue;  // b1: k_grad_b1
+    if (q >= ob1 && q < oW2) continue;  // b1: k_column_sums
     float t = 0.0f;
     if (q < nW1) {
       for (int z = 0; z < s1; ++z) t += w1part[(int64_t)z * nW1 + q];
@@ -326,17 +316,18 @@ __global__ void k_grad_rest(float* __restrict__ g, int n_in, int H, float const*
   }
 }
 
-// b1[i] = the sum over the np partial column sums part[p][i] of the g1 GEMM's
-// epilogue; one block per column, strided partial sums added in a fixed
-// tree order.
-__global__ void __launch_bounds__(256) k_grad_b1(float* __restrict__ b1, float const* __restrict__ part, int np,
-                                                 int H) {
+// out[i] = sum over p < np of a[p][i] (a: np rows of `ld`, one block per
+// column i): strided partial sums added in a fixed tree order, so the result
+// does not depend on timing. Used for b1 from the g1 GEMM's partial column
+// sums and for the CUDA-core path's bias gradients.
+__global__ void __launch_bounds__(256) k_column_sums(float* __restrict__ out, float const* __restrict__ a, int64_t np,
+                                                     int ld) {
   __shared__ float red[8];
   tc::grid_dependency_wait();
   tc::launch_dependents();
   int const i = blockIdx.x;
   float t = 0.0f;
-  for (int p = threadIdx.x; p < np; p += blockDim.x) t += part[(int64_t)p * H + i];
+  for (int64_t p = threadIdx.x; p < np; p += blockDim.x) t += a[p * ld + i];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
@@ -344,7 +335,7 @@ __global__ void __launch_bounds__(256) k_grad_b1(float* __restrict__ b1, float c
   if (threadIdx.x == 0) {
     float u = 0.0f;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) u += red[w];
-    b1[i] = u;
+    out[i] = u;
   }
 }
 
@@ -1200,7 +1191,7 @@ struct MlpData {
   // tensor maps over them (K-major "k" and M-/N-major "m" boxes)
   DeviceBuffer tX, tH1, tH2, tG2, tG1, tW1p, tState, tAbs, tSign, t_error;
   // partial sums of the gradient, reduced in a fixed order (k_grad_rest,
-  // k_grad_b1): the K-split slabs of dW1 and dW2, the column sums of g1 per
+  // k_column_sums): the K-split slabs of dW1 and dW2, the column sums of g1 per
   // (128-row tile, warp), the output-layer blocks' rows
   DeviceBuffer pW1, pW2, pB1, pHead;
   uint64_t t_cap = 0, t_cap_samples = 0, t_rows = 0;
@@ -1271,22 +1262,21 @@ int backward(MlpData& d, uint64_t const* states, uint64_t n, float const* t_abs,
   unsigned const lb = blocks_for((int64_t)n);
   SED_TRY_CUDA(cudaMemsetAsync(d.g.ptr, 0, d.n_params * 4, s));
   { k_out_grad<<<lb, 256, 0, s>>>(d.out.as<float>(), states, d.sign_mask, t_abs, t_sign, (int64_t)n, d.dout.as<float>(), d.loss_part.as<double>()); note_launches(1); }
-  unsigned const ry = (unsigned)std::min<int64_t>(512, std::max<int64_t>(1, (int64_t)n / 64));
   // dW3 [2 x H] = dout^T h2 ; db3 = colsum(dout)
   gemm<float>(s, 2, H, N, d.dout.as<float>(), 1, 2, d.h2.as<float>(), H, 1, G + d.oW3, H, nullptr, 0, 0);
-  { k_colsum<<<dim3(1, ry), 32, 0, s>>>(d.dout.as<float>(), (int64_t)n, 2, G + d.ob3); note_launches(1); }
+  { k_column_sums<<<2, 256, 0, s>>>(G + d.ob3, d.dout.as<float>(), (int64_t)n, 2); note_launches(1); }
   // dh2 [N x H] = dout W3, times tanh'
   gemm<__nv_bfloat16>(s, N, H, 2, d.dout.as<float>(), 2, 1, W + d.oW3, H, 1, d.d2.as<float>(), H, nullptr, 0, 0);
   { k_tanh_back<<<blocks_for((int64_t)n * H), 256, 0, s>>>(d.h2.as<float>(), d.d2.as<float>(), (int64_t)n * H); note_launches(1); }
   // dW2 [H x H] = dh2^T h1 ; db2
   gemm<float>(s, H, H, N, d.d2.as<float>(), 1, H, d.h1.as<float>(), H, 1, G + d.oW2, H, nullptr, 0, 0);
-  { k_colsum<<<dim3((H + 255) / 256, ry), 256, 0, s>>>(d.d2.as<float>(), (int64_t)n, H, G + d.ob2); note_launches(1); }
+  { k_column_sums<<<H, 256, 0, s>>>(G + d.ob2, d.d2.as<float>(), (int64_t)n, H); note_launches(1); }
   // dh1 [N x H] = dh2 W2, times tanh'
   gemm<__nv_bfloat16>(s, N, H, H, d.d2.as<float>(), H, 1, W + d.oW2, H, 1, d.d1.as<float>(), H, nullptr, 0, 0);
   { k_tanh_back<<<blocks_for((int64_t)n * H), 256, 0, s>>>(d.h1.as<float>(), d.d1.as<float>(), (int64_t)n * H); note_launches(1); }
   // dW1 [H x I] = dh1^T x ; db1
   gemm<float>(s, H, I, N, d.d1.as<float>(), 1, H, d.x.as<float>(), I, 1, G + d.oW1, I, nullptr, 0, 0);
-  { k_colsum<<<dim3((H + 255) / 256, ry), 256, 0, s>>>(d.d1.as<float>(), (int64_t)n, H, G + d.ob1); note_launches(1); }
+  { k_column_sums<<<H, 256, 0, s>>>(G + d.ob1, d.d1.as<float>(), (int64_t)n, H); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   if (loss) {
     std::vector<double> lp(lb);
@@ -1538,7 +1528,7 @@ int tc_train_step(MlpData& d, uint64_t n, double* loss) {
   w.split = sh.s1;
   if (int st = tc_gemm(s, d.mG1m, d.mXm, w, 64)) return st;
   // the gradient, each entry added in a fixed order
-  SED_TRY_CUDA(launch_pdl(k_grad_b1, dim3(H), dim3(256), 0, s, G + d.ob1, (float const*)d.pB1.as<float>(), sh.m_tiles * 4, H));
+  SED_TRY_CUDA(launch_pdl(k_column_sums, dim3(H), dim3(256), 0, s, G + d.ob1, (float const*)d.pB1.as<float>(), (int64_t)sh.m_tiles * 4, H));
   SED_TRY_CUDA(launch_pdl(k_grad_rest, dim3(blocks_for((int64_t)d.n_params)), dim3(256), 0, s, G, (int)d.n_in, H, (float const*)d.pW1.as<float>(), sh.s1, (float const*)d.pW2.as<float>(), sh.s2, (float const*)d.pHead.as<float>(), (int)hb));
   note_launches(2);
   if (loss) {
