@@ -396,7 +396,9 @@ SED_API int sed_mlp_loss_grad(sed_mlp* mlp, uint64_t const* states, float const*
  * every epoch (floor(n / batch) batches; the rest of a shuffle is unused);
  * final_loss (may be NULL) is the loss of the last batch. On the tensor-core
  * path (sed_mlp_set_path) the shuffle is a keyed permutation made on the
- * device, at most 2^31 - 1 samples; on the SIMT path a host shuffle. */
+ * device, at most 2^31 - 1 samples; on the SIMT path a host shuffle. Both
+ * paths add every gradient sum in a fixed order: the same data, starting
+ * parameters and seed give the same network bit for bit. */
 SED_API int sed_mlp_train(sed_mlp* mlp, uint64_t const* states, float const* t_abs, float const* t_sign, uint64_t n,
                           unsigned epochs, unsigned batch, float lr, uint64_t seed, double* final_loss);
 /* Training data from a real vector psi over the built basis: n representatives
