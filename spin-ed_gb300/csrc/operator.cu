@@ -29,9 +29,10 @@ namespace {
 // ---------------------------------------------------------------- kernels --
 
 // Per-slice maximum element count (slots = 32 * max) and element total.
+// (max_width: the largest slice width, for sizing k_record's buffers.)
 __global__ void k_count(uint64_t const* __restrict__ reps, uint64_t D, TermsView T,
                         uint64_t n_slices, uint64_t* __restrict__ slots,
-                        uint64_t* __restrict__ elements) {
+                        uint64_t* __restrict__ elements, unsigned* __restrict__ max_width) {
   uint64_t const i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t const s = i >> 5;
   if (s >= n_slices) return;
@@ -41,17 +42,21 @@ __global__ void k_count(uint64_t const* __restrict__ reps, uint64_t D, TermsView
   if ((threadIdx.x & 31) == 0) {
     slots[s] = (uint64_t)m * 32;
     elements[s] = tot;
+    atomicMax(max_width, m);
   }
 }
 
 constexpr unsigned kRecWarps = 4;    // warps per block of k_record
-constexpr unsigned kRecMaxElems = 80; // flattened path: elements per row
+constexpr unsigned kRecBlocks = 5;   // blocks of k_record per SM the registers allow
+constexpr unsigned kRecMaxElems = 80; // flattened path: elements per row at most
 
-size_t record_smem_bytes() {
-  return (size_t)kRecWarps * 32 * kRecMaxElems * 4      // element descriptors
-         + (size_t)kRecWarps * 32 * SED_PARAM_COSETS * 8  // coset images of each row
-         + SED_PARAM_COSETS * 64                         // bit landing positions
-         + 2048 * 2;                                     // row tables
+// k_record's shared memory for `me` element slots per row and `nc` cosets:
+// sized by the operator, so that narrow rows leave room for more blocks.
+size_t record_smem_bytes(unsigned me, unsigned nc) {
+  return (size_t)kRecWarps * 32 * me * 4      // element descriptors
+         + (size_t)kRecWarps * 32 * nc * 8    // coset images of each row
+         + (size_t)nc * 64                    // bit landing positions
+         + 2048 * 2;                          // row tables
 }
 
 // Records the stream form. One warp per SELL-32 slice (lane = row).
@@ -66,35 +71,34 @@ size_t record_smem_bytes() {
 //    leave lanes idle; wider slices fall back to one row per lane.
 // Entries land in the same slots (slice_ptr + 32 e + row) either way.
 template <class W, bool Real>
-__global__ void __launch_bounds__(kRecWarps * 32, 1)
+__global__ void __launch_bounds__(kRecWarps * 32, kRecBlocks)
     k_record(__grid_constant__ const PlanView P, IndexView I, TermsView T, CodeView C,
              uint32_t const* __restrict__ weights, uint64_t n_slices, uint64_t const* __restrict__ slice_ptr,
              uint32_t col_bits, bool packed, uint32_t* __restrict__ entries, uint16_t* __restrict__ codes,
-             void* __restrict__ diag, uint8_t* __restrict__ row_class) {
+             void* __restrict__ diag, uint8_t* __restrict__ row_class, uint32_t me, uint32_t nc) {
   extern __shared__ __align__(16) unsigned char rec_smem[];
   uint32_t* desc_all = reinterpret_cast<uint32_t*>(rec_smem);
-  W* imgs_all = reinterpret_cast<W*>(rec_smem + (size_t)kRecWarps * 32 * kRecMaxElems * 4);
-  uint8_t* pos_s = rec_smem + (size_t)kRecWarps * 32 * kRecMaxElems * 4 +
-                   (size_t)kRecWarps * 32 * SED_PARAM_COSETS * 8;
-  uint16_t* srow = reinterpret_cast<uint16_t*>(pos_s + SED_PARAM_COSETS * 64);
+  W* imgs_all = reinterpret_cast<W*>(rec_smem + (size_t)kRecWarps * 32 * me * 4);
+  uint8_t* pos_s = rec_smem + (size_t)kRecWarps * 32 * me * 4 + (size_t)kRecWarps * 32 * nc * 8;
+  uint16_t* srow = reinterpret_cast<uint16_t*>(pos_s + nc * 64);
   RowTab const RT = stage_rows(P, srow);
   bool const use_pos = P.fixed_nets != 0;
   if (use_pos) {
-    for (uint32_t q = threadIdx.x; q < P.n_cosets * 64; q += blockDim.x) pos_s[q] = P.pos[q];
+    for (uint32_t q = threadIdx.x; q < P.n_cosets * 64; q += blockDim.x) pos_s[q] = P.pos[q];  // n_cosets <= nc
     __syncthreads();
   }
   uint32_t const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t const s = (uint64_t)blockIdx.x * kRecWarps + warp;
   if (s >= n_slices) return;  // warp-uniform
-  uint32_t* desc = desc_all + (size_t)warp * 32 * kRecMaxElems;
-  W* imgs = imgs_all + (size_t)warp * 32 * SED_PARAM_COSETS;
+  uint32_t* desc = desc_all + (size_t)warp * 32 * me;
+  W* imgs = imgs_all + (size_t)warp * 32 * nc;
   uint64_t const i = s * 32 + lane;
   uint64_t const base = slice_ptr[s];
   uint32_t const width = (uint32_t)((slice_ptr[s + 1] - base) >> 5);
   bool const valid = i < I.D;
   uint64_t const r = valid ? I.reps[i] : 0;
   if (use_pos)
-    for (uint32_t c = 0; c < P.n_cosets; ++c) imgs[lane * SED_PARAM_COSETS + c] = coset_apply<W>((W)r, P, c);
+    for (uint32_t c = 0; c < P.n_cosets; ++c) imgs[lane * nc + c] = coset_apply<W>((W)r, P, c);
   __syncwarp();
   auto emit = [&](uint32_t e, uint32_t row, uint64_t r_row, uint64_t st, uint32_t vid) {
     W const x = (W)st;
@@ -108,7 +112,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, 1)
         d &= d - 1;
         pd |= (W)1 << pos_s[c * 64 + b];
       }
-      return imgs[row * SED_PARAM_COSETS + c] ^ pd;
+      return imgs[row * nc + c] ^ pd;
     };
     auto const cz = canonicalize_img<W>(x, P, RT, img);
     int64_t const j = find_index((uint64_t)cz.rep, I);
@@ -121,7 +125,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, 1)
     if (!packed) codes[base + (uint64_t)e * 32 + row] = (uint16_t)code;
   };
   uint32_t count = 0;
-  if (width <= kRecMaxElems && T.n_tuples < 65536) {
+  if (width <= me && T.n_tuples < 65536) {
     if (valid) {
       for (uint32_t u = 0; u < T.n_tuples; ++u) {
         uint32_t const tk = T.tuple_term[u];
@@ -129,7 +133,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, 1)
         uint32_t const a = local_index(r, T.tuple_sites[u], k);
         uint32_t const n = T.n_off[t * 16 + a];
         for (uint32_t q = 0; q < n; ++q)
-          desc[lane * kRecMaxElems + count++] = (q << 28) | (u << 8) | T.off_col[(t * 16 + a) * 16 + q];
+          desc[lane * me + count++] = (q << 28) | (u << 8) | T.off_col[(t * 16 + a) * 16 + q];
       }
     }
     __syncwarp();
@@ -154,7 +158,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, 1)
       uint64_t const r_row = __shfl_sync(0xffffffffu, r, row);
       if (f < total) {
         uint32_t const e = f - ex_row;
-        uint32_t const d = desc[row * kRecMaxElems + e];
+        uint32_t const d = desc[row * me + e];
         uint32_t const u = (d >> 8) & 0xFFFFu, a2 = d & 0xFFu, q = d >> 28;
         uint32_t const tk = T.tuple_term[u];
         uint32_t const t = tk & 0xFFFFu, k = tk >> 16;
@@ -1196,21 +1200,25 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
   bool const packed = col_bits + code_bits <= 31;  // kNull stays unrepresentable
   StreamForm& sf = op.stream;
   sf = StreamForm{};
-  DeviceBuffer elements;
+  DeviceBuffer elements, maxw;
   if (int st = sf.slice_ptr.allocate((n_slices + 1) * 8)) return st;
   if (int st = elements.allocate((n_slices + 1) * 8)) return st;
+  if (int st = maxw.allocate(16)) return st;
+  SED_TRY_CUDA(cudaMemsetAsync(maxw.ptr, 0, 4, stream));
   unsigned const grid = (unsigned)((n_slices * 32 + kBlock - 1) / kBlock);
   if (n_slices) {
     { k_count<<<grid, kBlock, 0, stream>>>(b.reps.as<uint64_t>(), D, op.terms_dev, n_slices,
-                                         sf.slice_ptr.as<uint64_t>(), elements.as<uint64_t>()); note_launches(1); }
+                                         sf.slice_ptr.as<uint64_t>(), elements.as<uint64_t>(), maxw.as<unsigned>()); note_launches(1); }
     SED_TRY_CUDA(cudaGetLastError());
   }
   { k_scan_u64<<<1, 1024, 0, stream>>>(sf.slice_ptr.as<uint64_t>(), n_slices); note_launches(1); }
   { k_scan_u64<<<1, 1024, 0, stream>>>(elements.as<uint64_t>(), n_slices); note_launches(1); }
   SED_TRY_CUDA(cudaGetLastError());
   uint64_t n_entries = 0, n_elements = 0;
+  unsigned max_width = 0;
   SED_TRY_CUDA(cudaMemcpyAsync(&n_entries, sf.slice_ptr.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
   SED_TRY_CUDA(cudaMemcpyAsync(&n_elements, elements.as<uint64_t>() + n_slices, 8, cudaMemcpyDeviceToHost, stream));
+  SED_TRY_CUDA(cudaMemcpyAsync(&max_width, maxw.ptr, 4, cudaMemcpyDeviceToHost, stream));
   SED_TRY_CUDA(cudaStreamSynchronize(stream));
   size_t free_b = 0, total_b = 0;
   SED_TRY_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -1341,12 +1349,16 @@ int operator_record_stream(OperatorData& op, cudaStream_t stream) {
 
       using W = decltype(w_tag);
       constexpr bool R = decltype(real_tag)::value;
-      size_t const smem = record_smem_bytes();
+      // descriptor slots for the widest slice (wider slices than kRecMaxElems
+      // take the row-per-lane path), coset images for this plan's cosets
+      unsigned const me = std::max(1u, std::min(max_width, kRecMaxElems));
+      unsigned const nc = std::max(1u, std::min<unsigned>(b.plan.n_cosets, SED_PARAM_COSETS));
+      size_t const smem = record_smem_bytes(me, nc);
       cudaFuncSetAttribute(k_record<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       { k_record<W, R><<<(unsigned)((n_slices + kRecWarps - 1) / kRecWarps), kRecWarps * 32, smem, stream>>>(
           b.plan_dev, I, op.terms_dev, tb.code, b.weights.as<uint32_t>(), n_slices,
           sf.slice_ptr.as<uint64_t>(), col_bits, packed, sf.entries.as<uint32_t>(),
-          sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>()); note_launches(1); }
+          sf.values.as<uint16_t>(), sf.diag.ptr, sf.row_class.as<uint8_t>(), me, nc); note_launches(1); }
     };
     if (wide) {
       if (op.is_real) launch(uint64_t{}, std::true_type{});
