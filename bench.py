@@ -628,10 +628,11 @@ def main():
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
     ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
     ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
-    ap.add_argument("--profile-case", default=None, choices=["mlp", "train", "batch16", "spmv", "rotate"],
+    ap.add_argument("--profile-case", default=None, choices=["mlp", "train", "record", "batch16", "spmv", "rotate"],
                     help="one small run of a single kernel family, for profilers: the tensor-core MLP "
                          "inference over 2^20 random 36-spin states, one tensor-core training epoch (2^18 "
-                         "samples, 64 batches of 4096), a 16-chain batched solve (one fixed launch shape), 10 "
+                         "samples, 64 batches of 4096), the chain-32 stream form recorded by "
+                         "canonicalisation, a 16-chain batched solve (one fixed launch shape), 10 "
                          "matvecs of the 6x6 stream form (about 3.5 GB on the device), or the thick-restart "
                          "basis rotation on 1e8 rows on both paths (--rotate-rows to change)")
     ap.add_argument("--rotate-rows", type=int, default=100_000_000)
@@ -659,6 +660,18 @@ def main():
         out = net.forward(st)
         print(json.dumps({"case": "mlp", "states": len(st), "tensor_cores": net.uses_tensor_cores,
                           "max_abs": float(np.abs(out).max())}))
+        return
+    if args.profile_case == "record":
+        from spined import internal as I, lattices, _lib as L
+        from spined.model import build_model
+        lib = L.load()
+        lib.sed_set_record_mode(L.SED_RECORD_CANONICALISE)
+        b = build_model(lattices.heisenberg_chain(32))
+        t0 = time.perf_counter()
+        b.hamiltonian.prepare(L.SED_FORM_STREAM)
+        print(json.dumps({"case": "record", "D": I.get_number_states(b.basis), "record_s": time.perf_counter() - t0,
+                          "elements": lib.sed_operator_stream_elements(b.hamiltonian.ptr)}))
+        lib.sed_set_record_mode(L.SED_RECORD_AUTO)
         return
     if args.profile_case == "train":
         import numpy as np
