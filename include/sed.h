@@ -471,6 +471,15 @@ SED_API void sed_set_device_wait_limit(double seconds);
  * reports LS_DEVICE_TIMEOUT; tests use it to exercise that path without a
  * GPU fault. Process-wide. */
 SED_API void sed_debug_barrier_extra_arrivals(unsigned n);
+/* Test hook: the group layout sed_eigh_batched uses on `grid` CTAs for
+ * `count` problems of modelled work work[i] (a block step on n CTAs costs
+ * fixed + work[i] / n) and at most max_ctas[i] CTAs each. Writes group_of[i],
+ * the group of problem i, and per group g below the returned number of
+ * groups its CTA count ncta[g] and problem count nprob[g] (ncta and nprob
+ * hold `grid` entries). Groups take consecutive CTAs in index order.
+ * Returns 0 on invalid arguments. Host only. */
+SED_API unsigned sed_debug_batched_layout(unsigned count, double const* work, uint32_t const* max_ctas, double fixed,
+                                          unsigned grid, uint32_t* group_of, uint32_t* ncta, uint32_t* nprob);
 
 /* Number of libsed kernels launched by this process so far (graph replays
  * count their kernel nodes). */

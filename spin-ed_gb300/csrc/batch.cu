@@ -48,6 +48,11 @@ constexpr int kMaxBlocks = 16;      // stored Krylov blocks per cycle (n <= 64)
 constexpr int kMaxN = kB * kMaxBlocks;
 constexpr int kPart = 16 * (kMaxBlocks + 1);  // partial sums per CTA and slot
 constexpr uint64_t kBarrierNs = 20000000000ull;  // default: 20 s per barrier, far beyond any phase
+// Part of a block step that more CTAs do not shorten, in rows of the mean
+// work per row (the group layout's model). Fitted on 128 J1-J2 chains
+// (N = 16..28, one group per chain): a block step took 1.62 ms plus 0.249 us
+// per row of the CTA's share, i.e. about 6500 rows.
+constexpr double kLayoutFixedRows = 6500.0;
 constexpr size_t kStatsOff = 12 * 8;                // per-problem output record: out[12], stats[4], flag[4], prof[8]
 constexpr size_t kProfOff = kStatsOff + 32;
 constexpr size_t kOutBytes = kProfOff + 64;
@@ -817,6 +822,123 @@ __global__ void k_unpack_block(double const* __restrict__ V, uint64_t D, uint32_
 
 // ------------------------------------------------------------ host side ---
 
+// Groups of the persistent launch. A problem's block step on n CTAs is
+// modelled as fixed + work / n: `fixed` is the part that more CTAs do not
+// shorten (the leader's Rayleigh-Ritz solve, the group barriers), work the
+// part that is split over the group's rows. The layout minimises the
+// modelled makespan T on `grid` CTAs:
+// - a problem with fixed + work > T gets a group of its own with
+//   ceil(work / (T - fixed)) CTAs (at most max_ctas, its slice count);
+// - the other problems are packed, first fit by decreasing work, into
+//   one-CTA groups that solve them one after another within T;
+// - T is the smallest bound (bisection) that needs no more than `grid` CTAs;
+//   CTAs left over go one at a time to the multi-CTA group with the largest
+//   modelled time.
+struct BatchLayout {
+  std::vector<GroupDesc> groups;
+  std::vector<uint32_t> cta_group, order, group_of_chain;
+};
+
+BatchLayout batch_layout(std::vector<double> const& work, std::vector<uint32_t> const& max_ctas, double fixed,
+                         unsigned grid) {
+  size_t const count = work.size();
+  std::vector<uint32_t> idx(count);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return work[a] > work[b]; });
+  struct Try {
+    std::vector<uint32_t> n;  // CTAs of a problem's own group, 0 when packed
+    std::vector<std::vector<uint32_t>> bins;
+    std::vector<double> load;
+    unsigned ctas = 0;
+  };
+  auto attempt = [&](double T, Try& t) {
+    t.n.assign(count, 0);
+    t.bins.clear();
+    t.load.clear();
+    t.ctas = 0;
+    for (uint32_t i : idx) {
+      double const alone = fixed + work[i];
+      if (alone <= T) {
+        size_t b = 0;
+        while (b < t.bins.size() && t.load[b] + alone > T) ++b;
+        if (b == t.bins.size()) {
+          t.bins.emplace_back();
+          t.load.push_back(0.0);
+          ++t.ctas;
+        }
+        t.bins[b].push_back(i);
+        t.load[b] += alone;
+      } else {
+        if (T <= fixed) return false;
+        double const need = std::ceil(work[i] / (T - fixed));
+        if (need > (double)std::max<uint32_t>(1, max_ctas[i]) || need > (double)grid) return false;
+        t.n[i] = (uint32_t)need;
+        t.ctas += t.n[i];
+      }
+      if (t.ctas > grid) return false;
+    }
+    return true;
+  };
+  Try best;
+  double hi = 0.0;
+  for (double w : work) hi += fixed + w;
+  hi = hi * 1.001 + 1.0;
+  if (!attempt(hi, best)) {  // cannot happen: everything fits in one bin
+    best.n.assign(count, 0);
+    best.bins.assign(1, idx);
+    best.ctas = 1;
+  }
+  double lo = 0.0;
+  for (int it = 0; it < 64 && hi - lo > 1e-6 * hi; ++it) {
+    double const mid = 0.5 * (lo + hi);
+    Try t;
+    if (attempt(mid, t)) {
+      hi = mid;
+      best = std::move(t);
+    } else {
+      lo = mid;
+    }
+  }
+  // CTAs left over: to the slowest multi-CTA groups
+  unsigned left = grid - std::min(grid, best.ctas);
+  while (left > 0) {
+    double worst = -1.0;
+    uint32_t wi = UINT32_MAX;
+    for (uint32_t i = 0; i < count; ++i)
+      if (best.n[i] > 0 && best.n[i] < std::max<uint32_t>(1, max_ctas[i])) {
+        double const t = fixed + work[i] / best.n[i];
+        if (t > worst) {
+          worst = t;
+          wi = i;
+        }
+      }
+    if (wi == UINT32_MAX) break;
+    ++best.n[wi];
+    --left;
+  }
+  BatchLayout L;
+  L.group_of_chain.assign(count, 0);
+  uint32_t cta = 0;
+  for (uint32_t i : idx)
+    if (best.n[i] > 0) {
+      L.group_of_chain[i] = (uint32_t)L.groups.size();
+      L.groups.push_back(GroupDesc{cta, best.n[i], (uint32_t)L.order.size(), 1, nullptr});
+      L.order.push_back(i);
+      cta += best.n[i];
+    }
+  for (auto const& bin : best.bins) {
+    L.groups.push_back(GroupDesc{cta, 1, (uint32_t)L.order.size(), (uint32_t)bin.size(), nullptr});
+    for (uint32_t i : bin) {
+      L.group_of_chain[i] = (uint32_t)L.groups.size() - 1;
+      L.order.push_back(i);
+    }
+    cta += 1;
+  }
+  for (uint32_t g = 0; g < L.groups.size(); ++g)
+    for (uint32_t k = 0; k < L.groups[g].ncta; ++k) L.cta_group.push_back(g);
+  return L;
+}
+
 struct Plan {
   unsigned threads = 256, ctas_per_sm = 1;
 };
@@ -952,68 +1074,18 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     }
   }
 
-  // group layout for a given grid
-  struct Layout {
-    std::vector<GroupDesc> groups;
-    std::vector<uint32_t> cta_group, order;
-    std::vector<uint32_t> group_of_chain;
-  };
-  auto make_layout = [&](unsigned grid) {
-    Layout L;
-    std::vector<uint32_t> idx(count);
-    std::iota(idx.begin(), idx.end(), 0u);
-    std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return work[a] > work[b]; });
-    L.group_of_chain.assign(count, 0);
-    if (count <= grid) {
-      // one group per problem, CTAs in proportion to work (largest remainders)
-      // every problem has one CTA; the other grid - count CTAs go out in
-      // proportion to work (floors first, then the largest remainders)
-      double const W = std::accumulate(work.begin(), work.end(), 0.0);
-      std::vector<uint32_t> n(count, 1);
-      unsigned const extra = grid - count;
-      unsigned left = extra;
-      std::vector<std::pair<double, uint32_t>> rem;
-      for (uint32_t i : idx) {
-        double const want = work[i] / W * extra;
-        uint32_t const add = std::min<uint32_t>((uint32_t)want, left);
-        n[i] += add;
-        left -= add;
-        rem.push_back({want - add, i});
-      }
-      std::sort(rem.begin(), rem.end(), [](auto& a, auto& b) { return a.first > b.first; });
-      for (size_t q = 0; q < rem.size() && left > 0; ++q, --left) n[rem[q].second] += 1;
-      // a group never has more CTAs than slices
-      for (unsigned i = 0; i < count; ++i)
-        n[i] = std::max<uint32_t>(1, std::min<uint32_t>(n[i], (uint32_t)od[i]->stream.n_slices));
-      uint32_t cta = 0;
-      for (unsigned q = 0; q < count; ++q) {
-        uint32_t const i = idx[q];
-        L.groups.push_back(GroupDesc{cta, n[i], q, 1, nullptr});
-        L.order.push_back(i);
-        L.group_of_chain[i] = q;
-        cta += n[i];
-      }
-    } else {
-      // more problems than CTAs: one CTA per group, longest-processing-time
-      std::vector<double> load(grid, 0.0);
-      std::vector<std::vector<uint32_t>> lists(grid);
-      for (uint32_t i : idx) {
-        unsigned const g = (unsigned)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[g] += work[i];
-        lists[g].push_back(i);
-      }
-      for (unsigned g = 0; g < grid; ++g) {
-        L.groups.push_back(GroupDesc{g, 1, (uint32_t)L.order.size(), (uint32_t)lists[g].size(), nullptr});
-        for (uint32_t i : lists[g]) {
-          L.group_of_chain[i] = g;
-          L.order.push_back(i);
-        }
-      }
-    }
-    for (uint32_t g = 0; g < L.groups.size(); ++g)
-      for (uint32_t k = 0; k < L.groups[g].ncta; ++k) L.cta_group.push_back(g);
-    return L;
-  };
+  // group layout for a given grid (batch_layout), the fixed part of a block
+  // step expressed in rows of the batch's mean work per row
+  using Layout = BatchLayout;
+  std::vector<uint32_t> max_ctas(count);
+  double sum_work = 0.0, sum_rows = 0.0;
+  for (unsigned i = 0; i < count; ++i) {
+    max_ctas[i] = (uint32_t)std::min<uint64_t>(od[i]->stream.n_slices, UINT32_MAX);
+    sum_work += work[i];
+    sum_rows += (double)od[i]->basis->D;
+  }
+  double const fixed = kLayoutFixedRows * sum_work / std::max(1.0, sum_rows);
+  auto make_layout = [&](unsigned grid) { return batch_layout(work, max_ctas, fixed, grid); };
 
   unsigned max_per_cand = 1;
   for (Plan const& p : cands) max_per_cand = std::max(max_per_cand, p.ctas_per_sm);
@@ -1158,10 +1230,16 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     unsigned worst = 0;
     uint64_t worst_t = 0;
     std::vector<uint64_t> prof(8);
+    Layout const L0 = make_layout((unsigned)sms * plan.ctas_per_sm);
     for (unsigned i = 0; i < count; ++i) {
       SED_TRY_CUDA(cudaMemcpy(prof.data(), base + off_out[i] + kProfOff, 64, cudaMemcpyDeviceToHost));
+      SED_TRY_CUDA(cudaMemcpy(stats.data(), base + off_out[i] + kStatsOff, 16, cudaMemcpyDeviceToHost));
       uint64_t t = 0;
       for (int q = 0; q < 6; ++q) t += prof[q];
+      GroupDesc const& g = L0.groups[L0.group_of_chain[i]];
+      log_line("sed_eigh_batched: problem %u: D = %llu, group %u (%u CTAs, %u problems), %u block steps, %.2f ms "
+               "(rayleigh-ritz %.2f ms)", i, (unsigned long long)od[i]->basis->D, L0.group_of_chain[i], g.ncta,
+               g.count, stats[0], t * 1e-6, prof[3] * 1e-6);
       if (t > worst_t) {
         worst_t = t;
         worst = i;
@@ -1169,11 +1247,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     }
     SED_TRY_CUDA(cudaMemcpy(prof.data(), base + off_out[worst] + kProfOff, 64, cudaMemcpyDeviceToHost));
     SED_TRY_CUDA(cudaMemcpy(stats.data(), base + off_out[worst] + kStatsOff, 16, cudaMemcpyDeviceToHost));
-    unsigned ncta = 0;
-    {
-      Layout L = make_layout((unsigned)sms * plan.ctas_per_sm);
-      ncta = L.groups[L.group_of_chain[worst]].ncta;
-    }
+    unsigned const ncta = L0.groups[L0.group_of_chain[worst]].ncta;
     log_line("sed_eigh_batched: slowest problem %u (D = %llu, %u CTAs, %u block steps, %u restarts): spmv %.2f ms, "
              "cgs2 %.2f ms, qr %.2f ms, rayleigh-ritz %.2f ms, ritz/restart %.2f ms, residual %.2f ms",
              worst, (unsigned long long)od[worst]->basis->D, ncta, stats[0], stats[1], prof[0] * 1e-6,
@@ -1206,4 +1280,21 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
 extern "C" void sed_set_batched_launch(unsigned threads_per_cta, unsigned ctas_per_sm) {
   sed::g_force_threads.store(threads_per_cta ? threads_per_cta : 0u);
   sed::g_force_per_sm.store(threads_per_cta ? ctas_per_sm : 0u);
+}
+
+extern "C" unsigned sed_debug_batched_layout(unsigned count, double const* work, uint32_t const* max_ctas, double fixed,
+                                             unsigned grid, uint32_t* group_of, uint32_t* ncta, uint32_t* nprob) {
+  if (count == 0 || grid == 0 || !work || !max_ctas || !group_of || !ncta || !nprob || !(fixed >= 0.0)) return 0;
+  std::vector<double> w(work, work + count);
+  std::vector<uint32_t> m(max_ctas, max_ctas + count);
+  for (double x : w)
+    if (!(x >= 0.0)) return 0;
+  sed::BatchLayout const L = sed::batch_layout(w, m, fixed, grid);
+  if (L.groups.size() > grid) return 0;
+  for (unsigned i = 0; i < count; ++i) group_of[i] = L.group_of_chain[i];
+  for (size_t g = 0; g < L.groups.size(); ++g) {
+    ncta[g] = L.groups[g].ncta;
+    nprob[g] = L.groups[g].count;
+  }
+  return (unsigned)L.groups.size();
 }

@@ -160,6 +160,8 @@ SIGNATURES = [
     ("sed_device_memory_in_use", _U64, []),
     ("sed_set_device_wait_limit", None, [C.c_double]),
     ("sed_debug_barrier_extra_arrivals", None, [C.c_uint]),
+    ("sed_debug_batched_layout", C.c_uint, [C.c_uint, C.POINTER(C.c_double), C.POINTER(C.c_uint32), C.c_double,
+                                           C.c_uint, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("sed_set_record_mode", None, [_I]),
     ("sed_operator_recorded_with_table", _I, [_P]),
     ("sed_mlp_uses_tensor_cores", _I, [_P]),

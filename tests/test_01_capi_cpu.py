@@ -184,3 +184,81 @@ def test_line_table_plans(sed, capfd, name, n, hw, inv, gens, lines, cols):
     m = re.search(r"line tables: (\d) \(columns: (\d)\)", err)
     assert m, err
     assert (int(m.group(1)), int(m.group(2))) == (lines, cols), err
+
+
+def _layout(lib, work, max_ctas, fixed, grid):
+    import ctypes as C
+    n = len(work)
+    w = (C.c_double * n)(*work)
+    m = (C.c_uint32 * n)(*max_ctas)
+    group_of = (C.c_uint32 * n)()
+    ncta = (C.c_uint32 * max(grid, 1))()
+    nprob = (C.c_uint32 * max(grid, 1))()
+    ng = lib.sed_debug_batched_layout(n, w, m, fixed, grid, group_of, ncta, nprob)
+    return ng, list(group_of), list(ncta[:ng]), list(nprob[:ng])
+
+
+def _makespan(work, fixed, group_of, ncta):
+    t = [0.0] * len(ncta)
+    for i, g in enumerate(group_of):
+        t[g] += fixed + work[i] / ncta[g]
+    return max(t)
+
+
+@pytest.mark.parametrize("count,grid", [(128, 304), (128, 152), (128, 456), (1, 304), (400, 304), (1000, 152)])
+def test_batched_layout(sed, count, grid):
+    """The persistent batched launch's group layout (host logic of
+    sed_eigh_batched): every problem lies in exactly one group, the groups use
+    at most `grid` CTAs and no group more than its problems' slices, a group
+    that solves several problems one after another has one CTA, and the
+    modelled makespan is no worse than one group per problem with CTAs in
+    proportion to work (the layout it replaced), on chain-like sizes."""
+    from spined import _lib as L
+    lib = L.load()
+    rng = np.random.default_rng(count * 7 + grid)
+    sizes = {16: 201, 18: 675, 20: 2309, 22: 8016, 24: 28968, 26: 100006, 28: 361270}
+    D = [sizes[int(n)] for n in rng.choice(np.arange(16, 29, 2), size=count)]
+    work = [float(d) * 100.0 for d in D]
+    max_ctas = [(d + 31) // 32 for d in D]
+    fixed = 6500.0 * 100.0
+    ng, group_of, ncta, nprob = _layout(lib, work, max_ctas, fixed, grid)
+    assert 1 <= ng <= grid
+    assert sum(ncta) <= grid
+    assert sorted(set(group_of)) == list(range(ng))
+    assert [group_of.count(g) for g in range(ng)] == nprob
+    for g in range(ng):
+        assert ncta[g] >= 1
+        if nprob[g] > 1:
+            assert ncta[g] == 1
+        else:
+            (i,) = [k for k in range(count) if group_of[k] == g]
+            assert ncta[g] <= max_ctas[i]
+    new = _makespan(work, fixed, group_of, ncta)
+    if count <= grid:  # the proportional layout: one CTA each, the rest by work
+        extra = grid - count
+        tot = sum(work)
+        n = [1 + int(w / tot * extra) for w in work]
+        rem = sorted(range(count), key=lambda i: -(w / tot * extra - int(w / tot * extra)) if (w := work[i]) else 0)
+        for i in rem[: grid - sum(n)]:
+            n[i] += 1
+        n = [max(1, min(k, m)) for k, m in zip(n, max_ctas)]
+        old = max(fixed + w / k for w, k in zip(work, n))
+        assert new <= old * (1 + 1e-9), (new, old)
+    # within 1.5x of a bound no layout beats: the largest problem on all the
+    # CTAs it may use, or all the work spread evenly over the grid
+    bound = max(max(fixed + w / min(m, grid) for w, m in zip(work, max_ctas)),
+                sum(w + fixed for w in work) / grid)
+    assert bound * (1 - 1e-9) <= new <= 1.5 * bound, (new, bound)
+
+
+def test_batched_layout_edges(sed):
+    from spined import _lib as L
+    lib = L.load()
+    ng, group_of, ncta, nprob = _layout(lib, [5e6], [1000], 1e3, 304)
+    assert (ng, group_of, ncta, nprob) == (1, [0], [304], [1])
+    ng, group_of, ncta, nprob = _layout(lib, [5e6], [7], 1e3, 304)  # capped by its slices
+    assert (ng, ncta) == (1, [7])
+    ng, group_of, ncta, nprob = _layout(lib, [0.0] * 10, [1] * 10, 0.0, 4)
+    assert 1 <= ng <= 4 and sum(nprob) == 10 and all(c == 1 for c in ncta)
+    assert _layout(lib, [1.0, -1.0], [1, 1], 0.0, 4)[0] == 0
+    assert _layout(lib, [1.0], [1], 0.0, 0)[0] == 0
