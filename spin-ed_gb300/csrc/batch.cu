@@ -61,6 +61,8 @@ struct ChainDesc {
   StreamView S;       // real operator, FP64 stream form
   uint64_t D, n_slices;
   double* V;          // (m_blocks + 1) blocks of [D][4]
+  float* Vs;          // V split into double-float rows (Row4s), for the Gram-Schmidt products
+  float* Xs;          // [D] Row4s: the block under Gram-Schmidt, in double-float
   double* W;          // [D][4]
   double* part;       // [2][ncta][kPart]
   double* W2;         // [D][4] second scratch block (thick restart)
@@ -107,6 +109,57 @@ __device__ __forceinline__ Row4 ldcg4(double const* p) {
   double2 const a = __ldcg(reinterpret_cast<double2 const*>(p));
   double2 const b = __ldcg(reinterpret_cast<double2 const*>(p) + 1);
   return mk4(a.x, a.y, b.x, b.y);
+}
+
+// Double-float arithmetic for the Gram-Schmidt products. A value is carried
+// as hi + lo (two floats), about 48 significant bits. Products and sums use
+// the error-free transformations of double-double arithmetic (TwoProd by
+// FMA; TwoSum, Knuth 1969 and Dekker 1971; as in Hida, Li & Bailey 2001) on
+// the FP32 pipe, which issues about 70 times the FP64 pipe's FMAs on this
+// part. The __f*_rn intrinsics are never contracted into FMAs, which would
+// break the transformations.
+struct alignas(32) Row4s {
+  float4 h, l;  // a [D][4] row: hi parts, then lo parts
+};
+
+__device__ __forceinline__ void df_split(double v, float& h, float& l) {
+  h = __double2float_rn(v);
+  l = __double2float_rn(v - (double)h);
+}
+
+__device__ __forceinline__ Row4s split_row(Row4 const& r) {
+  Row4s o;
+  df_split(r.x, o.h.x, o.l.x);
+  df_split(r.y, o.h.y, o.l.y);
+  df_split(r.z, o.h.z, o.l.z);
+  df_split(r.w, o.h.w, o.l.w);
+  return o;
+}
+
+// (S, E) += (ah + al)(bh + bl): S collects the rounded products exactly (the
+// TwoSum error goes to E), E the product errors and the cross terms; al*bl
+// (below 2^-48 of the product) is dropped.
+__device__ __forceinline__ void df_mac(float ah, float al, float bh, float bl, float& S, float& E) {
+  float const p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  float const s = __fadd_rn(S, p);
+  float const bb = __fsub_rn(s, S);
+  float const err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  S = s;
+  E = __fadd_rn(E, __fadd_rn(err, e));
+}
+
+// (h, l) -= (S + E), renormalised so that |l| <= ulp(h) / 2.
+__device__ __forceinline__ void df_sub(float& h, float& l, float S, float E) {
+  float const s = __fsub_rn(h, S);
+  float const bb = __fsub_rn(s, h);
+  float const err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(-S, bb));
+  float const t = __fadd_rn(err, __fsub_rn(l, E));
+  h = __fadd_rn(s, t);  // TwoSum(s, t): t may exceed s after cancellation
+  float const b2 = __fsub_rn(h, s);
+  l = __fadd_rn(__fsub_rn(s, __fsub_rn(h, b2)), __fsub_rn(t, b2));
 }
 
 // Bounded barrier of the `n` CTAs of a group; false if it timed out (then
@@ -357,26 +410,32 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
 // only (first > 0 where X = H V_{nb-1} is, in exact arithmetic, orthogonal
 // to the older blocks); the second pass always runs against all nb blocks.
 __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, uint32_t first = 0) {
-  double const* V = x.c.V;
+  Row4s const* Vs = reinterpret_cast<Row4s const*>(x.c.Vs);
+  Row4s* Xs = reinterpret_cast<Row4s*>(x.c.Xs);
   uint64_t const D = x.c.D;
   int const K = (int)nb * 16;
   if (C)
     for (int k = threadIdx.x; k < K; k += blockDim.x) C[k] = 0.0;
+  for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x)
+    Xs[r] = split_row(*reinterpret_cast<Row4 const*>(X + r * 4));
   __syncthreads();
   for (int pass = 0; pass < 2; ++pass) {
     uint32_t const i0 = pass == 0 ? first : 0u;
     for (uint32_t i = i0; i < nb; ++i) {
-      double p[16] = {};
-      double const* Vi = V + (uint64_t)i * D * 4;
+      float S[16] = {}, E[16] = {};
+      Row4s const* Vi = Vs + (uint64_t)i * D;
       for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-        Row4 const a = *reinterpret_cast<Row4 const*>(Vi + r * 4);
-        Row4 const w = *reinterpret_cast<Row4 const*>(X + r * 4);
-        double const av[4] = {a.x, a.y, a.z, a.w}, wv[4] = {w.x, w.y, w.z, w.w};
+        Row4s const a = Vi[r], w = Xs[r];
+        float const ah[4] = {a.h.x, a.h.y, a.h.z, a.h.w}, al[4] = {a.l.x, a.l.y, a.l.z, a.l.w};
+        float const wh[4] = {w.h.x, w.h.y, w.h.z, w.h.w}, wl[4] = {w.l.x, w.l.y, w.l.z, w.l.w};
 #pragma unroll
         for (int s = 0; s < 4; ++s)
 #pragma unroll
-          for (int t = 0; t < 4; ++t) p[s * 4 + t] = fma(av[s], wv[t], p[s * 4 + t]);
+          for (int t = 0; t < 4; ++t) df_mac(ah[s], al[s], wh[t], wl[t], S[s * 4 + t], E[s * 4 + t]);
       }
+      double p[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) p[k] = (double)S[k] + (double)E[k];
       cta_sum<16>(p, x.red, x.tmp + 16 * i);
     }
     int Kp = K;
@@ -398,22 +457,54 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
     if (C)
       for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) C[k] += tot[k];
     if (Kp > K && threadIdx.x < 4) norms2[threadIdx.x] = tot[K + threadIdx.x];
+    // the coefficients in double-float, over this CTA's partial sums (no
+    // longer needed once group_sum has returned)
+    float* ch = reinterpret_cast<float*>(x.tmp);
+    float* cl = ch + K;
+    for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) df_split(tot[k], ch[k], cl[k]);
+    __syncthreads();
     // X -= sum_i V_i tot_i
     for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-      Row4 w = *reinterpret_cast<Row4 const*>(X + r * 4);
+      float S[4] = {}, E[4] = {};
       for (uint32_t i = i0; i < nb; ++i) {
-        Row4 const a = *reinterpret_cast<Row4 const*>(V + (uint64_t)i * D * 4 + r * 4);
-        double const* c = tot + 16 * i;
-        w.x -= a.x * c[0] + a.y * c[4] + a.z * c[8] + a.w * c[12];
-        w.y -= a.x * c[1] + a.y * c[5] + a.z * c[9] + a.w * c[13];
-        w.z -= a.x * c[2] + a.y * c[6] + a.z * c[10] + a.w * c[14];
-        w.w -= a.x * c[3] + a.y * c[7] + a.z * c[11] + a.w * c[15];
+        Row4s const a = Vs[(uint64_t)i * D + r];
+        float const ah[4] = {a.h.x, a.h.y, a.h.z, a.h.w}, al[4] = {a.l.x, a.l.y, a.l.z, a.l.w};
+        float4 const* c4h = reinterpret_cast<float4 const*>(ch + 16 * i);
+        float4 const* c4l = reinterpret_cast<float4 const*>(cl + 16 * i);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          float4 const h = c4h[s], l = c4l[s];
+          df_mac(ah[s], al[s], h.x, l.x, S[0], E[0]);
+          df_mac(ah[s], al[s], h.y, l.y, S[1], E[1]);
+          df_mac(ah[s], al[s], h.z, l.z, S[2], E[2]);
+          df_mac(ah[s], al[s], h.w, l.w, S[3], E[3]);
+        }
       }
-      *reinterpret_cast<Row4*>(X + r * 4) = w;
+      Row4s w = Xs[r];
+      df_sub(w.h.x, w.l.x, S[0], E[0]);
+      df_sub(w.h.y, w.l.y, S[1], E[1]);
+      df_sub(w.h.z, w.l.z, S[2], E[2]);
+      df_sub(w.h.w, w.l.w, S[3], E[3]);
+      Xs[r] = w;
     }
     __syncthreads();
   }
+  for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+    Row4s const w = Xs[r];
+    *reinterpret_cast<Row4*>(X + r * 4) = mk4((double)w.h.x + (double)w.l.x, (double)w.h.y + (double)w.l.y,
+                                              (double)w.h.z + (double)w.l.z, (double)w.h.w + (double)w.l.w);
+  }
+  __syncthreads();
   return true;
+}
+
+// Double-float copies (Vs) of basis blocks b0 .. b1, own rows.
+__device__ void split_blocks(Ctx& x, uint32_t b0, uint32_t b1) {
+  Row4s* Vs = reinterpret_cast<Row4s*>(x.c.Vs);
+  for (uint32_t b = b0; b <= b1; ++b)
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x)
+      Vs[(uint64_t)b * x.c.D + r] = split_row(*reinterpret_cast<Row4 const*>(x.c.V + ((uint64_t)b * x.c.D + r) * 4));
+  __syncthreads();
 }
 
 // QR of the new Krylov block X (already projected against V_0 .. V_{nb-1})
@@ -690,6 +781,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
     bool broke = false;
     for (;; ++j) {
       double* Vj = c.V + (uint64_t)j * c.D * 4;
+      split_blocks(x, j == j0 ? 0u : j, j);  // blocks written since the last step (own rows)
       if (!group_barrier(bar, ncta, a)) return;  // V_j complete on every CTA before the gathers
       lap(4);
       block_spmv(x, Vj, c.W);
@@ -1022,7 +1114,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
 
   // Per-problem device arena
   std::vector<uint32_t> m_blocks(count);
-  std::vector<size_t> off_V(count), off_W(count), off_W2(count), off_T(count), off_B(count), off_Y(count), off_out(count);
+  std::vector<size_t> off_V(count), off_Vs(count), off_Xs(count), off_W(count), off_W2(count), off_T(count), off_B(count), off_Y(count), off_out(count);
   size_t total = 0;
   auto take = [&](size_t bytes) {
     size_t const o = total;
@@ -1035,6 +1127,8 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     m = std::max<uint32_t>(m, 1);
     m_blocks[i] = m;
     off_V[i] = take((size_t)(m + 1) * D * kB * 8);
+    off_Vs[i] = take((size_t)(m + 1) * D * kB * 8);  // Row4s: 8 floats a row
+    off_Xs[i] = take((size_t)D * kB * 8);
     off_W[i] = take((size_t)D * kB * 8);
     off_W2[i] = take((size_t)D * kB * 8);
     off_T[i] = take((size_t)kMaxBlocks * kMaxN * 4 * 8);
@@ -1111,6 +1205,8 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     c.D = op.basis->D;
     c.n_slices = op.stream.n_slices;
     c.V = reinterpret_cast<double*>(base + off_V[i]);
+    c.Vs = reinterpret_cast<float*>(base + off_Vs[i]);
+    c.Xs = reinterpret_cast<float*>(base + off_Xs[i]);
     c.W = reinterpret_cast<double*>(base + off_W[i]);
     c.part = reinterpret_cast<double*>(base + off_part[i]);
     c.W2 = reinterpret_cast<double*>(base + off_W2[i]);
