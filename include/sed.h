@@ -323,15 +323,19 @@ SED_API void sed_set_rotate_path(int path);
 
 /* Many Hamiltonians in one persistent launch. No counterpart in the
  * reference, which solves one operator per run. The lowest opts->nev (<= 4)
- * eigenpairs of every operator by block Lanczos with block size 4 in FP64
+ * eigenpairs of every operator by block Lanczos with block size 4
  * (opts->block_size 0 or 4; opts->max_basis / 4 stored blocks per cycle, at
  * most 16, default 12; opts->tol; opts->seed; opts->max_iter bounds the
- * matvec columns per problem). All operators must be real, built and on the
- * current device; their stream forms are recorded if needed. One cooperative
- * kernel solves all of them: its CTAs form groups, one problem per group at a
- * time, with CTAs given in proportion to each problem's work; the launch
- * shape (CTAs per SM) is picked by timing short trial runs on the first call
- * for a given set of sizes (cached afterwards). eigenvalues and residuals are
+ * matvec columns per problem). Vectors, matvec, QR and Rayleigh-Ritz are
+ * FP64; the Gram-Schmidt products run in double-float arithmetic (about 48
+ * significant bits). All operators must be real, built and on the current
+ * device; their stream forms are recorded if needed. One cooperative kernel
+ * solves all of them: its CTAs form groups that solve their problems one
+ * after another; large problems get a group of several CTAs each and small
+ * ones share one-CTA groups, by a cost model of a block step
+ * (sed_debug_batched_layout); the launch shape (threads and CTAs per SM) is
+ * picked by timing short trial runs on the first call for a given set of
+ * sizes (cached afterwards). eigenvalues and residuals are
  * count x nev host arrays (row i for operator i; residuals may be NULL);
  * eigenvectors[i] (host or device, may be NULL, or the array itself NULL) is
  * D_i x nev column-major with stride ldv[i] (ldv NULL: D_i). */

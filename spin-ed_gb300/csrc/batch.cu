@@ -162,6 +162,16 @@ __device__ __forceinline__ void df_sub(float& h, float& l, float S, float E) {
   l = __fadd_rn(__fsub_rn(s, __fsub_rn(h, b2)), __fsub_rn(t, b2));
 }
 
+// row -= (S + E), column by column.
+__device__ __forceinline__ void df_sub_row(Row4s& row, float const (&S)[4], float const (&E)[4]) {
+  Row4s w = row;
+  df_sub(w.h.x, w.l.x, S[0], E[0]);
+  df_sub(w.h.y, w.l.y, S[1], E[1]);
+  df_sub(w.h.z, w.l.z, S[2], E[2]);
+  df_sub(w.h.w, w.l.w, S[3], E[3]);
+  row = w;
+}
+
 // Bounded barrier of the `n` CTAs of a group; false if it timed out (then
 // *error = 2) or another CTA has already reported an error, which ends the
 // wait early. Every thread of the CTA must call it.
@@ -480,12 +490,7 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
           df_mac(ah[s], al[s], h.w, l.w, S[3], E[3]);
         }
       }
-      Row4s w = Xs[r];
-      df_sub(w.h.x, w.l.x, S[0], E[0]);
-      df_sub(w.h.y, w.l.y, S[1], E[1]);
-      df_sub(w.h.z, w.l.z, S[2], E[2]);
-      df_sub(w.h.w, w.l.w, S[3], E[3]);
-      Xs[r] = w;
+      df_sub_row(Xs[r], S, E);
     }
     __syncthreads();
   }
@@ -567,27 +572,34 @@ __device__ bool lanczos_qr(Ctx& x, double* X, uint32_t nb, double* norms2, doubl
 }
 
 // Cyclic Jacobi on the symmetric n x n matrix A (shared, row-major, n even)
-// with parallel round-robin rotations; Q (shared) receives the eigenvectors
-// as columns. Eigenvalues end on the diagonal of A.
+// with parallel round-robin rotations and a threshold: a rotation whose
+// off-diagonal entry is at most 1e-16 of ||A||_F (invariant under the
+// rotations) is skipped, and the sweeps end when one performs none (the
+// eigenvalues then carry errors of order 1e-32 ||A||^2 / gap). Q (shared)
+// receives the eigenvectors as columns. Eigenvalues end on the diagonal of A.
 __device__ void jacobi(double* A, double* Q, int n) {
   __shared__ double cs[kMaxN / 2][2];
   __shared__ int pp[kMaxN / 2][2];
-  __shared__ int done;
-  for (int k = threadIdx.x; k < n * n; k += blockDim.x) Q[k] = (k / n == k % n) ? 1.0 : 0.0;
+  __shared__ double wsum[8];
+  __shared__ double thr;
+  __shared__ int rotated;
+  double f = 0.0;
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+    Q[k] = (k / n == k % n) ? 1.0 : 0.0;
+    f = fma(A[k], A[k], f);
+  }
+  for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = f;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+    thr = 1e-16 * sqrt(t);
+    rotated = 0;
+  }
   __syncthreads();
   int const half = n / 2;
   for (int sweep = 0; sweep < 40; ++sweep) {
-    if (threadIdx.x == 0) {
-      double off = 0.0, dia = 0.0;
-      for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) {
-          if (i == j) dia += A[i * n + j] * A[i * n + j];
-          else off += A[i * n + j] * A[i * n + j];
-        }
-      done = off <= 1e-30 * dia || off == 0.0;
-    }
-    __syncthreads();
-    if (done) break;
     for (int round = 0; round < n - 1; ++round) {
       // round-robin pairing: player 0 fixed, the others rotate
       if ((int)threadIdx.x < half) {
@@ -601,11 +613,13 @@ __device__ void jacobi(double* A, double* Q, int n) {
         }
         double const apq = A[p * n + q];
         double c = 1.0, s = 0.0;
-        if (apq != 0.0) {
+        if (fabs(apq) > thr) {
+          // tan of the angle: the smaller root of t^2 + 2 tau t - 1 = 0
           double const tau = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
-          double const t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-          c = 1.0 / sqrt(1.0 + t * t);
+          double const t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(fma(tau, tau, 1.0)));
+          c = rsqrt(fma(t, t, 1.0));
           s = t * c;
+          if (s != 0.0) rotated = 1;
         }
         cs[k][0] = c;
         cs[k][1] = s;
@@ -616,8 +630,10 @@ __device__ void jacobi(double* A, double* Q, int n) {
       // rows: A <- J^T A
       for (int e = threadIdx.x; e < half * n; e += blockDim.x) {
         int const k = e / n, col = e % n;
+        double const s = cs[k][1];
+        if (s == 0.0) continue;
         int const p = pp[k][0], q = pp[k][1];
-        double const c = cs[k][0], s = cs[k][1];
+        double const c = cs[k][0];
         double const ap = A[p * n + col], aq = A[q * n + col];
         A[p * n + col] = c * ap - s * aq;
         A[q * n + col] = s * ap + c * aq;
@@ -626,8 +642,10 @@ __device__ void jacobi(double* A, double* Q, int n) {
       // columns: A <- A J, Q <- Q J
       for (int e = threadIdx.x; e < half * n; e += blockDim.x) {
         int const k = e / n, row = e % n;
+        double const s = cs[k][1];
+        if (s == 0.0) continue;
         int const p = pp[k][0], q = pp[k][1];
-        double const c = cs[k][0], s = cs[k][1];
+        double const c = cs[k][0];
         double const ap = A[row * n + p], aq = A[row * n + q];
         A[row * n + p] = c * ap - s * aq;
         A[row * n + q] = s * ap + c * aq;
@@ -637,6 +655,11 @@ __device__ void jacobi(double* A, double* Q, int n) {
       }
       __syncthreads();
     }
+    int const any = rotated;
+    __syncthreads();  // every thread has read the flag
+    if (!any) break;
+    if (threadIdx.x == 0) rotated = 0;
+    __syncthreads();
   }
 }
 
@@ -701,25 +724,34 @@ __device__ double rayleigh_ritz(ChainDesc const& c, uint32_t j, bool have_B, dou
 }
 
 // Ritz vectors Psi = V Y over the basis blocks 0..j (own rows): the lowest
-// four into W, the next four into W2 when `both`.
+// four into W, the next four into W2 when `both`. The products run in
+// double-float arithmetic on the split blocks Vs (every block 0..j is split
+// by the time of a restart); Y is split once per call. Ys: shared scratch of
+// at least 4 (j + 1) x 16 doubles.
 __device__ void ritz_vectors(Ctx& x, uint32_t j, double* Ys, bool both) {
   int const n = 4 * (int)(j + 1);
-  for (int e = threadIdx.x; e < n * 8; e += blockDim.x) Ys[e] = ldcg(x.c.Y + e);
+  float* Yh = reinterpret_cast<float*>(Ys);
+  float* Yl = Yh + n * 8;
+  for (int e = threadIdx.x; e < n * 8; e += blockDim.x) df_split(ldcg(x.c.Y + e), Yh[e], Yl[e]);
   __syncthreads();
   uint64_t const D = x.c.D;
+  Row4s const* Vs = reinterpret_cast<Row4s const*>(x.c.Vs);
   for (int half = 0; half < (both ? 2 : 1); ++half) {
     double* out = half ? x.c.W2 : x.c.W;
     for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-      double o[4] = {};
+      float S[4] = {}, E[4] = {};
       for (int b = 0; b <= (int)j; ++b) {
-        Row4 const a = *reinterpret_cast<Row4 const*>(x.c.V + (uint64_t)b * D * 4 + r * 4);
-        double const av[4] = {a.x, a.y, a.z, a.w};
+        Row4s const a = Vs[(uint64_t)b * D + r];
+        float const ah[4] = {a.h.x, a.h.y, a.h.z, a.h.w}, al[4] = {a.l.x, a.l.y, a.l.z, a.l.w};
 #pragma unroll
-        for (int s = 0; s < 4; ++s)
+        for (int s = 0; s < 4; ++s) {
+          int const k = (4 * b + s) * 8 + 4 * half;
 #pragma unroll
-          for (int i = 0; i < 4; ++i) o[i] = fma(av[s], Ys[(4 * b + s) * 8 + 4 * half + i], o[i]);
+          for (int i = 0; i < 4; ++i) df_mac(ah[s], al[s], Yh[k + i], Yl[k + i], S[i], E[i]);
+        }
       }
-      *reinterpret_cast<Row4*>(out + r * 4) = mk4(o[0], o[1], o[2], o[3]);
+      *reinterpret_cast<Row4*>(out + r * 4) = mk4((double)S[0] + (double)E[0], (double)S[1] + (double)E[1],
+                                                  (double)S[2] + (double)E[2], (double)S[3] + (double)E[3]);
     }
   }
   __syncthreads();
@@ -759,11 +791,19 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
   __shared__ double Rb[16], norms2[4];
   uint32_t steps = 0, restarts = 0, matvecs = 0, status = 2;
   double const tol = a.tol;
-  uint64_t tmark = tc::global_ns(), acc[6] = {};
-  auto lap = [&](int phase) {  // leader thread 0 only; others ignore
-    uint64_t const now = tc::global_ns();
-    acc[phase] += now - tmark;
-    tmark = now;
+  // phase timers, kept by thread 0 in shared memory (no registers held
+  // across the phases)
+  __shared__ unsigned long long acc[6], tmark;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 6; ++q) acc[q] = 0;
+    tmark = tc::global_ns();
+  }
+  auto lap = [&](int phase) {
+    if (threadIdx.x == 0) {
+      unsigned long long const now = tc::global_ns();
+      acc[phase] += now - tmark;
+      tmark = now;
+    }
   };
   random_block(x);
   bool qr_ok;

@@ -411,7 +411,8 @@ class BatchResult:
 def eigh_batched(ops: Sequence[Operator], nev: int = 4, tol: float = 1e-8, max_basis: int = 0,
                  seed: int = 1234, max_iter: int = 0, vectors: bool = True) -> BatchResult:
     """Lowest nev (<= 4) eigenpairs of every operator by block Lanczos (block
-    size 4, FP64), all operators in one persistent launch (sed_eigh_batched)."""
+    size 4; FP64 vectors and matvec, double-float Gram-Schmidt products), all
+    operators in one persistent launch (sed_eigh_batched)."""
     count = len(ops)
     opts, _ = eigh_options(nev=nev, tol=tol, max_iter=max_iter, max_basis=max_basis, block_size=4, seed=seed)
     evals = np.zeros((count, nev), dtype=np.float64)

@@ -1,5 +1,6 @@
 """sed_eigh_batched: many J1-J2 chains of uneven size in one persistent
-launch (block Lanczos, block size 4, FP64), against the FP64 oracle.
+launch (block Lanczos, block size 4; FP64 vectors and matvec, double-float
+Gram-Schmidt products), against the FP64 oracle.
 
 Small batches are compared eigenvalue by eigenvalue with dense
 diagonalisations of the oracle's sector matrices (1e-10 relative) and every
