@@ -47,6 +47,8 @@ constexpr int kB = 4;               // block size
 constexpr int kMaxBlocks = 16;      // stored Krylov blocks per cycle (n <= 64)
 constexpr int kMaxN = kB * kMaxBlocks;
 constexpr int kPart = 16 * (kMaxBlocks + 1);  // partial sums per CTA and slot
+constexpr int kGsStages = 4;                   // shared-memory stages of the Gram-Schmidt row streams
+constexpr uint64_t kGsWaitNs = 1000000000ull;  // bound on a wait for one stage's copies (1 s)
 constexpr uint64_t kBarrierNs = 20000000000ull;  // default: 20 s per barrier, far beyond any phase
 // Part of a block step that more CTAs do not shorten, in rows of the mean
 // work per row (the group layout's model). Fitted on 128 J1-J2 chains
@@ -162,6 +164,31 @@ __device__ __forceinline__ void df_sub(float& h, float& l, float S, float E) {
   l = __fadd_rn(__fsub_rn(s, __fsub_rn(h, b2)), __fsub_rn(t, b2));
 }
 
+// (S, E)[s][t] += a_s w_t over one row of a split block a and of X.
+__device__ __forceinline__ void df_dots(Row4s const& a, Row4s const& w, float (&S)[16], float (&E)[16]) {
+  float const ah[4] = {a.h.x, a.h.y, a.h.z, a.h.w}, al[4] = {a.l.x, a.l.y, a.l.z, a.l.w};
+  float const wh[4] = {w.h.x, w.h.y, w.h.z, w.h.w}, wl[4] = {w.l.x, w.l.y, w.l.z, w.l.w};
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+#pragma unroll
+    for (int t = 0; t < 4; ++t) df_mac(ah[s], al[s], wh[t], wl[t], S[s * 4 + t], E[s * 4 + t]);
+}
+
+// (S, E)[t] += sum_s a_s c[s][t] for one split row a and 4 x 4 split
+// coefficients (c4h, c4l: row s as one float4 each).
+__device__ __forceinline__ void df_axpy(Row4s const& a, float4 const* c4h, float4 const* c4l, float (&S)[4],
+                                        float (&E)[4]) {
+  float const ah[4] = {a.h.x, a.h.y, a.h.z, a.h.w}, al[4] = {a.l.x, a.l.y, a.l.z, a.l.w};
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    float4 const h = c4h[s], l = c4l[s];
+    df_mac(ah[s], al[s], h.x, l.x, S[0], E[0]);
+    df_mac(ah[s], al[s], h.y, l.y, S[1], E[1]);
+    df_mac(ah[s], al[s], h.z, l.z, S[2], E[2]);
+    df_mac(ah[s], al[s], h.w, l.w, S[3], E[3]);
+  }
+}
+
 // row -= (S + E), column by column.
 __device__ __forceinline__ void df_sub_row(Row4s& row, float const (&S)[4], float const (&E)[4]) {
   Row4s w = row;
@@ -242,6 +269,9 @@ struct Ctx {
   uint32_t slot;        // partial-sum double buffer
   double* red;          // shared [warps][16]
   double* tmp;          // shared [kPart]
+  double* dyn;          // the dynamic shared area (row-stream stages outside the Jacobi solve)
+  uint64_t* gs_bar;     // shared [kGsStages] mbarriers of the row streams
+  uint32_t* gs_phase;   // parity bit per mbarrier (same value in every thread)
 };
 
 // Publishes this CTA's K partial sums (in shared `local`), waits for the group
@@ -413,6 +443,123 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
   }
 }
 
+// ------------------------------------------- Gram-Schmidt row streams ---
+// The Gram-Schmidt products read the CTA's own rows of split blocks (Vs, Xs)
+// in tiles of 2 blockDim rows, copied into the dynamic shared area by bulk
+// asynchronous copies (one thread issues them; mbarriers count their bytes)
+// a few tiles ahead of the arithmetic, so the loads' latency is hidden
+// behind the products instead of stalling each warp once per row. Waits are
+// bounded (kGsWaitNs): a copy that does not arrive sets the launch's error
+// flag; thread 0 then waits (bounded) for the CTA's copies still in flight
+// and the solve returns.
+
+// Waits for stage barrier q (every thread) and flips its parity.
+__device__ bool gs_wait(Ctx& x, uint32_t q) {
+  bool const ok = tc::mbar_wait(&x.gs_bar[q], (*x.gs_phase >> q) & 1u, kGsWaitNs);
+  *x.gs_phase ^= 1u << q;
+  return ok;
+}
+
+// After a failed wait on barrier `failed` (its parity already flipped):
+// records the error; thread 0 waits (bounded) for the copies still in
+// flight on it and on the barriers in `pending` (bit mask, not yet waited).
+__device__ bool gs_abort(Ctx& x, uint32_t failed, uint32_t pending) {
+  if (threadIdx.x == 0) {
+    atomicExch(x.args->error, 3);
+    tc::mbar_wait(&x.gs_bar[failed], ((*x.gs_phase >> failed) & 1u) ^ 1u, kGsWaitNs);
+    for (uint32_t q = 0; q < (uint32_t)kGsStages; ++q)
+      if (pending & (1u << q)) tc::mbar_wait(&x.gs_bar[q], (*x.gs_phase >> q) & 1u, kGsWaitNs);
+  }
+  for (uint32_t q = 0; q < (uint32_t)kGsStages; ++q)
+    if (pending & (1u << q)) *x.gs_phase ^= 1u << q;
+  return false;
+}
+
+// (S, E) += V_i^T X over own rows (both split): two stages, each a V tile
+// and an X tile.
+__device__ bool gs_dots(Ctx& x, Row4s const* Vi, Row4s const* Xs, float (&S)[16], float (&E)[16]) {
+  uint32_t const TR = 2 * blockDim.x;
+  uint64_t const r0 = x.r0, r1 = x.r1;
+  uint32_t const ntiles = (uint32_t)((r1 - r0 + TR - 1) / TR);
+  Row4s* st = reinterpret_cast<Row4s*>(x.dyn);
+  auto rows_of = [&](uint32_t k) { return (uint32_t)min((uint64_t)TR, r1 - (r0 + (uint64_t)k * TR)); };
+  auto issue = [&](uint32_t k) {
+    uint32_t const q = k & 1u, n = rows_of(k);
+    uint64_t const row = r0 + (uint64_t)k * TR;
+    tc::mbar_expect_tx(&x.gs_bar[q], 2 * n * (uint32_t)sizeof(Row4s));
+    tc::bulk_g2s(st + q * 2 * TR, Vi + row, n * (uint32_t)sizeof(Row4s), &x.gs_bar[q]);
+    tc::bulk_g2s(st + q * 2 * TR + TR, Xs + row, n * (uint32_t)sizeof(Row4s), &x.gs_bar[q]);
+  };
+  tc::fence_proxy_async_smem();  // this thread's shared-memory accesses before the copies' writes
+  __syncthreads();               // the stages' previous readers are done
+  if (threadIdx.x == 0)
+    for (uint32_t k = 0; k < 2 && k < ntiles; ++k) issue(k);
+  for (uint32_t k = 0; k < ntiles; ++k) {
+    uint32_t const q = k & 1u, n = rows_of(k);
+    bool const ok = gs_wait(x, q);
+    if (ok) {
+      Row4s const* sv = st + q * 2 * TR;
+      for (uint32_t r = threadIdx.x; r < n; r += blockDim.x) df_dots(sv[r], sv[TR + r], S, E);
+    }
+    tc::fence_proxy_async_smem();
+    if (__syncthreads_or(!ok)) return gs_abort(x, q, (k + 1 < ntiles ? 1u << ((k + 1) & 1u) : 0u));
+    if (threadIdx.x == 0 && k + 2 < ntiles) issue(k + 2);
+  }
+  return true;
+}
+
+// Xs -= sum_{i0 <= i < nb} V_i C_i over own rows, C_i in double-float in
+// shared memory (ch, cl: 16 per block); the V tiles stream through
+// kGsStages stages, every block of one row tile before the next tile.
+__device__ bool gs_update(Ctx& x, Row4s const* Vs, Row4s* Xs, uint32_t i0, uint32_t nb, float const* ch,
+                          float const* cl) {
+  uint32_t const TR = 2 * blockDim.x;
+  uint64_t const r0 = x.r0, r1 = x.r1, D = x.c.D;
+  uint32_t const ntiles = (uint32_t)((r1 - r0 + TR - 1) / TR);
+  uint32_t const nbb = nb - i0, items = ntiles * nbb;
+  Row4s* st = reinterpret_cast<Row4s*>(x.dyn);
+  auto rows_of = [&](uint32_t k) { return (uint32_t)min((uint64_t)TR, r1 - (r0 + (uint64_t)k * TR)); };
+  auto issue = [&](uint32_t m) {
+    uint32_t const k = m / nbb, i = i0 + m % nbb, q = m % kGsStages, n = rows_of(k);
+    tc::mbar_expect_tx(&x.gs_bar[q], n * (uint32_t)sizeof(Row4s));
+    tc::bulk_g2s(st + q * TR, Vs + (uint64_t)i * D + r0 + (uint64_t)k * TR, n * (uint32_t)sizeof(Row4s),
+                 &x.gs_bar[q]);
+  };
+  tc::fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (uint32_t m = 0; m < (uint32_t)kGsStages && m < items; ++m) issue(m);
+  for (uint32_t k = 0; k < ntiles; ++k) {
+    uint32_t const n = rows_of(k);
+    uint32_t const ra = threadIdx.x, rb = threadIdx.x + blockDim.x;  // the thread's rows of the tile
+    float S0[4] = {}, E0[4] = {}, S1[4] = {}, E1[4] = {};
+    for (uint32_t ii = 0; ii < nbb; ++ii) {
+      uint32_t const m = k * nbb + ii, q = m % kGsStages;
+      bool const ok = gs_wait(x, q);
+      if (ok) {
+        Row4s const* sv = st + q * TR;
+        float4 const* c4h = reinterpret_cast<float4 const*>(ch + 16 * (i0 + ii));
+        float4 const* c4l = reinterpret_cast<float4 const*>(cl + 16 * (i0 + ii));
+        if (ra < n) df_axpy(sv[ra], c4h, c4l, S0, E0);
+        if (rb < n) df_axpy(sv[rb], c4h, c4l, S1, E1);
+      }
+      tc::fence_proxy_async_smem();
+      if (__syncthreads_or(!ok)) {
+        uint32_t pending = 0;
+        for (uint32_t p = m + 1; p < items && p < m + kGsStages; ++p) pending |= 1u << (p % kGsStages);
+        return gs_abort(x, q, pending);
+      }
+      if (threadIdx.x == 0 && m + kGsStages < items) issue(m + kGsStages);
+    }
+    uint64_t const row = r0 + (uint64_t)k * TR;
+    if (ra < n) df_sub_row(Xs[row + ra], S0, E0);
+    if (rb < n) df_sub_row(Xs[row + rb], S1, E1);
+  }
+  tc::fence_proxy_async_global();  // the next pass's streams read Xs
+  __syncthreads();
+  return true;
+}
+
 // X -= sum_{i<nb} V_i C_i (two passes of classical Gram-Schmidt). C (shared,
 // nb * 16, row-major a*4+c per block, may be null) receives the summed
 // coefficients; norms2 (shared, may be null) the squared column norms of X
@@ -428,21 +575,13 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
     for (int k = threadIdx.x; k < K; k += blockDim.x) C[k] = 0.0;
   for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x)
     Xs[r] = split_row(*reinterpret_cast<Row4 const*>(X + r * 4));
+  tc::fence_proxy_async_global();  // the row streams read Xs through the async proxy
   __syncthreads();
   for (int pass = 0; pass < 2; ++pass) {
     uint32_t const i0 = pass == 0 ? first : 0u;
     for (uint32_t i = i0; i < nb; ++i) {
       float S[16] = {}, E[16] = {};
-      Row4s const* Vi = Vs + (uint64_t)i * D;
-      for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-        Row4s const a = Vi[r], w = Xs[r];
-        float const ah[4] = {a.h.x, a.h.y, a.h.z, a.h.w}, al[4] = {a.l.x, a.l.y, a.l.z, a.l.w};
-        float const wh[4] = {w.h.x, w.h.y, w.h.z, w.h.w}, wl[4] = {w.l.x, w.l.y, w.l.z, w.l.w};
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-#pragma unroll
-          for (int t = 0; t < 4; ++t) df_mac(ah[s], al[s], wh[t], wl[t], S[s * 4 + t], E[s * 4 + t]);
-      }
+      if (!gs_dots(x, Vs + (uint64_t)i * D, Xs, S, E)) return false;
       double p[16];
 #pragma unroll
       for (int k = 0; k < 16; ++k) p[k] = (double)S[k] + (double)E[k];
@@ -474,25 +613,7 @@ __device__ bool cgs2(Ctx& x, double* X, uint32_t nb, double* C, double* norms2, 
     for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) df_split(tot[k], ch[k], cl[k]);
     __syncthreads();
     // X -= sum_i V_i tot_i
-    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
-      float S[4] = {}, E[4] = {};
-      for (uint32_t i = i0; i < nb; ++i) {
-        Row4s const a = Vs[(uint64_t)i * D + r];
-        float const ah[4] = {a.h.x, a.h.y, a.h.z, a.h.w}, al[4] = {a.l.x, a.l.y, a.l.z, a.l.w};
-        float4 const* c4h = reinterpret_cast<float4 const*>(ch + 16 * i);
-        float4 const* c4l = reinterpret_cast<float4 const*>(cl + 16 * i);
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          float4 const h = c4h[s], l = c4l[s];
-          df_mac(ah[s], al[s], h.x, l.x, S[0], E[0]);
-          df_mac(ah[s], al[s], h.y, l.y, S[1], E[1]);
-          df_mac(ah[s], al[s], h.z, l.z, S[2], E[2]);
-          df_mac(ah[s], al[s], h.w, l.w, S[3], E[3]);
-        }
-      }
-      df_sub_row(Xs[r], S, E);
-    }
-    __syncthreads();
+    if (!gs_update(x, Vs, Xs, i0, nb, ch, cl)) return false;
   }
   for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
     Row4s const w = Xs[r];
@@ -509,6 +630,7 @@ __device__ void split_blocks(Ctx& x, uint32_t b0, uint32_t b1) {
   for (uint32_t b = b0; b <= b1; ++b)
     for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x)
       Vs[(uint64_t)b * x.c.D + r] = split_row(*reinterpret_cast<Row4 const*>(x.c.V + ((uint64_t)b * x.c.D + r) * 4));
+  tc::fence_proxy_async_global();
   __syncthreads();
 }
 
@@ -780,8 +902,9 @@ __device__ void random_block(Ctx& x) {
 // as diag(theta_1..8) and the next step's projections supply the arrowhead
 // couplings), or, after a breakdown, the lowest four alone (explicit restart).
 __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, uint32_t* bar, BatchArgs const& a,
-                            double* red, double* tmp, double* C, double* A, double* Q) {
-  Ctx x{c, rank, ncta, bar, &a, 0, 0, 0, 0, 0, red, tmp};
+                            double* red, double* tmp, double* C, double* A, double* Q, uint64_t* gs_bar,
+                            uint32_t* gs_phase) {
+  Ctx x{c, rank, ncta, bar, &a, 0, 0, 0, 0, 0, red, tmp, A, gs_bar, gs_phase};
   x.s0 = c.n_slices * rank / ncta;
   x.s1 = c.n_slices * (rank + 1) / ncta;
   x.r0 = std::min<uint64_t>(c.D, x.s0 * 32);
@@ -932,12 +1055,19 @@ __global__ void __launch_bounds__(256, 2) k_batch_lanczos(BatchArgs a) {
   __shared__ double tmp[2 * kPart];
   __shared__ double C[kPart];
   extern __shared__ double dyn[];  // A [kMaxN^2], Q [kMaxN^2] (leader work)
+  __shared__ uint64_t gs_bar[kGsStages];
+  uint32_t gs_phase = 0;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < kGsStages; ++q) tc::mbar_init(&gs_bar[q], 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
   uint32_t const gi = a.cta_group[blockIdx.x];
   GroupDesc const g = a.groups[gi];
   uint32_t const rank = blockIdx.x - g.cta0;
   for (uint32_t q = 0; q < g.count; ++q) {
     ChainDesc const& c = a.chains[a.order[g.first + q]];
-    solve_chain(c, rank, g.ncta, g.bar, a, red, tmp, C, dyn, dyn + kMaxN * kMaxN);
+    solve_chain(c, rank, g.ncta, g.bar, a, red, tmp, C, dyn, dyn + kMaxN * kMaxN, gs_bar, &gs_phase);
     if (*(volatile int*)a.error) return;
     if (!group_barrier(g.bar, g.ncta, a)) return;
   }
@@ -1304,7 +1434,8 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     cudaEventDestroy(e1);
     SED_TRY_CUDA(le);
     SED_TRY_CUDA(se);
-    if (err) return fail(LS_DEVICE_TIMEOUT, "sed_eigh_batched: a group barrier timed out");
+    if (err) return fail(LS_DEVICE_TIMEOUT, err == 3 ? "sed_eigh_batched: a wait for a shared-memory copy timed out"
+                                                    : "sed_eigh_batched: a group barrier timed out");
     return LS_SUCCESS;
   };
 

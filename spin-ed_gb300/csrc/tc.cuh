@@ -100,6 +100,11 @@ __device__ __forceinline__ void tma_prefetch_map(void const* map) {
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// Makes this thread's generic-proxy writes to global memory visible to later
+// bulk copies (async proxy) that read them.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
 
 // ------------------------------------------------------------- tcgen05 ---
 // Allocation of `ncols` TMEM columns (a power of two >= 32) by one whole warp;
