@@ -189,6 +189,16 @@ __device__ __forceinline__ void df_axpy(Row4s const& a, float4 const* c4h, float
   }
 }
 
+// (h, l) = (ah + al)(bh + bl), renormalised (al bl dropped).
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& h, float& l) {
+  float const p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  h = __fadd_rn(p, e);
+  l = __fsub_rn(e, __fsub_rn(h, p));
+}
+
 // row -= (S + E), column by column.
 __device__ __forceinline__ void df_sub_row(Row4s& row, float const (&S)[4], float const (&E)[4]) {
   Row4s w = row;
@@ -384,6 +394,103 @@ __device__ bool block_qr(Ctx& x, double* X, double* Rtot, bool& ok) {
     }
     __syncthreads();
   }
+  return true;
+}
+
+// CholQR2 of the block X in double-float: on entry Xs holds X split (as
+// cgs2 leaves it); the Gram matrices and X R^{-1} run on the split rows, and
+// on exit X (FP64) and the split copy Vs_out (may be null) hold the factor Q.
+// Rtot (shared, 16) = R2 R1; false on breakdown or barrier failure (ok
+// distinguishes them).
+__device__ bool block_qr_df(Ctx& x, double* X, Row4s* Vs_out, double* Rtot, bool& ok) {
+  __shared__ double G[16], R[16], P[16];
+  __shared__ float Rh[16], Rl[16];
+  Row4s* Xs = reinterpret_cast<Row4s*>(x.c.Xs);
+  ok = true;
+  for (int pass = 0; pass < 2; ++pass) {
+    float S[10] = {}, E[10] = {};
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      Row4s const v = Xs[r];
+      float const ah[4] = {v.h.x, v.h.y, v.h.z, v.h.w}, al[4] = {v.l.x, v.l.y, v.l.z, v.l.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i; j < 4; ++j) {
+          int const q = i * 4 - i * (i - 1) / 2 + (j - i);  // packed upper triangle
+          df_mac(ah[i], al[i], ah[j], al[j], S[q], E[q]);
+        }
+    }
+    double g[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) g[q] = (double)S[q] + (double)E[q];
+    cta_sum<10>(g, x.red, x.tmp);
+    if (!group_sum(x, x.tmp, 10, x.tmp + 16)) {
+      ok = false;
+      return false;
+    }
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < 4; ++i)
+        for (int j = i; j < 4; ++j) {
+          int const q = i * 4 - i * (i - 1) / 2 + (j - i);
+          G[i * 4 + j] = G[j * 4 + i] = x.tmp[16 + q];
+        }
+    }
+    __syncthreads();
+    __shared__ int good;
+    if (threadIdx.x == 0) {
+      good = chol4(G, R) ? 1 : 0;
+      if (good) {
+        // R's off-diagonal entries and the reciprocals of its diagonal, split
+        for (int i = 0; i < 16; ++i) {
+          double const v = (i % 5 == 0) ? 1.0 / R[i] : R[i];
+          df_split(v, Rh[i], Rl[i]);
+        }
+      }
+    }
+    __syncthreads();
+    if (!good) return false;
+    // X <- X R^{-1}: y_j = (x_j - sum_{k<j} y_k R_kj) / R_jj
+    for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+      Row4s const v = Xs[r];
+      float yh[4] = {v.h.x, v.h.y, v.h.z, v.h.w}, yl[4] = {v.l.x, v.l.y, v.l.z, v.l.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int k = 0; k < j; ++k) {
+          float ph, pl;
+          df_mul(yh[k], yl[k], Rh[k * 4 + j], Rl[k * 4 + j], ph, pl);
+          df_sub(yh[j], yl[j], ph, pl);
+        }
+        df_mul(yh[j], yl[j], Rh[j * 5], Rl[j * 5], yh[j], yl[j]);
+      }
+      Row4s o;
+      o.h = make_float4(yh[0], yh[1], yh[2], yh[3]);
+      o.l = make_float4(yl[0], yl[1], yl[2], yl[3]);
+      Xs[r] = o;
+    }
+    if (threadIdx.x == 0) {
+      if (pass == 0) {
+        for (int i = 0; i < 16; ++i) Rtot[i] = R[i];
+      } else {  // Rtot = R2 * R1
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += R[i * 4 + k] * Rtot[k * 4 + j];
+            P[i * 4 + j] = s;
+          }
+        for (int i = 0; i < 16; ++i) Rtot[i] = P[i];
+      }
+    }
+    __syncthreads();
+  }
+  for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += blockDim.x) {
+    Row4s const w = Xs[r];
+    *reinterpret_cast<Row4*>(X + r * 4) = mk4((double)w.h.x + (double)w.l.x, (double)w.h.y + (double)w.l.y,
+                                              (double)w.h.z + (double)w.l.z, (double)w.h.w + (double)w.l.w);
+    if (Vs_out) Vs_out[r] = w;
+  }
+  tc::fence_proxy_async_global();  // Vs_out is read by the row streams
+  __syncthreads();
   return true;
 }
 
@@ -683,7 +790,8 @@ __device__ bool lanczos_qr(Ctx& x, double* X, uint32_t nb, double* norms2, doubl
     if (!cgs2(x, X, nb, nullptr, nullptr)) return false;
   }
   bool ok;
-  if (!block_qr(x, X, R, ok)) return false;  // dependent columns that are not small: a breakdown
+  // dependent columns that are not small: a breakdown
+  if (!block_qr_df(x, X, reinterpret_cast<Row4s*>(x.c.Vs) + (uint64_t)nb * x.c.D, R, ok)) return false;
   if (threadIdx.x < 16) {
     int const col = threadIdx.x & 3;
     Rb[threadIdx.x] = (total_mask_s & (1 << col)) ? 0.0 : R[threadIdx.x];
@@ -944,7 +1052,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
     bool broke = false;
     for (;; ++j) {
       double* Vj = c.V + (uint64_t)j * c.D * 4;
-      split_blocks(x, j == j0 ? 0u : j, j);  // blocks written since the last step (own rows)
+      if (j == j0) split_blocks(x, 0u, j0);  // later blocks come split from the QR of each step
       if (!group_barrier(bar, ncta, a)) return;  // V_j complete on every CTA before the gathers
       lap(4);
       block_spmv(x, Vj, c.W);
@@ -1052,9 +1160,9 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
 
 __global__ void __launch_bounds__(256, 2) k_batch_lanczos(BatchArgs a) {
   __shared__ double red[8 * 16];
-  __shared__ double tmp[2 * kPart];
+  __shared__ __align__(16) double tmp[2 * kPart];  // also read as float4 (split Gram-Schmidt coefficients)
   __shared__ double C[kPart];
-  extern __shared__ double dyn[];  // A [kMaxN^2], Q [kMaxN^2] (leader work)
+  extern __shared__ __align__(128) double dyn[];  // A [kMaxN^2], Q [kMaxN^2] (leader work); row-stream stages
   __shared__ uint64_t gs_bar[kGsStages];
   uint32_t gs_phase = 0;
   if (threadIdx.x == 0) {
