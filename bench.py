@@ -628,11 +628,13 @@ def main():
     ap.add_argument("--once", action="store_true", help="one solve, no timing (for profilers)")
     ap.add_argument("--hamming-weight", type=int, default=None, help="sector override for --once")
     ap.add_argument("--max-basis", type=int, default=0, help="stored Krylov vectors for --once (<= 32: thick restart)")
-    ap.add_argument("--profile-case", default=None, choices=["mlp", "train", "record", "batch16", "spmv", "rotate"],
+    ap.add_argument("--profile-case", default=None,
+                    choices=["mlp", "train", "record", "batch16", "batch128", "spmv", "rotate"],
                     help="one small run of a single kernel family, for profilers: the tensor-core MLP "
                          "inference over 2^20 random 36-spin states, one tensor-core training epoch (2^18 "
                          "samples, 64 batches of 4096), the chain-32 stream form recorded by "
-                         "canonicalisation, a 16-chain batched solve (one fixed launch shape), 10 "
+                         "canonicalisation, a 16-chain batched solve (one fixed launch shape), the 128-chain "
+                         "batched workload with the library's per-problem phase timers logged to stderr, 10 "
                          "matvecs of the 6x6 stream form (about 3.5 GB on the device), or the thick-restart "
                          "basis rotation on 1e8 rows on both paths (--rotate-rows to change)")
     ap.add_argument("--rotate-rows", type=int, default=100_000_000)
@@ -729,6 +731,22 @@ def main():
             del V, Y
             torch.cuda.empty_cache()
         print(json.dumps(out))
+        return
+    if args.profile_case == "batch128":
+        from spined import internal as I, lattices
+        from spined.model import build_model
+        from spined import _lib as L
+        ops = [build_model(m).hamiltonian for m in lattices.j1j2_chains(128, seed=2024)]
+        for op in ops:
+            op.prepare(L.SED_FORM_STREAM)
+        I.eigh_batched(ops, nev=4, vectors=False)  # launch-shape trials
+        L.load().ls_enable_logging()
+        try:
+            r = I.eigh_batched(ops, nev=4, vectors=False)
+        finally:
+            L.load().ls_disable_logging()
+        print(json.dumps({"case": "batch128", "kernel_ms": r.kernel_ms, "ctas_per_sm": r.ctas_per_sm,
+                          "block_steps_max": r.block_steps_max, "max_residual": float(r.residuals.max())}))
         return
     if args.profile_case == "batch16":
         from spined import internal as I, lattices
