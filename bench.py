@@ -393,7 +393,8 @@ def batched_arm():
     torch.cuda.synchronize()
     t_serial = time.perf_counter() - t0
     dims = [I.get_number_states(x.basis) for x in built]
-    return {"workload": "128 J1-J2 chains, N in 16..28, lowest 4 eigenpairs, block Lanczos (block 4, FP64)",
+    return {"workload": "128 J1-J2 chains, N in 16..28, lowest 4 eigenpairs, block Lanczos (block 4; FP64 vectors "
+                        "and matvec, double-float Gram-Schmidt)",
             "sum_D": int(sum(dims)), "max_D": int(max(dims)), "setup_s": t_setup, "batched_s": t_batch,
             "kernel_ms": res.kernel_ms, "ctas_per_sm": res.ctas_per_sm, "grid": res.grid,
             "block_steps_max": res.block_steps_max, "max_residual": float(res.residuals.max()),

@@ -293,9 +293,9 @@ SED_API int sed_operator_time_matvec(ls_operator const* op, void const* x, void*
  * to finish before it returns, so `out` holds the results on return. Partial
  * sums live in a 66 KiB scratch array in the library's static device memory
  * (held on every GPU that loads the library until exit) and shared by all
- * calls: calls that overlap on the GPU race on it. The first call on each
- * device looks up the scratch address (cudaGetSymbolAddress), so make that
- * first call before any stream capture. */
+ * calls: calls that overlap on the GPU race on it. Because the call
+ * synchronises with `stream` before it returns, it cannot be captured in a
+ * CUDA graph. */
 SED_API int sed_operator_expectation_noalloc(ls_operator const* op, int dtype, uint64_t size,
                                              uint64_t block_size, void const* x, uint64_t x_stride,
                                              void* y, uint64_t y_stride, void* out, void* stream);
