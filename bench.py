@@ -246,7 +246,7 @@ def gpu_arm(args, rank, world, dist):
     }
 
 
-# --------------------------------------------------- spec forms --
+# ------------------------------------------ solver forms on the 6x6 lattice --
 
 # the learned start's network: 36 -> 256 -> 256 -> 2 trained on the tensor cores for 96 epochs
 # (the best time to solution measured over hidden 128/256/512 and 32/96 epochs)
