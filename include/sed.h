@@ -464,8 +464,8 @@ SED_API uint64_t sed_device_memory_in_use(void);
 
 /* Bound on every wait inside libsed kernels that wait on other threads or
  * blocks: the group barriers of sed_eigh_batched's persistent kernel (20 s by
- * default) and the tensor-core MLP kernel's waits on its copies and MMAs (1 s
- * by default). A wait that runs out sets an error flag, the kernel drains
+ * default) and its waits for shared-memory copies (1 s by default), and the
+ * tensor-core kernels' waits on their copies and MMAs (1 s by default). A wait that runs out sets an error flag, the kernel drains
  * and returns, and the call fails with LS_DEVICE_TIMEOUT; the CUDA context
  * stays usable. seconds <= 0 restores the defaults. Process-wide. */
 SED_API void sed_set_device_wait_limit(double seconds);

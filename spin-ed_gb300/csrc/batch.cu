@@ -49,7 +49,7 @@ constexpr int kMaxBlocks = 16;      // stored Krylov blocks per cycle (n <= 64)
 constexpr int kMaxN = kB * kMaxBlocks;
 constexpr int kPart = 16 * (kMaxBlocks + 1);  // partial sums per CTA and slot
 constexpr int kGsStages = 4;                   // shared-memory stages of the Gram-Schmidt row streams
-constexpr uint64_t kGsWaitNs = 1000000000ull;  // bound on a wait for one stage's copies (1 s)
+constexpr uint64_t kGsWaitNs = 1000000000ull;  // default bound on a wait for one stage's copies (1 s)
 constexpr uint64_t kBarrierNs = 20000000000ull;  // default: 20 s per barrier, far beyond any phase
 // Part of a block step that more CTAs do not shorten, in rows of the mean
 // work per row (the group layout's model). Fitted on 128 J1-J2 chains
@@ -97,6 +97,7 @@ struct BatchArgs {
   uint32_t rr_every;
   int* error;
   uint64_t wait_ns;        // bound on every barrier wait
+  uint64_t copy_wait_ns;   // bound on every wait for a row-stream stage's copies
   uint32_t extra_arrivals; // arrivals a barrier waits for beyond its CTAs (0; see sed_debug_barrier_extra_arrivals)
 };
 
@@ -510,13 +511,13 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
 // asynchronous copies (one thread issues them; mbarriers count their bytes)
 // a few tiles ahead of the arithmetic, so the loads' latency is hidden
 // behind the products instead of stalling each warp once per row. Waits are
-// bounded (kGsWaitNs): a copy that does not arrive sets the launch's error
+// bounded (copy_wait_ns): a copy that does not arrive sets the launch's error
 // flag; thread 0 then waits (bounded) for the CTA's copies still in flight
 // and the solve returns.
 
 // Waits for stage barrier q (every thread) and flips its parity.
 __device__ bool gs_wait(Ctx& x, uint32_t q) {
-  bool const ok = tc::mbar_wait(&x.gs_bar[q], (*x.gs_phase >> q) & 1u, kGsWaitNs);
+  bool const ok = tc::mbar_wait(&x.gs_bar[q], (*x.gs_phase >> q) & 1u, x.args->copy_wait_ns);
   *x.gs_phase ^= 1u << q;
   return ok;
 }
@@ -527,9 +528,9 @@ __device__ bool gs_wait(Ctx& x, uint32_t q) {
 __device__ bool gs_abort(Ctx& x, uint32_t failed, uint32_t pending) {
   if (threadIdx.x == 0) {
     atomicExch(x.args->error, 3);
-    tc::mbar_wait(&x.gs_bar[failed], ((*x.gs_phase >> failed) & 1u) ^ 1u, kGsWaitNs);
+    tc::mbar_wait(&x.gs_bar[failed], ((*x.gs_phase >> failed) & 1u) ^ 1u, x.args->copy_wait_ns);
     for (uint32_t q = 0; q < (uint32_t)kGsStages; ++q)
-      if (pending & (1u << q)) tc::mbar_wait(&x.gs_bar[q], (*x.gs_phase >> q) & 1u, kGsWaitNs);
+      if (pending & (1u << q)) tc::mbar_wait(&x.gs_bar[q], (*x.gs_phase >> q) & 1u, x.args->copy_wait_ns);
   }
   for (uint32_t q = 0; q < (uint32_t)kGsStages; ++q)
     if (pending & (1u << q)) *x.gs_phase ^= 1u << q;
@@ -1478,6 +1479,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     a.rr_every = 4;  // measured on the 128-chain workload: 772 ms against 797 ms every 2 steps, same step counts
     a.error = reinterpret_cast<int*>(base + off_err);
     a.wait_ns = device_wait_ns(kBarrierNs);
+    a.copy_wait_ns = device_wait_ns(kGsWaitNs);
     a.extra_arrivals = g_barrier_extra_arrivals.load();
     cudaEvent_t e0, e1;
     SED_TRY_CUDA(cudaEventCreate(&e0));
