@@ -66,6 +66,7 @@ struct ChainDesc {
   double* V;          // (m_blocks + 1) blocks of [D][4]
   float* Vs;          // V split into double-float rows (Row4s), for the Gram-Schmidt products
   float* Xs;          // [D] Row4s: the block under Gram-Schmidt, in double-float
+  float2* table_s;    // [n_codes]: the matrix-element table split into double-float (k_split_tables)
   double* W;          // [D][4]
   double* part;       // [2][ncta][kPart]
   double* W2;         // [D][4] second scratch block (thick restart)
@@ -622,6 +623,76 @@ __device__ bool gs_update(Ctx& x, Row4s const* Vs, Row4s* Xs, uint32_t i0, uint3
   return true;
 }
 
+// W = H V_j on own rows from the split copy of V_j (Vs block j, complete on
+// every CTA): each element's product t x_c is formed and summed in
+// double-float (df.cuh) with the split table, so the FP64 pipe only runs the
+// row epilogue y = d x + a / sqrt(S_i). Same gathers (one 32-byte row per
+// element) and slot scheme as block_spmv.
+__device__ void block_spmv_df(Ctx& x, uint32_t j, double* W) {
+  StreamView const& S = x.c.S;
+  uint32_t const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t const col_mask = S.col_bits < 32 ? ((1u << S.col_bits) - 1u) : 0xFFFFFFFFu;
+  bool const packed = x.c.packed != 0;
+  float2 const* table = x.c.table_s;
+  Row4s const* Xs = reinterpret_cast<Row4s const*>(x.c.Vs) + (uint64_t)j * x.c.D;
+  double const* X = x.c.V + (uint64_t)j * x.c.D * 4;
+  for (uint64_t s = x.s0 + warp; s < x.s1; s += nw) {
+    uint64_t const base = S.slice_ptr[s];
+    uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
+    float Sa[4] = {}, Ea[4] = {};
+    uint32_t const* ent = S.entries + base + lane;
+    // the next step's entries are loaded while this step's gathers are in
+    // flight (with 16 warps per SM, the entry load and the gather would
+    // otherwise be two exposed latencies per step)
+    uint32_t v[kBlockSpmvU];
+#pragma unroll
+    for (int u = 0; u < kBlockSpmvU; ++u) v[u] = (uint32_t)u < width ? __ldcs(ent + (uint64_t)u * 32) : kNull;
+    for (uint32_t e0 = 0; e0 < width; e0 += kBlockSpmvU) {
+      uint32_t vn[kBlockSpmvU];
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u)
+        vn[u] = e0 + kBlockSpmvU + u < width ? __ldcs(ent + (uint64_t)(e0 + kBlockSpmvU + u) * 32) : kNull;
+      float2 t[kBlockSpmvU];
+      float4 gh[kBlockSpmvU], gl[kBlockSpmvU];
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u) {
+        if (v[u] != kNull) {
+          uint32_t const col = v[u] & col_mask;
+          uint32_t const code =
+              packed ? (v[u] >> S.col_bits) : (uint32_t)__ldcs(S.codes + base + lane + (uint64_t)(e0 + u) * 32);
+          t[u] = __ldg(table + code);
+          float4 const* row = reinterpret_cast<float4 const*>(Xs + col);
+          gh[u] = __ldcg(row);
+          gl[u] = __ldcg(row + 1);
+        } else {
+          t[u] = make_float2(0.0f, 0.0f);
+          gh[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          gl[u] = gh[u];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u) {
+        df_mac(t[u].x, t[u].y, gh[u].x, gl[u].x, Sa[0], Ea[0]);
+        df_mac(t[u].x, t[u].y, gh[u].y, gl[u].y, Sa[1], Ea[1]);
+        df_mac(t[u].x, t[u].y, gh[u].z, gl[u].z, Sa[2], Ea[2]);
+        df_mac(t[u].x, t[u].y, gh[u].w, gl[u].w, Sa[3], Ea[3]);
+      }
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u) v[u] = vn[u];
+    }
+    uint64_t const i = s * 32 + lane;
+    if (i < x.c.D) {
+      double const f = S.inv_sqrt_s[S.row_class[i]];
+      double const dg = static_cast<double const*>(S.diag)[i];
+      Row4 const xi = ldcg4(X + i * 4);
+      *reinterpret_cast<Row4*>(W + i * 4) = mk4(fma(f, (double)Sa[0] + (double)Ea[0], dg * xi.x),
+                                                fma(f, (double)Sa[1] + (double)Ea[1], dg * xi.y),
+                                                fma(f, (double)Sa[2] + (double)Ea[2], dg * xi.z),
+                                                fma(f, (double)Sa[3] + (double)Ea[3], dg * xi.w));
+    }
+  }
+}
+
 // X -= sum_{i<nb} V_i C_i (two passes of classical Gram-Schmidt). C (shared,
 // nb * 16, row-major a*4+c per block, may be null) receives the summed
 // coefficients; norms2 (shared, may be null) the squared column norms of X
@@ -1010,7 +1081,7 @@ __device__ void solve_chain(ChainDesc const& c, uint32_t rank, uint32_t ncta, ui
       if (j == j0) split_blocks(x, 0u, j0);  // later blocks come split from the QR of each step
       if (!group_barrier(bar, ncta, a)) return;  // V_j complete on every CTA before the gathers
       lap(4);
-      block_spmv(x, Vj, c.W);
+      block_spmv_df(x, j, c.W);
       ++matvecs;
       __syncthreads();
       lap(0);
@@ -1133,6 +1204,18 @@ __global__ void __launch_bounds__(256, 2) k_batch_lanczos(BatchArgs a) {
     solve_chain(c, rank, g.ncta, g.bar, a, red, tmp, C, dyn, dyn + kMaxN * kMaxN, gs_bar, &gs_phase);
     if (*(volatile int*)a.error) return;
     if (!group_barrier(g.bar, g.ncta, a)) return;
+  }
+}
+
+// chains[blockIdx.y].table_s = its FP64 matrix-element table split into
+// double-float pairs.
+__global__ void k_split_tables(ChainDesc const* __restrict__ chains) {
+  ChainDesc const& c = chains[blockIdx.y];
+  double const* t = static_cast<double const*>(c.S.table);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < c.S.n_codes; k += gridDim.x * blockDim.x) {
+    float h, l;
+    df_split(t[k], h, l);
+    c.table_s[k] = make_float2(h, l);
   }
 }
 
@@ -1347,7 +1430,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
 
   // Per-problem device arena
   std::vector<uint32_t> m_blocks(count);
-  std::vector<size_t> off_V(count), off_Vs(count), off_Xs(count), off_W(count), off_W2(count), off_T(count), off_B(count), off_Y(count), off_out(count);
+  std::vector<size_t> off_V(count), off_Vs(count), off_Xs(count), off_Ts(count), off_W(count), off_W2(count), off_T(count), off_B(count), off_Y(count), off_out(count);
   size_t total = 0;
   auto take = [&](size_t bytes) {
     size_t const o = total;
@@ -1362,6 +1445,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     off_V[i] = take((size_t)(m + 1) * D * kB * 8);
     off_Vs[i] = take((size_t)(m + 1) * D * kB * 8);  // Row4s: 8 floats a row
     off_Xs[i] = take((size_t)D * kB * 8);
+    off_Ts[i] = take((size_t)std::max<uint32_t>(1, od[i]->tables->n_codes) * sizeof(float2));
     off_W[i] = take((size_t)D * kB * 8);
     off_W2[i] = take((size_t)D * kB * 8);
     off_T[i] = take((size_t)kMaxBlocks * kMaxN * 4 * 8);
@@ -1440,6 +1524,7 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     c.V = reinterpret_cast<double*>(base + off_V[i]);
     c.Vs = reinterpret_cast<float*>(base + off_Vs[i]);
     c.Xs = reinterpret_cast<float*>(base + off_Xs[i]);
+    c.table_s = reinterpret_cast<float2*>(base + off_Ts[i]);
     c.W = reinterpret_cast<double*>(base + off_W[i]);
     c.part = reinterpret_cast<double*>(base + off_part[i]);
     c.W2 = reinterpret_cast<double*>(base + off_W2[i]);
@@ -1456,6 +1541,13 @@ int sed_eigh_batched(unsigned count, ls_operator* const ops[], sed_eigh_options 
     c.seed = o.seed + 0x9E3779B97F4A7C15ull * (i + 1);
   }
   SED_TRY_CUDA(cudaMemcpyAsync(base + off_chains, chains.data(), sizeof(ChainDesc) * count, cudaMemcpyHostToDevice, stream));
+  {
+    uint32_t max_codes = 1;
+    for (unsigned i = 0; i < count; ++i) max_codes = std::max(max_codes, od[i]->tables->n_codes);
+    k_split_tables<<<dim3((max_codes + 255) / 256, count), 256, 0, stream>>>(
+        reinterpret_cast<ChainDesc const*>(base + off_chains));
+    note_launches(1);
+  }
 
   uint32_t const max_steps_total = o.max_iter ? std::max<uint32_t>(1, o.max_iter / kB) : 2000;
   auto run = [&](Plan const& p, uint32_t max_steps, float* ms) -> int {
