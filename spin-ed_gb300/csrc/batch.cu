@@ -464,13 +464,17 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
     uint32_t const width = (uint32_t)((S.slice_ptr[s + 1] - base) >> 5);
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     uint32_t const* ent = S.entries + base + lane;
-    // kBlockSpmvU slots per step: their entry loads, then their gathers, then
-    // the FMAs in slot order (the same order as one slot at a time), so
-    // several gathers are in flight per lane
-    for (uint32_t e0 = 0; e0 < width; e0 += kBlockSpmvU) {
-      uint32_t v[kBlockSpmvU];
+    // kBlockSpmvU slots per step: their entry loads (issued one step ahead),
+    // then their gathers, then the FMAs in slot order (the same order as one
+    // slot at a time), so several gathers are in flight per lane
+    uint32_t v[kBlockSpmvU];
 #pragma unroll
-      for (int u = 0; u < kBlockSpmvU; ++u) v[u] = e0 + u < width ? __ldcs(ent + (uint64_t)(e0 + u) * 32) : kNull;
+    for (int u = 0; u < kBlockSpmvU; ++u) v[u] = (uint32_t)u < width ? __ldcs(ent + (uint64_t)u * 32) : kNull;
+    for (uint32_t e0 = 0; e0 < width; e0 += kBlockSpmvU) {
+      uint32_t vn[kBlockSpmvU];
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u)
+        vn[u] = e0 + kBlockSpmvU + u < width ? __ldcs(ent + (uint64_t)(e0 + kBlockSpmvU + u) * 32) : kNull;
       double t[kBlockSpmvU];
       Row4 xv[kBlockSpmvU];
 #pragma unroll
@@ -494,6 +498,8 @@ __device__ void block_spmv(Ctx& x, double const* X, double* W) {
         a2 = fma(t[u], xv[u].z, a2);
         a3 = fma(t[u], xv[u].w, a3);
       }
+#pragma unroll
+      for (int u = 0; u < kBlockSpmvU; ++u) v[u] = vn[u];
     }
     uint64_t const i = s * 32 + lane;
     if (i < x.c.D) {
@@ -643,7 +649,8 @@ __device__ void block_spmv_df(Ctx& x, uint32_t j, double* W) {
     uint32_t const* ent = S.entries + base + lane;
     // the next step's entries are loaded while this step's gathers are in
     // flight (with 16 warps per SM, the entry load and the gather would
-    // otherwise be two exposed latencies per step)
+    // otherwise be two exposed latencies per step; two steps ahead measured
+    // the same)
     uint32_t v[kBlockSpmvU];
 #pragma unroll
     for (int u = 0; u < kBlockSpmvU; ++u) v[u] = (uint32_t)u < width ? __ldcs(ent + (uint64_t)u * 32) : kNull;
