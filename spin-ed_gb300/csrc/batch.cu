@@ -1,12 +1,15 @@
 // batch.cu — many Hamiltonians of uneven size solved in one persistent launch
 // (sed_eigh_batched): the lowest nev <= 4 eigenpairs of every operator by
-// block Lanczos with block size 4 in FP64.
+// block Lanczos with block size 4. Vectors are stored in FP64; the products
+// of the block SpMV, the Gram-Schmidt passes, CholQR2 and the Ritz vectors
+// run in double-float arithmetic on the FP32 pipe (df.cuh); norms, the
+// Rayleigh-Ritz solve and the true residuals are FP64.
 //
 // One cooperative kernel runs the whole solve for all problems. Its CTAs are
-// split into groups; a group owns one problem at a time (several small
-// problems are queued on one group when there are more problems than CTAs)
-// and synchronises through a bounded barrier in global memory. Within a
-// group the rows of the problem are split by SELL-32 slices.
+// split into groups (batch_layout: large problems get several CTAs, small
+// ones share one-CTA groups and are solved one after another), and a group
+// synchronises through a bounded barrier in global memory. Within a group
+// the rows of the problem are split by SELL-32 slices.
 //
 // Per problem, with Krylov blocks V_j stored row-interleaved ([D][4], so the
 // SpMV gathers one 32-byte sector per element for all four columns):
