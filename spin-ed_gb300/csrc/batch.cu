@@ -56,9 +56,9 @@ constexpr uint64_t kGsWaitNs = 1000000000ull;  // default bound on a wait for on
 constexpr uint64_t kBarrierNs = 20000000000ull;  // default: 20 s per barrier, far beyond any phase
 // Part of a block step that more CTAs do not shorten, in rows of the mean
 // work per row (the group layout's model). Fitted on 128 J1-J2 chains
-// (N = 16..28, one group per chain): a block step took 1.62 ms plus 0.249 us
-// per row of the CTA's share, i.e. about 6500 rows.
-constexpr double kLayoutFixedRows = 6500.0;
+// (N = 16..28, problems alone in their groups): a block step took 0.25 ms
+// plus 0.18 us per row of the CTA's share, i.e. about 1400 rows.
+constexpr double kLayoutFixedRows = 1400.0;
 constexpr size_t kStatsOff = 12 * 8;                // per-problem output record: out[12], stats[4], flag[4], prof[8]
 constexpr size_t kProfOff = kStatsOff + 32;
 constexpr size_t kOutBytes = kProfOff + 64;

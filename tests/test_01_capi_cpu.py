@@ -220,7 +220,7 @@ def test_batched_layout(sed, count, grid):
     D = [sizes[int(n)] for n in rng.choice(np.arange(16, 29, 2), size=count)]
     work = [float(d) * 100.0 for d in D]
     max_ctas = [(d + 31) // 32 for d in D]
-    fixed = 6500.0 * 100.0
+    fixed = 1400.0 * 100.0
     ng, group_of, ncta, nprob = _layout(lib, work, max_ctas, fixed, grid)
     assert 1 <= ng <= grid
     assert sum(ncta) <= grid
