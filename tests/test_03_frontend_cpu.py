@@ -166,3 +166,37 @@ def test_hdf5_rejects_garbage(tmp_path):
     p.write_bytes(b"not hdf5 at all")
     with pytest.raises(H.H5Error):
         H.read(str(p))
+
+
+def test_square_patches_are_translation_covariant():
+    """The patch table of the size-independent network (spined/lattices.py):
+    row i lists the (2r+1)^2 sites around site i in a fixed offset order, so
+    translating the lattice translates every patch; the same offsets on any L."""
+    from spined import lattices as LT
+    for L in (4, 6):
+        P = LT.square_patches(L)
+        assert P.shape == (L * L, 9) and P.dtype == np.uint16
+        tx = LT.square_symmetries(L)[0]  # x -> x + 1
+        for i in range(L * L):
+            assert P[i, 4] == i  # the centre
+            assert sorted(set(P[i].tolist())) == sorted(P[i].tolist())  # nine distinct sites
+            assert [tx[s] for s in P[i]] == P[tx[i]].tolist()
+    # the offsets are the same on both sizes: (dx, dy) of column k
+    for L in (4, 6):
+        P = LT.square_patches(L)
+        off = [(int(s) % L, int(s) // L) for s in P[0]]  # (x, y) of the patch of site (0, 0)
+        assert off == [(dx % L, dy % L) for dy in (-1, 0, 1) for dx in (-1, 0, 1)]
+
+
+def test_j1j2_chain_workload_is_seeded():
+    """The batched workload (128 J1-J2 chains): deterministic for a seed, N even in 16..28,
+    J2/J1 in [0, 0.6], and the sublattice mask of a ring marks every other site."""
+    from spined import lattices as LT
+    a = LT.j1j2_chains(128, seed=2024)
+    b = LT.j1j2_chains(128, seed=2024)
+    assert [(m.number_spins, m.meta["j2"]) for m in a] == [(m.number_spins, m.meta["j2"]) for m in b]
+    assert all(m.number_spins % 2 == 0 and 16 <= m.number_spins <= 28 for m in a)
+    assert all(0.0 <= m.meta["j2"] <= 0.6 for m in a)
+    assert {m.number_spins for m in a} == set(range(16, 29, 2))
+    assert LT.chain_sublattice_mask(6) == 0b010101
+    assert bin(LT.square_sublattice_mask(4)).count("1") == 8
